@@ -1,0 +1,188 @@
+/*
+ * mpm.h -- C ABI of libmpm.so, a GB300 (sm_103a) MLS-MPM fluid solver that
+ * drops in for WebGPU-Ocean's MLSMPMSimulator (mls-mpm/mls-mpm.ts:12-276).
+ *
+ * Conventions
+ *   - Every function returns MPM_OK (0) or a negative MPM_E_* code; no C++
+ *     exception crosses the ABI.  mpm_last_error() gives a message for the
+ *     last failing call on the calling thread.
+ *   - The library owns its device state; handles are opaque.  A handle lives
+ *     on the CUDA device that was current when it was created; every call
+ *     switches to that device and restores the caller's device on return.
+ *   - One handle serves one host thread at a time (the reference runs on a
+ *     single-threaded JS event loop).  Calls that take a `stream` enqueue
+ *     work on that cudaStream_t (NULL = the legacy default stream) and return
+ *     without waiting, like WebGPU command submission.
+ *   - Layouts are the reference's own:
+ *       particle  80 B = pos vec3f @0, v vec3f @16, C mat3x3f @32 (three
+ *                 16-byte columns)          mls-mpm/mls-mpm.ts:10,204-209
+ *       cell      16 B = i32 vx, vy, vz, mass  mls-mpm/p2g_1.wgsl:6-11
+ *       posvel    32 B = pos vec3f @0, v vec3f @16  copyPosition.wgsl:7-10
+ */
+#ifndef GB300_MPM_H
+#define GB300_MPM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mpm_sim mpm_sim;
+
+/* Pipeline override constants, mls-mpm/mls-mpm.ts:53-59. */
+typedef struct mpm_params {
+    float stiffness;              /* 3.0  */
+    float rest_density;           /* 4.0  */
+    float dynamic_viscosity;      /* 0.1  */
+    float dt;                     /* 0.2  */
+    float fixed_point_multiplier; /* 1e7  */
+} mpm_params;
+
+enum {
+    MPM_OK = 0,
+    MPM_E_INVALID = -1,       /* null handle or pointer, negative size, bad enum */
+    MPM_E_CAPACITY = -2,      /* more particles than max_particles */
+    MPM_E_GRID_CAPACITY = -3, /* gridCount > max grid (mls-mpm/mls-mpm.ts:230-232) */
+    MPM_E_CUDA = -4,          /* a CUDA runtime call failed */
+    MPM_E_NO_DEVICE = -5,     /* no CUDA device */
+    MPM_E_STATE = -6,         /* no scene loaded yet */
+    MPM_E_NONFINITE = -7      /* watchdog: non-finite particle state */
+};
+
+/* Engines.  Both give bit-identical results. */
+enum {
+    MPM_ENGINE_SORTED = 0,   /* default: binned particles, fused stages */
+    MPM_ENGINE_DISPATCH = 1  /* one kernel per WGSL entry point, as the reference */
+};
+
+/* The six WGSL entry points, in the order execute() dispatches them
+ * (mls-mpm/mls-mpm.ts:248-265). */
+enum {
+    MPM_KERNEL_CLEAR_GRID = 0,    /* mls-mpm/clearGrid.wgsl:10    */
+    MPM_KERNEL_P2G_1 = 1,         /* mls-mpm/p2g_1.wgsl:24        */
+    MPM_KERNEL_P2G_2 = 2,         /* mls-mpm/p2g_2.wgsl:30        */
+    MPM_KERNEL_UPDATE_GRID = 3,   /* mls-mpm/updateGrid.wgsl:23   */
+    MPM_KERNEL_G2P = 4,           /* mls-mpm/g2p.wgsl:26          */
+    MPM_KERNEL_COPY_POSITION = 5  /* mls-mpm/copyPosition.wgsl:15 */
+};
+
+/* Fills the reference's constants (mls-mpm/mls-mpm.ts:53-59). */
+void mpm_default_params(mpm_params* out);
+
+/*
+ * Replaces `new MLSMPMSimulator(particleBuffer, posvelBuffer, renderDiameter,
+ * device)` (mls-mpm/mls-mpm.ts:42-193).  `params` NULL = the reference's
+ * constants.  The grid capacity generalises the fixed 64^3 cell buffer
+ * (mls-mpm.ts:13-15,122-130); `max_particles` generalises numParticlesMax
+ * (common.ts:11).  `posvel_device` is the caller-owned posvelBuffer
+ * (main.ts:115-119): a device pointer of at least 32*max_particles bytes
+ * (`posvel_bytes`), or NULL to let the library allocate it.  The particle
+ * state itself is library-owned (mpm_download_particles gives it back in the
+ * 80-byte layout).  `render_diameter` is kept for the renderer hand-off
+ * (reset() copies it to sphere_size, mls-mpm.ts:226).
+ */
+int mpm_create(const mpm_params* params, int max_particles, int max_grid_x, int max_grid_y,
+               int max_grid_z, float render_diameter, void* posvel_device, size_t posvel_bytes,
+               mpm_sim** out);
+int mpm_destroy(mpm_sim* sim);
+
+/*
+ * Replaces reset(numParticles, initBoxSize) (mls-mpm/mls-mpm.ts:225-243):
+ * builds the dam-break block of initDambreak (mls-mpm.ts:195-223) with
+ * Math.random replaced by SplitMix64(seed), uploads it and sets both box
+ * uniforms to init_box.  init_box is given in doubles because the reference's
+ * loop bounds are JS numbers.  Returns MPM_E_GRID_CAPACITY (the reference's
+ * throw) when ceil(X)*ceil(Y)*ceil(Z) exceeds the grid capacity.
+ */
+int mpm_reset_dambreak(mpm_sim* sim, int num_particles, const double init_box[3],
+                       uint64_t seed);
+
+/* Loads n particles in the reference's 80-byte layout (host memory) and sets
+ * both box uniforms to init_box (the writeBuffer calls of mls-mpm.ts:239-241). */
+int mpm_upload(mpm_sim* sim, const float* particles_aos80, int n, const float init_box[3]);
+
+/* Replaces execute(commandEncoder) (mls-mpm/mls-mpm.ts:245-268): enqueues
+ * `substeps` substeps (the reference runs 2) on `stream`; ends with posvel
+ * holding the particles' positions and velocities. */
+int mpm_step(mpm_sim* sim, int substeps, void* stream);
+
+/* Replaces changeBoxSize(realBoxSize) (mls-mpm/mls-mpm.ts:270-275).  Takes
+ * effect for work enqueued after the call. */
+int mpm_set_real_box(mpm_sim* sim, const float real_box[3]);
+
+/* The numParticles and gridCount fields (mls-mpm/mls-mpm.ts:19-20). */
+int mpm_num_particles(const mpm_sim* sim);
+int64_t mpm_grid_count(const mpm_sim* sim);
+float mpm_render_diameter(const mpm_sim* sim);
+
+/* posvelBuffer (main.ts:115-119): device pointer, 32 B per particle. */
+void* mpm_posvel_device_ptr(mpm_sim* sim);
+
+/* Synchronous copies back to host memory (for parity checks and tools). */
+int mpm_download_particles(mpm_sim* sim, float* out_aos80);
+int mpm_download_grid(mpm_sim* sim, int32_t* out_cells);
+/* Asynchronous on `stream`: copies n*32 B of posvel into host memory
+ * (pinned memory makes it truly asynchronous). */
+int mpm_download_posvel(mpm_sim* sim, float* out_posvel, void* stream);
+
+/* Enqueues one WGSL entry point alone (mls-mpm/mls-mpm.ts:248-265) on the
+ * dispatch engine's state.  Running the six in order equals one substep. */
+int mpm_dispatch(mpm_sim* sim, int kernel, void* stream);
+
+int mpm_set_engine(mpm_sim* sim, int engine);
+int mpm_get_engine(const mpm_sim* sim);
+
+/* Waits for all work of the handle (its streams and the legacy stream). */
+int mpm_synchronize(mpm_sim* sim);
+
+/* Watchdog (the reference only reports device loss, main.ts:185-188):
+ * counts non-finite particle records and grid accesses that fell outside
+ * [0, gridCount) since the last reset.  Synchronous. */
+typedef struct mpm_health {
+    int64_t nonfinite_particles;
+    int64_t out_of_range_accesses;
+} mpm_health;
+int mpm_check_health(mpm_sim* sim, mpm_health* out);
+
+/* Launch accounting (the reference only times JS encoding with
+ * performance.now(), main.ts:209,278).  mpm_set_profiling(1) starts
+ * bracketing every kernel with CUDA events on its launch stream and resets
+ * the counters; mpm_kernel_stats waits for those events and fills up to
+ * max_entries records, returning how many kernels have records.
+ * mpm_launch_count is the number of kernels this handle has launched. */
+typedef struct mpm_kernel_stat {
+    const char* name;
+    int64_t launches;
+    int64_t timed_launches;
+    double total_ms;
+} mpm_kernel_stat;
+int mpm_set_profiling(mpm_sim* sim, int enable);
+int mpm_kernel_stats(mpm_sim* sim, mpm_kernel_stat* out, int max_entries);
+int64_t mpm_launch_count(const mpm_sim* sim);
+
+const char* mpm_error_string(int code);
+const char* mpm_last_error(void);
+
+/* Host-only scene builders (no GPU).  Each returns the particle count or a
+ * negative code.
+ * mpm_scene_dambreak: initDambreak (mls-mpm/mls-mpm.ts:195-223) with
+ *   Math.random -> SplitMix64(seed); writes at most max_particles records.
+ * mpm_scene_lattice: jittered cubic lattice, particle (ix,iy,iz) x-major at
+ *   origin + spacing*i plus per-component jitter U[-jitter, jitter). */
+int mpm_scene_dambreak(float* out_aos80, int max_particles, const double init_box[3],
+                       uint64_t seed);
+int mpm_scene_lattice(float* out_aos80, int n_per_axis, double origin, double spacing,
+                      double jitter, uint64_t seed);
+
+/* Diagnostic: evaluates the fixed-point conversions on the device.
+ * enc_out[i] = i32(in[i] * fm) (p2g_1.wgsl:15-17), dec_out[i] =
+ * f32(bits(in[i])) / fm (p2g_2.wgsl:22-24).  Synchronous, host arrays. */
+int mpm_probe_conversions(const float* in, int n, float fm, int32_t* enc_out, float* dec_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GB300_MPM_H */

@@ -1,0 +1,170 @@
+"""ctypes front end of the C oracle (oracle/mpm_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py (cpu_baseline leg and `--impl reference`) as the checker or the
+CPU baseline.  The product never imports it.
+
+Arrays use the reference's layouts: particles (n, 20) float32 (80 B each,
+mls-mpm/mls-mpm.ts:10), cells (grid_count, 4) int32 {vx, vy, vz, mass}
+(mls-mpm/p2g_1.wgsl:6-11), posvel (n, 8) float32 (copyPosition.wgsl:7-10).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "build")
+LIB_PATH = os.path.join(BUILD_DIR, "libmpm_oracle.so")
+SOURCES = [os.path.join(HERE, "mpm_oracle.c")]
+
+# -ffp-contract=off: every float op rounds separately, as the WGSL restatement
+# requires; no -ffast-math (keeps IEEE division, NaN and denormal semantics).
+CFLAGS = ["-O2", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+          "-pthread"]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle into oracle/build/libmpm_oracle.so."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    newest = max(os.path.getmtime(s) for s in SOURCES)
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
+        return LIB_PATH
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    subprocess.check_call(["gcc", *CFLAGS, "-o", tmp, *SOURCES, "-lm"])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+class Params(ctypes.Structure):
+    """orc_params; defaults are mls-mpm/mls-mpm.ts:53-59."""
+    _fields_ = [
+        ("stiffness", ctypes.c_float),
+        ("rest_density", ctypes.c_float),
+        ("dynamic_viscosity", ctypes.c_float),
+        ("dt", ctypes.c_float),
+        ("fixed_point_multiplier", ctypes.c_float),
+    ]
+
+    @classmethod
+    def reference(cls) -> "Params":
+        return cls(3.0, 4.0, 0.1, 0.2, 1e7)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build()
+        L = ctypes.CDLL(path)
+        f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+        i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+        box = ctypes.POINTER(ctypes.c_float)
+        prm = ctypes.POINTER(Params)
+        i64 = ctypes.c_int64
+        L.orc_grid_count.argtypes = [box]
+        L.orc_grid_count.restype = i64
+        L.orc_clear_grid.argtypes = [i32p, i64]
+        L.orc_p2g_1.argtypes = [f32p, i64, i32p, i64, box, prm]
+        L.orc_p2g_1.restype = i64
+        L.orc_p2g_2.argtypes = [f32p, i64, i32p, i64, box, prm]
+        L.orc_p2g_2.restype = i64
+        L.orc_update_grid.argtypes = [i32p, i64, box, box, prm]
+        L.orc_g2p.argtypes = [f32p, i64, i32p, i64, box, box, prm]
+        L.orc_g2p.restype = i64
+        L.orc_copy_position.argtypes = [f32p, i64, f32p]
+        L.orc_execute.argtypes = [f32p, i64, i32p, i64, box, box, prm, ctypes.c_void_p,
+                                  ctypes.c_int, ctypes.c_int]
+        L.orc_execute.restype = i64
+        L.orc_enc.argtypes = [ctypes.c_float, ctypes.c_float]
+        L.orc_enc.restype = ctypes.c_int32
+        L.orc_dec.argtypes = [ctypes.c_int32, ctypes.c_float]
+        L.orc_dec.restype = ctypes.c_float
+        _lib = L
+    return _lib
+
+
+def _box(b) -> ctypes.Array:
+    return (ctypes.c_float * 3)(*[float(np.float32(x)) for x in b])
+
+
+def grid_count(init_box) -> int:
+    return int(lib().orc_grid_count(_box(init_box)))
+
+
+class OracleSim:
+    """CPU mirror of MLSMPMSimulator's state (mls-mpm/mls-mpm.ts:12-276)."""
+
+    def __init__(self, particles: np.ndarray, init_box, params: Params | None = None,
+                 real_box=None):
+        self.params = params or Params.reference()
+        self.particles = np.ascontiguousarray(particles, dtype=np.float32).reshape(-1, 20).copy()
+        self.init_box = [float(np.float32(x)) for x in init_box]
+        self.real_box = list(self.init_box if real_box is None else
+                             [float(np.float32(x)) for x in real_box])
+        self.grid_count = grid_count(self.init_box)
+        self.cells = np.zeros((self.grid_count, 4), dtype=np.int32)
+        self.posvel = np.zeros((len(self.particles), 8), dtype=np.float32)
+        self.oob = 0
+
+    @property
+    def n(self) -> int:
+        return len(self.particles)
+
+    def change_box_size(self, real_box):
+        self.real_box = [float(np.float32(x)) for x in real_box]
+
+    # one call per WGSL entry point
+    def clear_grid(self):
+        lib().orc_clear_grid(self.cells, self.grid_count)
+
+    def p2g_1(self):
+        self.oob += lib().orc_p2g_1(self.particles, self.n, self.cells, self.grid_count,
+                                    _box(self.init_box), ctypes.byref(self.params))
+
+    def p2g_2(self):
+        self.oob += lib().orc_p2g_2(self.particles, self.n, self.cells, self.grid_count,
+                                    _box(self.init_box), ctypes.byref(self.params))
+
+    def update_grid(self):
+        lib().orc_update_grid(self.cells, self.grid_count, _box(self.real_box),
+                              _box(self.init_box), ctypes.byref(self.params))
+
+    def g2p(self):
+        self.oob += lib().orc_g2p(self.particles, self.n, self.cells, self.grid_count,
+                                  _box(self.real_box), _box(self.init_box),
+                                  ctypes.byref(self.params))
+
+    def copy_position(self):
+        lib().orc_copy_position(self.particles, self.n, self.posvel)
+
+    def substep(self):
+        self.clear_grid()
+        self.p2g_1()
+        self.p2g_2()
+        self.update_grid()
+        self.g2p()
+        self.copy_position()
+
+    def execute(self, substeps: int = 2, nthreads: int = 1):
+        """mls-mpm/mls-mpm.ts:245-268 (2 substeps per call by default)."""
+        r = lib().orc_execute(self.particles, self.n, self.cells, self.grid_count,
+                              _box(self.real_box), _box(self.init_box),
+                              ctypes.byref(self.params),
+                              self.posvel.ctypes.data_as(ctypes.c_void_p), substeps, nthreads)
+        if r < 0:
+            raise RuntimeError("oracle thread error")
+        self.oob += r
+
+
+def enc(f: float, fm: float = 1e7) -> int:
+    return int(lib().orc_enc(f, fm))
+
+
+def dec(i: int, fm: float = 1e7) -> float:
+    return float(lib().orc_dec(i, fm))

@@ -1,0 +1,73 @@
+"""The C ABI without a GPU: the library loads, exports every function that
+include/mpm.h declares, and its host-only scene builders match the oracle's
+restatements bit for bit."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from helpers import assert_bits_equal
+
+
+def test_exports_every_declared_symbol(pkg):
+    lib = pkg._lib.load()
+    declared = pkg._lib.declared_functions()
+    assert len(declared) >= 20
+    missing = [name for name in declared if not hasattr(lib, name)]
+    assert not missing, f"not exported: {missing}"
+
+
+def test_error_strings(pkg):
+    lib = pkg._lib.load()
+    assert lib.mpm_error_string(pkg._lib.MPM_E_GRID_CAPACITY) == \
+        b"gridCount should be equal to or less than maxGridCount"
+    assert lib.mpm_error_string(0) == b"ok"
+
+
+def test_null_handles_are_rejected(pkg):
+    lib = pkg._lib.load()
+    assert lib.mpm_step(None, 2, None) == pkg._lib.MPM_E_INVALID
+    assert lib.mpm_set_real_box(None, None) == pkg._lib.MPM_E_INVALID
+    assert lib.mpm_num_particles(None) == 0
+    assert lib.mpm_destroy(None) == 0
+
+
+def test_default_params_are_the_reference_constants(pkg):
+    p = pkg.default_params()
+    assert (p.stiffness, p.rest_density, p.dt) == (3.0, 4.0, np.float32(0.2))
+    assert np.float32(p.dynamic_viscosity) == np.float32(0.1)
+    assert p.fixed_point_multiplier == 1e7
+
+
+@pytest.mark.parametrize("box,n,seed", [
+    ([40, 30, 60], 70000, 0),      # main.ts:128-129 defaults
+    ([35, 25, 55], 40000, 1),
+    ([50, 50, 80], 200000, 2),
+    ([45.5, 40.25, 80.75], 120000, 3),
+    ([12, 10, 14], 10**6, 4),       # fewer lattice sites than asked
+])
+def test_dambreak_scene_matches_restatement(pkg, box, n, seed):
+    from oracle import scene
+    got = pkg.scene_dambreak(box, n, seed)
+    want = scene.dambreak(box, n, seed)
+    assert_bits_equal(got, want, f"initDambreak {box} n={n}")
+
+
+def test_lattice_scene_matches_restatement(pkg):
+    from oracle import scene
+    got = pkg.scene_lattice(12, 3.0, 0.5, 0.05, 2024)
+    want = scene.lattice(12, 3.0, 0.5, 0.05, 2024)
+    assert_bits_equal(got, want, "lattice")
+    assert got.shape == (12 ** 3, 20)
+    assert np.all(np.abs(got[:, 0:3] - np.round((got[:, 0:3] - 3.0) / 0.5) * 0.5 - 3.0) <= 0.0501)
+
+
+def test_no_device_is_reported_not_faked(pkg):
+    """Without a GPU, creating a simulator fails loudly (no CPU fallback)."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(pkg.MPMError, match="no CUDA device"):
+        pkg.MLSMPMSimulator(None, None, 1.2)

@@ -1,0 +1,14 @@
+"""GB300-native MLS-MPM solver: a drop-in for WebGPU-Ocean's MLSMPMSimulator
+(mls-mpm/mls-mpm.ts).  The compute path is libmpm.so (csrc/, C ABI in
+include/mpm.h); this package is its Python host mirror.
+
+The directory name is not a Python identifier; load it with
+`load_package()` from the repository root helpers, which registers it as
+`webgpu_ocean_gb300`.
+"""
+from . import _lib, build
+from .mlsmpm import (MLSMPMSimulator, MPMError, GridCapacityError, default_params,
+                     probe_conversions, scene_dambreak, scene_lattice)
+
+__all__ = ["MLSMPMSimulator", "MPMError", "GridCapacityError", "default_params",
+           "scene_dambreak", "scene_lattice", "probe_conversions", "build", "_lib"]

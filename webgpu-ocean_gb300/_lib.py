@@ -1,0 +1,118 @@
+"""ctypes bindings of libmpm.so (declarations: include/mpm.h).
+
+The library is built in-tree by build.py.  Loading never falls back to
+anything else: if libmpm.so is missing or fails to load, the import error
+propagates.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+from . import build as _build
+
+HEADER = os.path.join(_build.INCLUDE, "mpm.h")
+
+MPM_OK = 0
+MPM_E_INVALID = -1
+MPM_E_CAPACITY = -2
+MPM_E_GRID_CAPACITY = -3
+MPM_E_CUDA = -4
+MPM_E_NO_DEVICE = -5
+MPM_E_STATE = -6
+MPM_E_NONFINITE = -7
+
+MPM_ENGINE_SORTED = 0
+MPM_ENGINE_DISPATCH = 1
+
+KERNELS = {
+    "clearGrid": 0,
+    "p2g_1": 1,
+    "p2g_2": 2,
+    "updateGrid": 3,
+    "g2p": 4,
+    "copyPosition": 5,
+}
+
+
+class Params(ctypes.Structure):
+    """mpm_params: the pipeline override constants (mls-mpm/mls-mpm.ts:53-59)."""
+    _fields_ = [
+        ("stiffness", ctypes.c_float),
+        ("rest_density", ctypes.c_float),
+        ("dynamic_viscosity", ctypes.c_float),
+        ("dt", ctypes.c_float),
+        ("fixed_point_multiplier", ctypes.c_float),
+    ]
+
+
+class KernelStat(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char_p), ("launches", ctypes.c_int64),
+                ("timed_launches", ctypes.c_int64), ("total_ms", ctypes.c_double)]
+
+
+class Health(ctypes.Structure):
+    _fields_ = [("nonfinite_particles", ctypes.c_int64),
+                ("out_of_range_accesses", ctypes.c_int64)]
+
+
+_lib = None
+
+
+def declared_functions() -> list[str]:
+    """Names of every function include/mpm.h declares."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mpm_[a-z0-9_]+)\s*\(", text)))
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if build_if_missing:
+        path = _build.build()
+    if not os.path.exists(path):
+        raise ImportError(f"libmpm.so not built ({path}); run build()")
+    L = ctypes.CDLL(path)
+    vp, i32, i64, f32 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_float
+    fp, dp, ip = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int32)
+    sig = {
+        "mpm_default_params": (None, [ctypes.POINTER(Params)]),
+        "mpm_create": (i32, [ctypes.POINTER(Params), i32, i32, i32, i32, f32, vp, ctypes.c_size_t,
+                             ctypes.POINTER(vp)]),
+        "mpm_destroy": (i32, [vp]),
+        "mpm_reset_dambreak": (i32, [vp, i32, dp, ctypes.c_uint64]),
+        "mpm_upload": (i32, [vp, fp, i32, fp]),
+        "mpm_step": (i32, [vp, i32, vp]),
+        "mpm_set_real_box": (i32, [vp, fp]),
+        "mpm_num_particles": (i32, [vp]),
+        "mpm_grid_count": (i64, [vp]),
+        "mpm_render_diameter": (f32, [vp]),
+        "mpm_posvel_device_ptr": (vp, [vp]),
+        "mpm_download_particles": (i32, [vp, fp]),
+        "mpm_download_grid": (i32, [vp, ip]),
+        "mpm_download_posvel": (i32, [vp, fp, vp]),
+        "mpm_dispatch": (i32, [vp, i32, vp]),
+        "mpm_set_engine": (i32, [vp, i32]),
+        "mpm_get_engine": (i32, [vp]),
+        "mpm_synchronize": (i32, [vp]),
+        "mpm_check_health": (i32, [vp, ctypes.POINTER(Health)]),
+        "mpm_error_string": (ctypes.c_char_p, [i32]),
+        "mpm_last_error": (ctypes.c_char_p, []),
+        "mpm_scene_dambreak": (i32, [fp, i32, dp, ctypes.c_uint64]),
+        "mpm_scene_lattice": (i32, [fp, i32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_uint64]),
+        "mpm_probe_conversions": (i32, [fp, i32, f32, ip, fp]),
+        "mpm_set_profiling": (i32, [vp, i32]),
+        "mpm_kernel_stats": (i32, [vp, ctypes.POINTER(KernelStat), i32]),
+        "mpm_launch_count": (i64, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L

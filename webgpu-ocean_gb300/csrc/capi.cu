@@ -1,0 +1,590 @@
+// capi.cu -- the C ABI of libmpm.so (include/mpm.h): simulator handle,
+// device memory, scene builders and the per-frame stage sequencing of
+// MLSMPMSimulator (mls-mpm/mls-mpm.ts:12-276).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/mpm.h"
+#include "mpm_internal.h"
+#include "sorted_engine.h"
+
+using namespace mpm;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(MPM_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define MPM_CUDA(call)                                   \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+// Switches to the handle's device for the duration of a call.
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) { ok = false; return; }
+        if (prev != dev && cudaSetDevice(dev) != cudaSuccess) ok = false;
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Scene builders (host).  Doubles throughout, as JS numbers; this file is
+// compiled with -ffp-contract=off so each double operation rounds alone.
+// ---------------------------------------------------------------------------
+
+struct SplitMix64 {
+    uint64_t s;
+    explicit SplitMix64(uint64_t seed) : s(seed) {}
+    uint64_t next() {
+        s += 0x9E3779B97F4A7C15ull;
+        uint64_t z = s;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    double random() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+};
+
+// initDambreak, mls-mpm/mls-mpm.ts:195-223.
+int scene_dambreak(float* out, int max_particles, const double box[3], uint64_t seed) {
+    SplitMix64 rng(seed);
+    const double spacing = 0.65;
+    int n = 0;
+    for (double j = 0; j < box[1] * 0.80 && n < max_particles; j += spacing) {
+        for (double i = 3; i < box[0] - 4 && n < max_particles; i += spacing) {
+            for (double k = 3; k < box[2] / 2 && n < max_particles; k += spacing) {
+                const double jitter = 2.0 * rng.random();
+                float* P = out + 20 * (size_t)n;
+                std::memset(P, 0, 80);
+                P[0] = (float)(i + jitter);
+                P[1] = (float)(j + jitter);
+                P[2] = (float)(k + jitter);
+                ++n;
+            }
+        }
+    }
+    return n;
+}
+
+int scene_lattice(float* out, int npa, double origin, double spacing, double jitter,
+                  uint64_t seed) {
+    SplitMix64 rng(seed);
+    size_t p = 0;
+    for (int ix = 0; ix < npa; ++ix)
+        for (int iy = 0; iy < npa; ++iy)
+            for (int iz = 0; iz < npa; ++iz) {
+                float* P = out + 20 * p;
+                std::memset(P, 0, 80);
+                const int idx[3] = {ix, iy, iz};
+                for (int a = 0; a < 3; ++a) {
+                    const double u = rng.random();
+                    const double x = (origin + spacing * (double)idx[a]) + jitter * (2.0 * u - 1.0);
+                    P[a] = (float)x;
+                }
+                ++p;
+            }
+    return (int)p;
+}
+
+// Reference 80-byte records <-> the library's four float4 streams.
+void aos80_to_soa(const float* in, int n, std::vector<float4> q[4]) {
+    for (int k = 0; k < 4; ++k) q[k].resize((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const float* P = in + 20 * (size_t)i;
+        // C[c][r] = P[8 + 4c + r]
+        q[0][i] = make_float4(P[0], P[1], P[2], P[8]);
+        q[1][i] = make_float4(P[9], P[10], P[12], P[13]);
+        q[2][i] = make_float4(P[14], P[16], P[17], P[18]);
+        q[3][i] = make_float4(P[4], P[5], P[6], 0.0f);
+    }
+}
+
+void soa_to_aos80(const std::vector<float4> q[4], int n, float* out) {
+    for (int i = 0; i < n; ++i) {
+        float* P = out + 20 * (size_t)i;
+        std::memset(P, 0, 80);
+        const float4 a = q[0][i], b = q[1][i], c = q[2][i], d = q[3][i];
+        P[0] = a.x; P[1] = a.y; P[2] = a.z;
+        P[4] = d.x; P[5] = d.y; P[6] = d.z;
+        P[8] = a.w; P[9] = b.x; P[10] = b.y;
+        P[12] = b.z; P[13] = b.w; P[14] = c.x;
+        P[16] = c.y; P[17] = c.z; P[18] = c.w;
+    }
+}
+
+int f2i_trunc_sat(float x) {
+    if (x != x) return 0;
+    if (x >= 2147483648.0f) return INT32_MAX;
+    if (x <= -2147483648.0f) return INT32_MIN;
+    return (int)x;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// The handle
+// ---------------------------------------------------------------------------
+
+struct mpm_sim {
+    int device = 0;
+    mpm_params params{};
+    int max_particles = 0;
+    long long max_cells = 0;
+    float render_diameter = 0.f;
+
+    int n = 0;
+    long long grid_count = 0;
+    float init_box[3] = {0, 0, 0};
+    float real_box[3] = {0, 0, 0};
+    bool loaded = false;
+
+    Particles P{};
+    // The reference's cell buffer (x-major, mls-mpm.ts:126-130): the dispatch
+    // engine works in it; the sorted engine exports into it on demand.
+    int4* grid_ref = nullptr;
+    bool ref_current = true;   // false: the sorted engine holds the newest grid
+    bool sorted_ok = false;    // the sorted engine can run this scene
+    float4* posvel = nullptr;
+    bool posvel_owned = false;
+    unsigned long long* counters = nullptr;  // [0] out-of-range, [1] non-finite scratch
+
+    int engine = MPM_ENGINE_DISPATCH;
+    SortedEngine* sorted = nullptr;
+    cudaStream_t internal = nullptr;
+    LaunchProfiler prof;
+
+    SimConsts consts() const {
+        SimConsts k{};
+        k.stiffness = params.stiffness;
+        k.rest_density = params.rest_density;
+        k.dynamic_viscosity = params.dynamic_viscosity;
+        k.dt = params.dt;
+        k.fm = params.fixed_point_multiplier;
+        for (int a = 0; a < 3; ++a) {
+            k.init_box[a] = init_box[a];
+            k.real_box[a] = real_box[a];
+        }
+        k.Y = f2i_trunc_sat(init_box[1]);
+        k.Z = f2i_trunc_sat(init_box[2]);
+        k.grid_count = (int)grid_count;
+        k.n = n;
+        return k;
+    }
+};
+
+namespace {
+
+int check_sim(const mpm_sim* s) {
+    if (!s) return fail(MPM_E_INVALID, "null simulator handle");
+    return MPM_OK;
+}
+
+// mls-mpm.ts:229 gridCount = ceil(X) * ceil(Y) * ceil(Z)
+long long grid_count_of(const float b[3]) {
+    return (long long)std::ceil((double)b[0]) * (long long)std::ceil((double)b[1]) *
+           (long long)std::ceil((double)b[2]);
+}
+
+int load_particles(mpm_sim* s, const float* aos80, int n, const float init_box[3]) {
+    if (n < 0) return fail(MPM_E_INVALID, "negative particle count");
+    if (n > s->max_particles)
+        return fail(MPM_E_CAPACITY, "numParticles exceeds the particle capacity");
+    for (int a = 0; a < 3; ++a)
+        if (!(init_box[a] >= 0.f) || !std::isfinite(init_box[a]))
+            return fail(MPM_E_INVALID, "init box size must be finite and non-negative");
+    const long long gc = grid_count_of(init_box);
+    if (gc > s->max_cells)
+        return fail(MPM_E_GRID_CAPACITY, "gridCount should be equal to or less than maxGridCount");
+    if (gc > 0x7fffffffLL) return fail(MPM_E_GRID_CAPACITY, "gridCount exceeds the i32 index range");
+    DeviceGuard g(s->device);
+    if (!g.ok) return fail(MPM_E_CUDA, "cannot select the simulator's device");
+    MPM_CUDA(cudaDeviceSynchronize());
+    std::vector<float4> q[4];
+    aos80_to_soa(aos80, n, q);
+    float4* dst[4] = {s->P.p0, s->P.p1, s->P.p2, s->P.p3};
+    for (int k = 0; k < 4; ++k)
+        if (n) MPM_CUDA(cudaMemcpy(dst[k], q[k].data(), sizeof(float4) * (size_t)n,
+                                   cudaMemcpyHostToDevice));
+    s->n = n;
+    s->grid_count = gc;
+    for (int a = 0; a < 3; ++a) s->init_box[a] = s->real_box[a] = init_box[a];
+    MPM_CUDA(cudaMemset(s->grid_ref, 0, sizeof(int4) * (size_t)s->max_cells));
+    MPM_CUDA(cudaMemset(s->counters, 0, sizeof(unsigned long long) * 2));
+    if (n) MPM_CUDA(cudaMemset(s->posvel, 0, sizeof(float4) * 2 * (size_t)n));
+    s->ref_current = true;
+    s->loaded = true;
+    sorted_invalidate(s->sorted);
+    s->sorted_ok = sorted_configure(s->sorted, s->consts()) == 0;
+    MPM_CUDA(cudaDeviceSynchronize());
+    return MPM_OK;
+}
+
+// Brings the reference-layout grid up to date (exports the sorted engine's
+// last grid, as updateGrid left it).
+int sync_ref_grid(mpm_sim* s, cudaStream_t st) {
+    if (s->ref_current) return MPM_OK;
+    if (sorted_has_grid(s->sorted)) {
+        if (sorted_export_grid(s->sorted, s->consts(), s->grid_ref, st, &s->prof) != 0)
+            return fail(MPM_E_CUDA, std::string("sorted engine: ") + sorted_error());
+    }
+    s->ref_current = true;
+    return MPM_OK;
+}
+
+// One reference substep on the dispatch engine (mls-mpm.ts:248-265).
+void dispatch_kernel(mpm_sim* s, int kernel, const SimConsts& k, cudaStream_t st) {
+    int4* cells = s->grid_ref;
+    s->prof.before(st);
+    switch (kernel) {
+        case MPM_KERNEL_CLEAR_GRID: launch_clear_grid(cells, k.grid_count, st); break;
+        case MPM_KERNEL_P2G_1: launch_p2g_1(s->P, cells, k, s->counters, st); break;
+        case MPM_KERNEL_P2G_2: launch_p2g_2(s->P, cells, k, s->counters, st); break;
+        case MPM_KERNEL_UPDATE_GRID: launch_update_grid(cells, k, st); break;
+        case MPM_KERNEL_G2P: launch_g2p(s->P, cells, k, s->counters, st); break;
+        case MPM_KERNEL_COPY_POSITION: launch_copy_position(s->P, s->posvel, k.n, st); break;
+    }
+    s->prof.after(kernel, st);  // MPM_KERNEL_* == KID_* for the six entry points
+}
+
+void dispatch_substep(mpm_sim* s, const SimConsts& k, cudaStream_t st) {
+    for (int kernel = MPM_KERNEL_CLEAR_GRID; kernel <= MPM_KERNEL_COPY_POSITION; ++kernel)
+        dispatch_kernel(s, kernel, k, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+void mpm_default_params(mpm_params* out) {
+    if (!out) return;
+    out->stiffness = 3.0f;
+    out->rest_density = 4.0f;
+    out->dynamic_viscosity = 0.1f;
+    out->dt = 0.2f;
+    out->fixed_point_multiplier = 1e7f;
+}
+
+int mpm_create(const mpm_params* params, int max_particles, int max_grid_x, int max_grid_y,
+               int max_grid_z, float render_diameter, void* posvel_device, size_t posvel_bytes,
+               mpm_sim** out) {
+    if (!out) return fail(MPM_E_INVALID, "out is null");
+    *out = nullptr;
+    if (max_particles < 0 || max_grid_x <= 0 || max_grid_y <= 0 || max_grid_z <= 0)
+        return fail(MPM_E_INVALID, "capacities must be positive");
+    const long long max_cells = (long long)max_grid_x * max_grid_y * max_grid_z;
+    if (max_cells > 0x7fffffffLL) return fail(MPM_E_INVALID, "grid capacity exceeds i32 indices");
+    if (posvel_device && posvel_bytes < (size_t)32 * (size_t)max_particles)
+        return fail(MPM_E_INVALID, "posvel buffer smaller than 32 * max_particles bytes");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(MPM_E_NO_DEVICE, "no CUDA device");
+    }
+    mpm_sim* s = new (std::nothrow) mpm_sim();
+    if (!s) return fail(MPM_E_INVALID, "out of host memory");
+    MPM_CUDA(cudaGetDevice(&s->device));
+    if (params) s->params = *params;
+    else mpm_default_params(&s->params);
+    s->max_particles = max_particles;
+    s->max_cells = max_cells;
+    s->render_diameter = render_diameter;
+    const size_t np = (size_t)(max_particles > 0 ? max_particles : 1);
+    cudaError_t e = cudaSuccess;
+    float4** ps[4] = {&s->P.p0, &s->P.p1, &s->P.p2, &s->P.p3};
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaMalloc(ps[k], sizeof(float4) * np);
+    if (e == cudaSuccess) e = cudaMalloc(&s->grid_ref, sizeof(int4) * (size_t)max_cells);
+    if (e == cudaSuccess) e = cudaMalloc(&s->counters, sizeof(unsigned long long) * 2);
+    if (e == cudaSuccess) {
+        if (posvel_device) {
+            s->posvel = static_cast<float4*>(posvel_device);
+        } else {
+            e = cudaMalloc(&s->posvel, sizeof(float4) * 2 * np);
+            s->posvel_owned = true;
+        }
+    }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->internal, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        e = cudaMemset(s->grid_ref, 0, sizeof(int4) * (size_t)max_cells);
+        if (e == cudaSuccess) e = cudaMemset(s->counters, 0, sizeof(unsigned long long) * 2);
+    }
+    if (e == cudaSuccess) {
+        int rc = sorted_create(&s->sorted, max_particles);
+        if (rc != 0) e = cudaErrorMemoryAllocation;
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        int rc = cuda_fail(e, "mpm_create");
+        mpm_destroy(s);
+        return rc;
+    }
+    s->engine = MPM_ENGINE_SORTED;
+    *out = s;
+    return MPM_OK;
+}
+
+int mpm_destroy(mpm_sim* s) {
+    if (!s) return MPM_OK;
+    DeviceGuard g(s->device);
+    cudaDeviceSynchronize();
+    cudaFree(s->P.p0);
+    cudaFree(s->P.p1);
+    cudaFree(s->P.p2);
+    cudaFree(s->P.p3);
+    cudaFree(s->grid_ref);
+    cudaFree(s->counters);
+    if (s->posvel_owned) cudaFree(s->posvel);
+    if (s->sorted) sorted_destroy(s->sorted);
+    if (s->internal) cudaStreamDestroy(s->internal);
+    s->prof.release();
+    delete s;
+    return MPM_OK;
+}
+
+int mpm_reset_dambreak(mpm_sim* s, int num_particles, const double init_box[3], uint64_t seed) {
+    if (int rc = check_sim(s)) return rc;
+    if (!init_box) return fail(MPM_E_INVALID, "init_box is null");
+    if (num_particles < 0) return fail(MPM_E_INVALID, "negative particle count");
+    if (num_particles > s->max_particles)
+        return fail(MPM_E_CAPACITY, "numParticles exceeds the particle capacity");
+    std::vector<float> buf((size_t)20 * (size_t)(num_particles > 0 ? num_particles : 1));
+    const int n = scene_dambreak(buf.data(), num_particles, init_box, seed);
+    const float box[3] = {(float)init_box[0], (float)init_box[1], (float)init_box[2]};
+    return load_particles(s, buf.data(), n, box);
+}
+
+int mpm_upload(mpm_sim* s, const float* aos80, int n, const float init_box[3]) {
+    if (int rc = check_sim(s)) return rc;
+    if (!init_box || (n > 0 && !aos80)) return fail(MPM_E_INVALID, "null pointer");
+    return load_particles(s, aos80, n, init_box);
+}
+
+int mpm_step(mpm_sim* s, int substeps, void* stream) {
+    if (int rc = check_sim(s)) return rc;
+    if (!s->loaded) return fail(MPM_E_STATE, "no scene loaded (call reset first)");
+    if (substeps < 0) return fail(MPM_E_INVALID, "negative substep count");
+    DeviceGuard g(s->device);
+    if (!g.ok) return fail(MPM_E_CUDA, "cannot select the simulator's device");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const SimConsts k = s->consts();
+    if (s->engine == MPM_ENGINE_DISPATCH || !s->sorted_ok) {
+        if (int rc = sync_ref_grid(s, st)) return rc;
+        for (int i = 0; i < substeps; ++i) dispatch_substep(s, k, st);
+        if (substeps > 0) sorted_invalidate(s->sorted);
+    } else if (substeps > 0) {
+        if (sorted_step(s->sorted, s->P, s->posvel, s->counters, k, substeps, st, &s->prof) != 0)
+            return fail(MPM_E_CUDA, std::string("sorted engine: ") + sorted_error());
+        s->ref_current = false;
+    }
+    MPM_CUDA(cudaGetLastError());
+    return MPM_OK;
+}
+
+int mpm_set_real_box(mpm_sim* s, const float real_box[3]) {
+    if (int rc = check_sim(s)) return rc;
+    if (!real_box) return fail(MPM_E_INVALID, "real_box is null");
+    for (int a = 0; a < 3; ++a) s->real_box[a] = real_box[a];
+    return MPM_OK;
+}
+
+int mpm_num_particles(const mpm_sim* s) { return s ? s->n : 0; }
+int64_t mpm_grid_count(const mpm_sim* s) { return s ? s->grid_count : 0; }
+float mpm_render_diameter(const mpm_sim* s) { return s ? s->render_diameter : 0.f; }
+void* mpm_posvel_device_ptr(mpm_sim* s) { return s ? s->posvel : nullptr; }
+
+int mpm_download_particles(mpm_sim* s, float* out) {
+    if (int rc = check_sim(s)) return rc;
+    if (!out && s->n) return fail(MPM_E_INVALID, "null output");
+    DeviceGuard g(s->device);
+    MPM_CUDA(cudaDeviceSynchronize());
+    std::vector<float4> q[4];
+    const float4* src[4] = {s->P.p0, s->P.p1, s->P.p2, s->P.p3};
+    for (int k = 0; k < 4; ++k) {
+        q[k].resize((size_t)s->n);
+        if (s->n)
+            MPM_CUDA(cudaMemcpy(q[k].data(), src[k], sizeof(float4) * (size_t)s->n,
+                                cudaMemcpyDeviceToHost));
+    }
+    soa_to_aos80(q, s->n, out);
+    return MPM_OK;
+}
+
+int mpm_download_grid(mpm_sim* s, int32_t* out) {
+    if (int rc = check_sim(s)) return rc;
+    if (!out && s->grid_count) return fail(MPM_E_INVALID, "null output");
+    DeviceGuard g(s->device);
+    if (int rc = sync_ref_grid(s, nullptr)) return rc;
+    MPM_CUDA(cudaDeviceSynchronize());
+    if (s->grid_count)
+        MPM_CUDA(cudaMemcpy(out, s->grid_ref, sizeof(int4) * (size_t)s->grid_count,
+                            cudaMemcpyDeviceToHost));
+    return MPM_OK;
+}
+
+int mpm_download_posvel(mpm_sim* s, float* out, void* stream) {
+    if (int rc = check_sim(s)) return rc;
+    if (!out && s->n) return fail(MPM_E_INVALID, "null output");
+    DeviceGuard g(s->device);
+    if (s->n)
+        MPM_CUDA(cudaMemcpyAsync(out, s->posvel, sizeof(float4) * 2 * (size_t)s->n,
+                                 cudaMemcpyDeviceToHost, static_cast<cudaStream_t>(stream)));
+    return MPM_OK;
+}
+
+int mpm_dispatch(mpm_sim* s, int kernel, void* stream) {
+    if (int rc = check_sim(s)) return rc;
+    if (!s->loaded) return fail(MPM_E_STATE, "no scene loaded (call reset first)");
+    DeviceGuard g(s->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (kernel < MPM_KERNEL_CLEAR_GRID || kernel > MPM_KERNEL_COPY_POSITION)
+        return fail(MPM_E_INVALID, "unknown kernel id");
+    const SimConsts k = s->consts();
+    if (int rc = sync_ref_grid(s, st)) return rc;
+    sorted_invalidate(s->sorted);
+    dispatch_kernel(s, kernel, k, st);
+    MPM_CUDA(cudaGetLastError());
+    return MPM_OK;
+}
+
+int mpm_set_engine(mpm_sim* s, int engine) {
+    if (int rc = check_sim(s)) return rc;
+    if (engine != MPM_ENGINE_SORTED && engine != MPM_ENGINE_DISPATCH)
+        return fail(MPM_E_INVALID, "unknown engine");
+    s->engine = engine;
+    return MPM_OK;
+}
+
+int mpm_get_engine(const mpm_sim* s) { return s ? s->engine : MPM_E_INVALID; }
+
+int mpm_synchronize(mpm_sim* s) {
+    if (int rc = check_sim(s)) return rc;
+    DeviceGuard g(s->device);
+    MPM_CUDA(cudaDeviceSynchronize());
+    return MPM_OK;
+}
+
+int mpm_check_health(mpm_sim* s, mpm_health* out) {
+    if (int rc = check_sim(s)) return rc;
+    if (!out) return fail(MPM_E_INVALID, "null output");
+    DeviceGuard g(s->device);
+    MPM_CUDA(cudaDeviceSynchronize());
+    MPM_CUDA(cudaMemset(s->counters + 1, 0, sizeof(unsigned long long)));
+    launch_count_nonfinite(s->P, s->n, s->counters + 1, nullptr);
+    unsigned long long h[2] = {0, 0};
+    MPM_CUDA(cudaMemcpy(h, s->counters, sizeof(h), cudaMemcpyDeviceToHost));
+    out->out_of_range_accesses = (int64_t)h[0];
+    out->nonfinite_particles = (int64_t)h[1];
+    return h[1] ? fail(MPM_E_NONFINITE, "non-finite particle state") : MPM_OK;
+}
+
+int mpm_set_profiling(mpm_sim* s, int enable) {
+    if (int rc = check_sim(s)) return rc;
+    DeviceGuard g(s->device);
+    s->prof.reset();
+    s->prof.enabled = enable != 0;
+    return MPM_OK;
+}
+
+int mpm_kernel_stats(mpm_sim* s, mpm_kernel_stat* out, int max_entries) {
+    if (int rc = check_sim(s)) return rc;
+    if (max_entries < 0 || (max_entries > 0 && !out)) return fail(MPM_E_INVALID, "bad arguments");
+    DeviceGuard g(s->device);
+    if (s->prof.collect() != 0) return fail(MPM_E_CUDA, "profiling events failed");
+    int count = 0;
+    for (int id = 0; id < KID_COUNT; ++id) {
+        if (s->prof.launches[id] == 0) continue;
+        if (count < max_entries) {
+            out[count].name = kernel_name(id);
+            out[count].launches = s->prof.launches[id];
+            out[count].timed_launches = s->prof.timed[id];
+            out[count].total_ms = s->prof.total_ms[id];
+        }
+        ++count;
+    }
+    return count;
+}
+
+int64_t mpm_launch_count(const mpm_sim* s) {
+    if (!s) return 0;
+    long long t = 0;
+    for (int id = 0; id < KID_COUNT; ++id) t += s->prof.launches[id];
+    return t;
+}
+
+const char* mpm_error_string(int code) {
+    switch (code) {
+        case MPM_OK: return "ok";
+        case MPM_E_INVALID: return "invalid argument";
+        case MPM_E_CAPACITY: return "particle capacity exceeded";
+        case MPM_E_GRID_CAPACITY: return "gridCount should be equal to or less than maxGridCount";
+        case MPM_E_CUDA: return "CUDA error";
+        case MPM_E_NO_DEVICE: return "no CUDA device";
+        case MPM_E_STATE: return "no scene loaded";
+        case MPM_E_NONFINITE: return "non-finite particle state";
+        default: return "unknown error";
+    }
+}
+
+const char* mpm_last_error(void) { return g_last_error.c_str(); }
+
+int mpm_scene_dambreak(float* out, int max_particles, const double init_box[3], uint64_t seed) {
+    if (!out || !init_box || max_particles < 0) return fail(MPM_E_INVALID, "bad arguments");
+    return scene_dambreak(out, max_particles, init_box, seed);
+}
+
+int mpm_scene_lattice(float* out, int n_per_axis, double origin, double spacing, double jitter,
+                      uint64_t seed) {
+    if (!out || n_per_axis < 0 || n_per_axis > 1290) return fail(MPM_E_INVALID, "bad arguments");
+    return scene_lattice(out, n_per_axis, origin, spacing, jitter, seed);
+}
+
+int mpm_probe_conversions(const float* in, int n, float fm, int32_t* enc_out, float* dec_out) {
+    if (n < 0 || (n > 0 && (!in || !enc_out || !dec_out))) return fail(MPM_E_INVALID, "bad arguments");
+    if (n == 0) return MPM_OK;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(MPM_E_NO_DEVICE, "no CUDA device");
+    }
+    float* d_in = nullptr;
+    int* d_enc = nullptr;
+    float* d_dec = nullptr;
+    cudaError_t e = cudaMalloc(&d_in, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&d_enc, sizeof(int) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&d_dec, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMemcpy(d_in, in, sizeof(float) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        launch_convert_probe(d_in, n, fm, d_enc, d_dec, nullptr);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(enc_out, d_enc, sizeof(int) * n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(dec_out, d_dec, sizeof(float) * n, cudaMemcpyDeviceToHost);
+    cudaFree(d_in);
+    cudaFree(d_enc);
+    cudaFree(d_dec);
+    if (e != cudaSuccess) return cuda_fail(e, "mpm_probe_conversions");
+    return MPM_OK;
+}
+
+}  // extern "C"

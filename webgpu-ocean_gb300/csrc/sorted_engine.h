@@ -1,0 +1,37 @@
+// sorted_engine.h -- the binned, fused MLS-MPM engine (kernels_sorted.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "mpm_internal.h"
+
+namespace mpm {
+
+struct SortedEngine;
+
+// Allocates the per-particle sort arrays; grids are sized at configure().
+int sorted_create(SortedEngine** out, int max_particles);
+void sorted_destroy(SortedEngine* e);
+
+// Sizes the brick grid for a scene (box, grid_count).  Returns 0, or -1 when
+// the box is degenerate (i32(Y) or i32(Z) == 0), in which case the caller
+// must use the dispatch engine.
+int sorted_configure(SortedEngine* e, const SimConsts& k);
+
+// Forgets the carried-over state (the next step re-bins and redoes p2g_1).
+void sorted_invalidate(SortedEngine* e);
+
+// Enqueues `substeps` substeps.  posvel is written by the last one.
+int sorted_step(SortedEngine* e, const Particles& P, float4* posvel, unsigned long long* oob,
+                const SimConsts& k, int substeps, cudaStream_t st, LaunchProfiler* prof);
+
+// True once a substep has run since configure/invalidate.
+bool sorted_has_grid(const SortedEngine* e);
+
+// Writes the last substep's grid, as updateGrid left it, in the reference's
+// x-major layout (grid_count int4 cells) to device memory `out`.
+int sorted_export_grid(SortedEngine* e, const SimConsts& k, int4* out, cudaStream_t st,
+                       LaunchProfiler* prof);
+
+const char* sorted_error();
+
+}  // namespace mpm

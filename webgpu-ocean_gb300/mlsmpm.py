@@ -1,0 +1,271 @@
+"""MLSMPMSimulator: the host-side mirror of WebGPU-Ocean's simulator class
+(mls-mpm/mls-mpm.ts:12-276) over the C ABI of libmpm.so.
+
+Names, arguments and error behaviour follow the TypeScript class:
+  MLSMPMSimulator(particleBuffer, posvelBuffer, renderDiameter, device)
+  reset(numParticles, initBoxSize)        -- throws on gridCount > capacity
+  execute(commandEncoder)                 -- 2 substeps, asynchronous
+  changeBoxSize(realBoxSize)
+  numParticles, gridCount
+Differences that come from the platform, not the algorithm:
+  * buffers are CUDA device memory; posvelBuffer may be a torch CUDA tensor
+    (or an object with data_ptr()/nbytes) or None, in which case the library
+    allocates it; particleBuffer, if given, receives the 80-byte particle
+    records at reset() and on writeParticleBuffer();
+  * `commandEncoder` is the CUDA stream to enqueue on (a torch.cuda.Stream,
+    a raw cudaStream_t integer, or None for the legacy default stream);
+  * Math.random in initDambreak is SplitMix64(seed) (the `seed` keyword).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+
+PARTICLE_STRUCT_SIZE = 80  # mlsmpmParticleStructSize, mls-mpm/mls-mpm.ts:10
+NUM_PARTICLES_MAX = 200000  # common.ts:11
+
+
+class MPMError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+class GridCapacityError(MPMError):
+    """The reference's `throw new Error("gridCount should be ...")`."""
+
+
+def _check(code: int, what: str = "") -> int:
+    if code >= 0:
+        return code
+    lib = L.load()
+    msg = (lib.mpm_last_error() or b"").decode() or lib.mpm_error_string(code).decode()
+    if what:
+        msg = f"{what}: {msg}"
+    cls = GridCapacityError if code == L.MPM_E_GRID_CAPACITY else MPMError
+    raise cls(code, msg)
+
+
+def _stream_handle(stream) -> int | None:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream or None
+    h = getattr(stream, "cuda_stream", None)
+    if h is not None:
+        return int(h) or None
+    raise TypeError("commandEncoder must be a CUDA stream, an int handle or None")
+
+
+def _dev_ptr(buf) -> tuple[int, int]:
+    if hasattr(buf, "data_ptr"):
+        ptr = int(buf.data_ptr())
+        nbytes = int(buf.numel() * buf.element_size()) if hasattr(buf, "numel") else int(buf.nbytes)
+        if hasattr(buf, "is_cuda") and not buf.is_cuda:
+            raise ValueError("buffer must live in CUDA device memory")
+        if hasattr(buf, "is_contiguous") and not buf.is_contiguous():
+            raise ValueError("buffer must be contiguous")
+        return ptr, nbytes
+    raise TypeError("device buffers must expose data_ptr()")
+
+
+def default_params() -> L.Params:
+    p = L.Params()
+    L.load().mpm_default_params(ctypes.byref(p))
+    return p
+
+
+class MLSMPMSimulator:
+    max_x_grids = 64  # mls-mpm/mls-mpm.ts:13-15
+    max_y_grids = 64
+    max_z_grids = 64
+    cellStructSize = 16  # mls-mpm/mls-mpm.ts:16
+
+    def __init__(self, particleBuffer=None, posvelBuffer=None, renderDiameter: float = 1.2,
+                 device=None, *, maxParticles: int = NUM_PARTICLES_MAX,
+                 maxGrid=(64, 64, 64), params: L.Params | None = None, seed: int = 0):
+        self._lib = L.load()
+        self.renderDiameter = float(renderDiameter)
+        self.max_x_grids, self.max_y_grids, self.max_z_grids = (int(g) for g in maxGrid)
+        self.maxParticles = int(maxParticles)
+        self.particleBuffer = particleBuffer
+        self.posvelBuffer = posvelBuffer
+        self.seed = int(seed)
+        self._device = device
+        self._handle = ctypes.c_void_p()
+        pv_ptr, pv_bytes = (None, 0)
+        if posvelBuffer is not None:
+            pv_ptr, pv_bytes = _dev_ptr(posvelBuffer)
+        if particleBuffer is not None:
+            _, pb = _dev_ptr(particleBuffer)
+            if pb < PARTICLE_STRUCT_SIZE * self.maxParticles:
+                raise ValueError("particleBuffer smaller than 80 * maxParticles bytes")
+        prm = params if params is not None else default_params()
+        with self._on_device():
+            _check(self._lib.mpm_create(ctypes.byref(prm), self.maxParticles, self.max_x_grids,
+                                        self.max_y_grids, self.max_z_grids,
+                                        self.renderDiameter, pv_ptr, pv_bytes,
+                                        ctypes.byref(self._handle)), "MLSMPMSimulator")
+        self.params = prm
+        self.sphere_size = None
+
+    # -- device selection -------------------------------------------------
+    def _on_device(self):
+        dev = self._device
+        if dev is None:
+            import contextlib
+            return contextlib.nullcontext()
+        import torch
+        return torch.cuda.device(dev)
+
+    # -- the reference's interface ---------------------------------------
+    @property
+    def numParticles(self) -> int:
+        return int(self._lib.mpm_num_particles(self._handle))
+
+    @property
+    def gridCount(self) -> int:
+        return int(self._lib.mpm_grid_count(self._handle))
+
+    def reset(self, numParticles: int, initBoxSize) -> None:
+        """mls-mpm/mls-mpm.ts:225-243."""
+        self.sphere_size = self.renderDiameter  # renderUniformsViews.sphere_size (:226)
+        box = (ctypes.c_double * 3)(*[float(b) for b in initBoxSize])
+        _check(self._lib.mpm_reset_dambreak(self._handle, int(numParticles), box,
+                                            ctypes.c_uint64(self.seed)), "reset")
+        if self.particleBuffer is not None:
+            self.writeParticleBuffer()
+
+    def execute(self, commandEncoder=None, substeps: int = 2) -> None:
+        """mls-mpm/mls-mpm.ts:245-268 (two substeps per frame)."""
+        _check(self._lib.mpm_step(self._handle, int(substeps), _stream_handle(commandEncoder)),
+               "execute")
+
+    def changeBoxSize(self, realBoxSize) -> None:
+        """mls-mpm/mls-mpm.ts:270-275."""
+        box = (ctypes.c_float * 3)(*[float(b) for b in realBoxSize])
+        _check(self._lib.mpm_set_real_box(self._handle, box), "changeBoxSize")
+
+    # -- beyond the reference: state access and diagnostics ---------------
+    def upload(self, particles: np.ndarray, initBoxSize) -> None:
+        arr = np.ascontiguousarray(particles, dtype=np.float32).reshape(-1, 20)
+        box = (ctypes.c_float * 3)(*[float(b) for b in initBoxSize])
+        _check(self._lib.mpm_upload(self._handle, arr.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                    len(arr), box), "upload")
+
+    def downloadParticles(self) -> np.ndarray:
+        out = np.zeros((self.numParticles, 20), dtype=np.float32)
+        _check(self._lib.mpm_download_particles(
+            self._handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))), "downloadParticles")
+        return out
+
+    def downloadGrid(self) -> np.ndarray:
+        out = np.zeros((self.gridCount, 4), dtype=np.int32)
+        _check(self._lib.mpm_download_grid(
+            self._handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))), "downloadGrid")
+        return out
+
+    def downloadPosvel(self, commandEncoder=None, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.zeros((self.numParticles, 8), dtype=np.float32)
+        _check(self._lib.mpm_download_posvel(
+            self._handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+            _stream_handle(commandEncoder)), "downloadPosvel")
+        if commandEncoder is None:
+            self.synchronize()
+        return out
+
+    def writeParticleBuffer(self) -> None:
+        """Copies the particle records (80-byte layout) into particleBuffer."""
+        import torch
+        recs = torch.from_numpy(self.downloadParticles().reshape(-1).view(np.uint8))
+        dst = self.particleBuffer.view(torch.uint8).reshape(-1)[: recs.numel()]
+        dst.copy_(recs)
+
+    def dispatch(self, kernel: str, commandEncoder=None) -> None:
+        """Runs one WGSL entry point alone (mls-mpm/mls-mpm.ts:248-265)."""
+        _check(self._lib.mpm_dispatch(self._handle, L.KERNELS[kernel],
+                                      _stream_handle(commandEncoder)), kernel)
+
+    @property
+    def engine(self) -> str:
+        return "dispatch" if self._lib.mpm_get_engine(self._handle) == L.MPM_ENGINE_DISPATCH else "sorted"
+
+    @engine.setter
+    def engine(self, name: str) -> None:
+        code = {"sorted": L.MPM_ENGINE_SORTED, "dispatch": L.MPM_ENGINE_DISPATCH}[name]
+        _check(self._lib.mpm_set_engine(self._handle, code), "engine")
+
+    def posvelDevicePtr(self) -> int:
+        return int(self._lib.mpm_posvel_device_ptr(self._handle) or 0)
+
+    def checkHealth(self) -> dict:
+        h = L.Health()
+        code = self._lib.mpm_check_health(self._handle, ctypes.byref(h))
+        if code not in (L.MPM_OK, L.MPM_E_NONFINITE):
+            _check(code, "checkHealth")
+        return {"nonfinite_particles": int(h.nonfinite_particles),
+                "out_of_range_accesses": int(h.out_of_range_accesses),
+                "ok": code == L.MPM_OK}
+
+    def setProfiling(self, enable: bool) -> None:
+        """Per-kernel CUDA-event timing on the launch stream (resets counters)."""
+        _check(self._lib.mpm_set_profiling(self._handle, int(bool(enable))), "setProfiling")
+
+    def kernelStats(self) -> dict:
+        """{kernel name: (launches, timed launches, total device ms)}."""
+        buf = (L.KernelStat * 32)()
+        n = _check(self._lib.mpm_kernel_stats(self._handle, buf, 32), "kernelStats")
+        return {buf[i].name.decode(): (int(buf[i].launches), int(buf[i].timed_launches),
+                                       float(buf[i].total_ms)) for i in range(min(n, 32))}
+
+    def launchCount(self) -> int:
+        return int(self._lib.mpm_launch_count(self._handle))
+
+    def synchronize(self) -> None:
+        _check(self._lib.mpm_synchronize(self._handle), "synchronize")
+
+    def close(self) -> None:
+        if self._handle:
+            self._lib.mpm_destroy(self._handle)
+            self._handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def scene_dambreak(initBoxSize, numParticles: int, seed: int) -> np.ndarray:
+    """initDambreak (mls-mpm/mls-mpm.ts:195-223) on the host, Math.random ->
+    SplitMix64(seed); returns (n, 20) float32 records."""
+    out = np.zeros((max(int(numParticles), 1), 20), dtype=np.float32)
+    box = (ctypes.c_double * 3)(*[float(b) for b in initBoxSize])
+    n = _check(L.load().mpm_scene_dambreak(out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                           int(numParticles), box, ctypes.c_uint64(seed)))
+    return out[:n].copy()
+
+
+def scene_lattice(n_per_axis: int, origin: float, spacing: float = 0.5, jitter: float = 0.05,
+                  seed: int = 0) -> np.ndarray:
+    """Jittered cubic lattice of n_per_axis^3 particles (x-major)."""
+    out = np.zeros((max(n_per_axis, 1) ** 3, 20), dtype=np.float32)
+    n = _check(L.load().mpm_scene_lattice(out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                          int(n_per_axis), float(origin), float(spacing),
+                                          float(jitter), ctypes.c_uint64(seed)))
+    return out[:n].copy()
+
+
+def probe_conversions(values: np.ndarray, fm: float = 1e7):
+    vals = np.ascontiguousarray(values, dtype=np.float32)
+    enc = np.zeros(len(vals), dtype=np.int32)
+    dec = np.zeros(len(vals), dtype=np.float32)
+    _check(L.load().mpm_probe_conversions(vals.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                          len(vals), fm,
+                                          enc.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                          dec.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+    return enc, dec
