@@ -256,6 +256,16 @@ def run_ours(args) -> None:
     dev_ms = max_over_ranks(dev_ms)
     value = world * n * SUBSTEPS * K / (dev_ms / 1e3)
 
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                              "steps": K, "warmup": args.warmup, "ms_per_step": dev_ms / K,
+                              "quick": True, "gpu_launches": launches}), flush=True)
+        sim.close()
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
     # --- per-kernel timing pass (roofline) ------------------------------
     sim.setProfiling(True)
     for i in range(K):
@@ -368,6 +378,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="time the device-resident steps only (for profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
