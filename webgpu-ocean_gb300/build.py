@@ -16,7 +16,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "build")
+# MPM_BUILD_DIR places a build elsewhere (tuning sweeps build variants side
+# by side); MPM_NVCC_DEFINES adds -D flags, e.g. "MPM_G2P_MIN_BLOCKS=4".
+BUILD = os.environ.get("MPM_BUILD_DIR") or os.path.join(HERE, "build")
 LIB = os.path.join(BUILD, "libmpm.so")
 REPO = os.path.dirname(HERE)
 INCLUDE = os.path.join(REPO, "include")
@@ -55,7 +57,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     for src in SOURCES:
         obj = os.path.join(BUILD, src.replace(".cu", ".o"))
         objs.append(obj)
-        cmd = [cc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        defines = ["-D" + d for d in os.environ.get("MPM_NVCC_DEFINES", "").split() if d]
+        cmd = [cc, *ARCH, *NVCC_FLAGS, *defines, "-c", os.path.join(CSRC, src), "-o", obj]
         if ptxas_info:
             cmd.insert(1, "-Xptxas=-v")
         if verbose:

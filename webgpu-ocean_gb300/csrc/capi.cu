@@ -160,7 +160,7 @@ struct mpm_sim {
     float real_box[3] = {0, 0, 0};
     bool loaded = false;
 
-    Particles P{};
+    ParticleStore ps{};
     // The reference's cell buffer (x-major, mls-mpm.ts:126-130): the dispatch
     // engine works in it; the sorted engine exports into it on demand.
     int4* grid_ref = nullptr;
@@ -223,10 +223,15 @@ int load_particles(mpm_sim* s, const float* aos80, int n, const float init_box[3
     MPM_CUDA(cudaDeviceSynchronize());
     std::vector<float4> q[4];
     aos80_to_soa(aos80, n, q);
-    float4* dst[4] = {s->P.p0, s->P.p1, s->P.p2, s->P.p3};
+    s->ps.cur = 0;
+    s->ps.canonical = true;
+    const Particles& P = s->ps.P[0];
+    float4* dst[4] = {P.p0, P.p1, P.p2, P.p3};
     for (int k = 0; k < 4; ++k)
         if (n) MPM_CUDA(cudaMemcpy(dst[k], q[k].data(), sizeof(float4) * (size_t)n,
                                    cudaMemcpyHostToDevice));
+    launch_iota(s->ps.id[0], n, nullptr);
+    MPM_CUDA(cudaGetLastError());
     s->n = n;
     s->grid_count = gc;
     for (int a = 0; a < 3; ++a) s->init_box[a] = s->real_box[a] = init_box[a];
@@ -238,6 +243,21 @@ int load_particles(mpm_sim* s, const float* aos80, int n, const float init_box[3
     sorted_invalidate(s->sorted);
     s->sorted_ok = sorted_configure(s->sorted, s->consts()) == 0;
     MPM_CUDA(cudaDeviceSynchronize());
+    return MPM_OK;
+}
+
+// Puts particle i back in slot i (the dispatch engine and the reference
+// address particles by index).  Forgets the sorted engine's carried state.
+int ensure_canonical(mpm_sim* s, cudaStream_t st) {
+    if (s->ps.canonical) return MPM_OK;
+    const int c = s->ps.cur;
+    s->prof.before(st);
+    launch_canonicalize(s->ps.P[c], s->ps.id[c], s->ps.P[c ^ 1], s->ps.id[c ^ 1], s->n, st);
+    s->prof.after(KID_CANONICALIZE, st);
+    MPM_CUDA(cudaGetLastError());
+    s->ps.cur = c ^ 1;
+    s->ps.canonical = true;
+    sorted_invalidate(s->sorted);
     return MPM_OK;
 }
 
@@ -256,14 +276,15 @@ int sync_ref_grid(mpm_sim* s, cudaStream_t st) {
 // One reference substep on the dispatch engine (mls-mpm.ts:248-265).
 void dispatch_kernel(mpm_sim* s, int kernel, const SimConsts& k, cudaStream_t st) {
     int4* cells = s->grid_ref;
+    const Particles& P = s->ps.P[s->ps.cur];
     s->prof.before(st);
     switch (kernel) {
         case MPM_KERNEL_CLEAR_GRID: launch_clear_grid(cells, k.grid_count, st); break;
-        case MPM_KERNEL_P2G_1: launch_p2g_1(s->P, cells, k, s->counters, st); break;
-        case MPM_KERNEL_P2G_2: launch_p2g_2(s->P, cells, k, s->counters, st); break;
+        case MPM_KERNEL_P2G_1: launch_p2g_1(P, cells, k, s->counters, st); break;
+        case MPM_KERNEL_P2G_2: launch_p2g_2(P, cells, k, s->counters, st); break;
         case MPM_KERNEL_UPDATE_GRID: launch_update_grid(cells, k, st); break;
-        case MPM_KERNEL_G2P: launch_g2p(s->P, cells, k, s->counters, st); break;
-        case MPM_KERNEL_COPY_POSITION: launch_copy_position(s->P, s->posvel, k.n, st); break;
+        case MPM_KERNEL_G2P: launch_g2p(P, cells, k, s->counters, st); break;
+        case MPM_KERNEL_COPY_POSITION: launch_copy_position(P, s->posvel, k.n, st); break;
     }
     s->prof.after(kernel, st);  // MPM_KERNEL_* == KID_* for the six entry points
 }
@@ -312,8 +333,12 @@ int mpm_create(const mpm_params* params, int max_particles, int max_grid_x, int 
     s->render_diameter = render_diameter;
     const size_t np = (size_t)(max_particles > 0 ? max_particles : 1);
     cudaError_t e = cudaSuccess;
-    float4** ps[4] = {&s->P.p0, &s->P.p1, &s->P.p2, &s->P.p3};
-    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaMalloc(ps[k], sizeof(float4) * np);
+    for (int b = 0; b < 2; ++b) {
+        Particles& P = s->ps.P[b];
+        float4** ps[4] = {&P.p0, &P.p1, &P.p2, &P.p3};
+        for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaMalloc(ps[k], sizeof(float4) * np);
+        if (e == cudaSuccess) e = cudaMalloc(&s->ps.id[b], sizeof(uint32_t) * np);
+    }
     if (e == cudaSuccess) e = cudaMalloc(&s->grid_ref, sizeof(int4) * (size_t)max_cells);
     if (e == cudaSuccess) e = cudaMalloc(&s->counters, sizeof(unsigned long long) * 2);
     if (e == cudaSuccess) {
@@ -348,10 +373,13 @@ int mpm_destroy(mpm_sim* s) {
     if (!s) return MPM_OK;
     DeviceGuard g(s->device);
     cudaDeviceSynchronize();
-    cudaFree(s->P.p0);
-    cudaFree(s->P.p1);
-    cudaFree(s->P.p2);
-    cudaFree(s->P.p3);
+    for (int b = 0; b < 2; ++b) {
+        cudaFree(s->ps.P[b].p0);
+        cudaFree(s->ps.P[b].p1);
+        cudaFree(s->ps.P[b].p2);
+        cudaFree(s->ps.P[b].p3);
+        cudaFree(s->ps.id[b]);
+    }
     cudaFree(s->grid_ref);
     cudaFree(s->counters);
     if (s->posvel_owned) cudaFree(s->posvel);
@@ -390,10 +418,11 @@ int mpm_step(mpm_sim* s, int substeps, void* stream) {
     const SimConsts k = s->consts();
     if (s->engine == MPM_ENGINE_DISPATCH || !s->sorted_ok) {
         if (int rc = sync_ref_grid(s, st)) return rc;
+        if (int rc = ensure_canonical(s, st)) return rc;
         for (int i = 0; i < substeps; ++i) dispatch_substep(s, k, st);
         if (substeps > 0) sorted_invalidate(s->sorted);
     } else if (substeps > 0) {
-        if (sorted_step(s->sorted, s->P, s->posvel, s->counters, k, substeps, st, &s->prof) != 0)
+        if (sorted_step(s->sorted, &s->ps, s->posvel, s->counters, k, substeps, st, &s->prof) != 0)
             return fail(MPM_E_CUDA, std::string("sorted engine: ") + sorted_error());
         s->ref_current = false;
     }
@@ -418,8 +447,18 @@ int mpm_download_particles(mpm_sim* s, float* out) {
     if (!out && s->n) return fail(MPM_E_INVALID, "null output");
     DeviceGuard g(s->device);
     MPM_CUDA(cudaDeviceSynchronize());
+    // Particles held in bin order are put back in index order in the spare
+    // buffer (no state changes).
+    const int c = s->ps.cur;
+    const Particles* Psrc = &s->ps.P[c];
+    if (!s->ps.canonical) {
+        launch_canonicalize(s->ps.P[c], s->ps.id[c], s->ps.P[c ^ 1], nullptr, s->n, nullptr);
+        MPM_CUDA(cudaGetLastError());
+        MPM_CUDA(cudaDeviceSynchronize());
+        Psrc = &s->ps.P[c ^ 1];
+    }
     std::vector<float4> q[4];
-    const float4* src[4] = {s->P.p0, s->P.p1, s->P.p2, s->P.p3};
+    const float4* src[4] = {Psrc->p0, Psrc->p1, Psrc->p2, Psrc->p3};
     for (int k = 0; k < 4; ++k) {
         q[k].resize((size_t)s->n);
         if (s->n)
@@ -461,6 +500,7 @@ int mpm_dispatch(mpm_sim* s, int kernel, void* stream) {
         return fail(MPM_E_INVALID, "unknown kernel id");
     const SimConsts k = s->consts();
     if (int rc = sync_ref_grid(s, st)) return rc;
+    if (int rc = ensure_canonical(s, st)) return rc;
     sorted_invalidate(s->sorted);
     dispatch_kernel(s, kernel, k, st);
     MPM_CUDA(cudaGetLastError());
@@ -490,7 +530,7 @@ int mpm_check_health(mpm_sim* s, mpm_health* out) {
     DeviceGuard g(s->device);
     MPM_CUDA(cudaDeviceSynchronize());
     MPM_CUDA(cudaMemset(s->counters + 1, 0, sizeof(unsigned long long)));
-    launch_count_nonfinite(s->P, s->n, s->counters + 1, nullptr);
+    launch_count_nonfinite(s->ps.P[s->ps.cur], s->n, s->counters + 1, nullptr);
     unsigned long long h[2] = {0, 0};
     MPM_CUDA(cudaMemcpy(h, s->counters, sizeof(h), cudaMemcpyDeviceToHost));
     out->out_of_range_accesses = (int64_t)h[0];

@@ -113,6 +113,23 @@ __global__ void k_copy_position(Particles P, float4* __restrict__ posvel, int n)
     posvel[2 * i + 1] = make_float4(v.x, v.y, v.z, 0.0f);
 }
 
+__global__ void k_canonicalize(Particles src, const uint32_t* __restrict__ id, Particles dst,
+                               uint32_t* __restrict__ id_dst, int n) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const uint32_t i = id[j];
+    dst.p0[i] = src.p0[j];
+    dst.p1[i] = src.p1[j];
+    dst.p2[i] = src.p2[j];
+    dst.p3[i] = src.p3[j];
+    if (id_dst) id_dst[j] = (uint32_t)j;
+}
+
+__global__ void k_iota(uint32_t* __restrict__ id, int n) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) id[j] = (uint32_t)j;
+}
+
 __global__ void k_count_nonfinite(Particles P, int n, unsigned long long* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned bad = 0;
@@ -169,6 +186,17 @@ void launch_g2p(const Particles& P, const int4* cells, const SimConsts& k,
 void launch_copy_position(const Particles& P, float4* posvel, int n, cudaStream_t st) {
     if (n <= 0) return;
     k_copy_position<<<blocks_for(n), kThreads, 0, st>>>(P, posvel, n);
+}
+
+void launch_canonicalize(const Particles& src, const uint32_t* id, const Particles& dst,
+                         uint32_t* id_dst, int n, cudaStream_t st) {
+    if (n <= 0) return;
+    k_canonicalize<<<blocks_for(n), kThreads, 0, st>>>(src, id, dst, id_dst, n);
+}
+
+void launch_iota(uint32_t* id, int n, cudaStream_t st) {
+    if (n <= 0) return;
+    k_iota<<<blocks_for(n), kThreads, 0, st>>>(id, n);
 }
 
 void launch_count_nonfinite(const Particles& P, int n, unsigned long long* out, cudaStream_t st) {

@@ -5,26 +5,28 @@
 // of mpm_math.cuh, and the grid is an i32 sum, so the order in which
 // contributions arrive does not matter.  What changes is where the work runs:
 //
-//  * The grid is stored brick-major: 4x4x4-cell bricks of 1 KB, contiguous,
-//    so a particle neighbourhood is a handful of 64-byte runs.
-//  * Particles are counting-sorted by brick every substep.  A task is up to
-//    256 particles of one brick; a CTA runs one task at a time and keeps the
-//    grid cells the task touches (its "arena", the particles' bounding box of
-//    base cells plus a one-cell halo) in shared memory.  Gathers read the
-//    arena; scatters are shared-memory i32 atomics, flushed with one
-//    red.global.add per touched cell and component.
-//  * Stage fusion per substep:
-//      k_p2g2        p2g_2 (and clears the other grid's dirty bricks)
-//      k_g2p_p2g1    updateGrid (applied while staging the arena) + g2p +
-//                    copyPosition (last substep) + the next substep's
-//                    clearGrid-free p2g_1 into the other grid + binning
+//  * The grid is stored brick-major: 4x4x4-cell bricks of 1 KB, contiguous.
+//  * Particles are counting-sorted by the brick of their base cell every
+//    substep, and kept physically in that order: g2p writes each particle to
+//    its position in the bin order of the other particle buffer (an id array
+//    rides along), so the next substep reads nearly contiguous memory.
+//  * A task is one brick's particles; CTAs claim tasks from an atomic work
+//    counter and walk a task in chunks of 256 particles.  The CTA keeps the
+//    cells the task's stencils reach (its "arena") in shared memory: the
+//    brick plus a one-cell halo (6^3 cells) for p2g_2 and g2p, plus a
+//    two-cell halo (8^3) for the next substep's p2g_1, whose particles have
+//    moved.  Gathers read the arena; scatters are shared-memory i32 atomics,
+//    flushed once per task with one red.global.add per touched cell and
+//    component.  Arena offsets are compile-time constants.
+//  * Per substep:
+//      k_p2g2        p2g_2; also clears the other grid's dirty bricks
+//      k_update      updateGrid over the bricks that hold contributions
+//      k_g2p_p2g1    g2p + copyPosition (last substep) + the next substep's
+//                    p2g_1 into the other (already cleared) grid + binning
 //      k_scan, k_scatter   counting sort for the next substep
-//    The updated grid is never written back: download recomputes updateGrid
-//    from the raw post-p2g_2 grid, which is what the reference's buffer holds
-//    once updateGrid has run.
 //  * Particles whose 27-cell stencil leaves the box (quirk Q1 aliasing, NaN,
-//    huge coordinates) and tasks whose arena would not fit take a global path
-//    that uses the reference's flat indices directly.
+//    huge coordinates) or leaves the task's arena take a global path that
+//    uses the reference's flat indices directly.
 #include <climits>
 #include <cstdio>
 #include <string>
@@ -36,9 +38,20 @@ namespace mpm {
 
 namespace {
 
-constexpr int kTask = 256;        // particles per task == threads per CTA
-constexpr int kArenaMax = 1024;   // cells a shared-memory arena can hold
+constexpr int kTask = 256;       // particles per task == threads per CTA
+constexpr int kA = 6;            // p2g_2 / g2p arena edge: brick + 1-cell halo
+constexpr int kA3 = kA * kA * kA;
+constexpr int kB = 8;            // next-p2g_1 arena edge: brick + 2-cell halo
+constexpr int kB3 = kB * kB * kB;
 constexpr int kScanThreads = 1024;
+
+// Minimum resident CTAs per SM requested from the register allocator.
+#ifndef MPM_G2P_MIN_BLOCKS
+#define MPM_G2P_MIN_BLOCKS 3
+#endif
+#ifndef MPM_P2G2_MIN_BLOCKS
+#define MPM_P2G2_MIN_BLOCKS 3
+#endif
 
 thread_local std::string g_err;
 
@@ -50,9 +63,13 @@ struct Geo {
     int nbricks;       // BX*BY*BZ; bin id nbricks collects irregular particles
 };
 
-struct Task {
+// A task: particles [first, first + count) of the bin order, all in `brick`
+// (-1: the bin of irregular particles).
+struct __align__(16) Task {
     int first;
     int count;
+    int brick;
+    int pad;
 };
 
 struct Dev {
@@ -68,7 +85,16 @@ struct Dev {
     uint32_t* order;
     Task* tasks;
     uint32_t* ntasks;
+    uint32_t* task_next;  // [3] work counters: p2g_2, g2p+p2g_1, first p2g_1
 };
+
+enum { kCtrP2G2 = 0, kCtrG2P = 1, kCtrP2G1 = 2 };
+
+// Dynamic task fetch: thread 0 claims task ids from a global counter, one
+// ahead, through a two-slot shared buffer (see the loops below).
+__device__ __forceinline__ int claim_task(const Dev& d, int ctr) {
+    return (int)atomicAdd(d.task_next + ctr, 1u);
+}
 
 __device__ __forceinline__ int brick_of(const Geo& g, int x, int y, int z) {
     return ((x >> 2) * g.BY + (y >> 2)) * g.BZ + (z >> 2);
@@ -91,6 +117,13 @@ __device__ __forceinline__ bool in_grid(const Geo& g, int idx) {
     return (unsigned)idx < (unsigned)g.grid_count;
 }
 
+// A cell that exists in the reference grid: per-axis in range and its flat
+// index below grid_count.
+__device__ __forceinline__ bool cell_exists(const Geo& g, int x, int y, int z) {
+    if (x < 0 || y < 0 || z < 0 || x >= g.Xi || y >= g.Y || z >= g.Z) return false;
+    return (x * g.Y + y) * g.Z + z < g.grid_count;
+}
+
 // A particle is regular when all 27 stencil cells are in-range cells whose
 // flat index equals their geometric position (no aliasing).
 __device__ __forceinline__ bool regular_base(const Geo& g, int bx, int by, int bz) {
@@ -106,82 +139,19 @@ __device__ __forceinline__ void base_cell(const float x[3], int& bx, int& by, in
     bz = f2i_sat(floorf(x[2]));
 }
 
+__device__ __forceinline__ void brick_coords(const Geo& g, int brick, int& x, int& y, int& z) {
+    const int byz = g.BY * g.BZ;
+    x = brick / byz;
+    const int r = brick - x * byz;
+    y = r / g.BZ;
+    z = r - y * g.BZ;
+}
+
 __device__ __forceinline__ void mark_brick(const Dev& d, int gi, uint32_t b) {
     if (__ldcg(d.dirty_flag[gi] + b) != 0u) return;
     if (atomicExch(d.dirty_flag[gi] + b, 1u) == 0u) {
         const uint32_t pos = atomicAdd(d.dirty_n + gi, 1u);
         d.dirty_list[gi][pos] = b;
-    }
-}
-
-// Bounding box of the valid base cells of the CTA's particles.
-struct Box {
-    int lo[3], hi[3];
-    int dim[3];
-    int cells;
-    bool any, fits;
-};
-
-__device__ __forceinline__ Box block_box(bool valid, int bx, int by, int bz, int* s_box) {
-    if (threadIdx.x < 6) s_box[threadIdx.x] = threadIdx.x < 3 ? INT_MAX : INT_MIN;
-    __syncthreads();
-    const int v[3] = {bx, by, bz};
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const int mn = __reduce_min_sync(0xffffffffu, valid ? v[a] : INT_MAX);
-        const int mx = __reduce_max_sync(0xffffffffu, valid ? v[a] : INT_MIN);
-        if ((threadIdx.x & 31) == 0) {
-            if (mn != INT_MAX) atomicMin(s_box + a, mn);
-            if (mx != INT_MIN) atomicMax(s_box + 3 + a, mx);
-        }
-    }
-    __syncthreads();
-    Box b;
-    b.any = s_box[0] <= s_box[3];
-    long long cells = 0;
-    if (b.any) {
-        cells = 1;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            b.lo[a] = s_box[a] - 1;
-            b.hi[a] = s_box[3 + a] + 1;
-            const long long dd = (long long)b.hi[a] - b.lo[a] + 1;
-            cells *= dd;
-            b.dim[a] = dd > kArenaMax ? kArenaMax + 1 : (int)dd;
-        }
-    } else {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) b.lo[a] = b.hi[a] = 0, b.dim[a] = 0;
-    }
-    b.fits = b.any && cells <= kArenaMax;
-    b.cells = b.fits ? (int)cells : 0;
-    return b;
-}
-
-__device__ __forceinline__ void arena_coords(const Box& b, int li, int& x, int& y, int& z) {
-    const int dyz = b.dim[1] * b.dim[2];
-    const int ax = li / dyz;
-    const int r = li - ax * dyz;
-    const int ay = r / b.dim[2];
-    const int az = r - ay * b.dim[2];
-    x = b.lo[0] + ax;
-    y = b.lo[1] + ay;
-    z = b.lo[2] + az;
-}
-
-// Marks every brick overlapped by the arena as dirty in grid gi.
-__device__ __forceinline__ void mark_arena_bricks(const Dev& d, const Geo& g, int gi, const Box& b) {
-    const int b0[3] = {b.lo[0] >> 2, b.lo[1] >> 2, b.lo[2] >> 2};
-    const int nb[3] = {(b.hi[0] >> 2) - b0[0] + 1, (b.hi[1] >> 2) - b0[1] + 1,
-                       (b.hi[2] >> 2) - b0[2] + 1};
-    const int total = nb[0] * nb[1] * nb[2];
-    for (int i = threadIdx.x; i < total; i += blockDim.x) {
-        const int ix = i / (nb[1] * nb[2]);
-        const int r = i - ix * nb[1] * nb[2];
-        const int iy = r / nb[2];
-        const int iz = r - iy * nb[2];
-        const uint32_t brick = ((b0[0] + ix) * g.BY + (b0[1] + iy)) * g.BZ + (b0[2] + iz);
-        mark_brick(d, gi, brick);
     }
 }
 
@@ -231,68 +201,96 @@ __device__ __forceinline__ void clear_dirty(const Dev& d, int gi) {
     }
 }
 
+// Arena cell li of an E^3 arena at origin o -> grid coordinates.
+template <int E>
+__device__ __forceinline__ void arena_cell(int li, int ox, int oy, int oz, int& x, int& y, int& z) {
+    const int ax = li / (E * E);
+    const int r = li - ax * (E * E);
+    const int ay = r / E;
+    x = ox + ax;
+    y = oy + ay;
+    z = oz + (r - ay * E);
+}
+
+// Global-path mass source (flat indices, as the reference's shaders address).
+struct GlobalMass {
+    const Geo& g;
+    const int4* grid;
+    float fm;
+    unsigned& bad;
+    __device__ float operator()(int idx, int, int, int) const {
+        if (!in_grid(g, idx)) { ++bad; return dec(0, fm); }
+        return dec(__ldcg(reinterpret_cast<const int*>(grid + flat_to_addr(g, idx)) + 3), fm);
+    }
+};
+
 // ---------------------------------------------------------------------------
 // p2g_2 (p2g_2.wgsl:30-94) over tasks; also clears grid `cur ^ 1`.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTask) k_p2g2(Particles P, Geo g, SimConsts k, Dev d, int cur,
-                                                unsigned long long* oob) {
-    __shared__ __align__(16) int s_mem[4 * kArenaMax];
-    __shared__ int s_box[6];
-    float* s_mass = reinterpret_cast<float*>(s_mem);
-    int* s_q = s_mem + kArenaMax;
+__global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
+    k_p2g2(Particles P, Geo g, SimConsts k, Dev d, int cur, unsigned long long* oob) {
+    __shared__ float s_mass[kA3];
+    __shared__ int s_q[3][kA3];
+    __shared__ int s_task[2];
 
     clear_dirty(d, cur ^ 1);
 
     int4* __restrict__ grid = d.grid[cur];
     unsigned bad = 0;
-    const uint32_t ntasks = __ldcg(d.ntasks);
-    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+    const int ntasks = (int)__ldcg(d.ntasks);
+    if (threadIdx.x == 0) s_task[0] = claim_task(d, kCtrP2G2);
+    __syncthreads();
+    int buf = 0;
+    int t = s_task[0];
+    while (t < ntasks) {
+        if (threadIdx.x == 0) s_task[buf ^ 1] = claim_task(d, kCtrP2G2);
         const Task task = d.tasks[t];
-        const bool active = (int)threadIdx.x < task.count;
-        PState s;
-        int bx = 0, by = 0, bz = 0;
-        bool reg = false;
-        if (active) {
-            const int slot = (int)d.order[task.first + threadIdx.x];
-            unpack_xC(P.p0[slot], P.p1[slot], P.p2[slot], s);
-            base_cell(s.x, bx, by, bz);
-            reg = regular_base(g, bx, by, bz);
-        }
-        const Box b = block_box(active && reg, bx, by, bz, s_box);
-        for (int li = threadIdx.x; li < b.cells; li += blockDim.x) {
-            int x, y, z;
-            arena_coords(b, li, x, y, z);
-            const int m = __ldcg(reinterpret_cast<const int*>(grid + brick_addr(g, x, y, z)) + 3);
-            s_mass[li] = dec(m, k.fm);
-            s_q[li] = 0;
-            s_q[li + kArenaMax] = 0;
-            s_q[li + 2 * kArenaMax] = 0;
+        int ox = 0, oy = 0, oz = 0;
+        if (task.brick >= 0) {
+            brick_coords(g, task.brick, ox, oy, oz);
+            ox = 4 * ox - 1;
+            oy = 4 * oy - 1;
+            oz = 4 * oz - 1;
+            for (int li = threadIdx.x; li < kA3; li += kTask) {
+                int x, y, z;
+                arena_cell<kA>(li, ox, oy, oz, x, y, z);
+                int m = 0;
+                if (cell_exists(g, x, y, z))
+                    m = __ldcg(reinterpret_cast<const int*>(grid + brick_addr(g, x, y, z)) + 3);
+                s_mass[li] = dec(m, k.fm);
+                s_q[0][li] = 0;
+                s_q[1][li] = 0;
+                s_q[2][li] = 0;
+            }
         }
         __syncthreads();
-        if (active) {
-            if (reg && b.fits) {
-                const int dz = b.dim[2], dyz = b.dim[1] * b.dim[2];
-                const int li0 = ((bx - 1 - b.lo[0]) * b.dim[1] + (by - 1 - b.lo[1])) * dz +
-                                (bz - 1 - b.lo[2]);
+        for (int j = threadIdx.x; j < task.count; j += kTask) {
+            const int slot = (int)d.order[task.first + j];
+            PState s;
+            unpack_xC(P.p0[slot], P.p1[slot], P.p2[slot], s);
+            int bx, by, bz;
+            base_cell(s.x, bx, by, bz);
+            const int ax = bx - 1 - ox, ay = by - 1 - oy, az = bz - 1 - oz;
+            const bool in_arena = task.brick >= 0 && regular_base(g, bx, by, bz) &&
+                                  (unsigned)ax <= (unsigned)(kA - 3) &&
+                                  (unsigned)ay <= (unsigned)(kA - 3) &&
+                                  (unsigned)az <= (unsigned)(kA - 3);
+            if (in_arena) {
+                const int li0 = (ax * kA + ay) * kA + az;
                 p2g2_particle(
                     s, k,
                     [&](int, int gx, int gy, int gz) -> float {
-                        return s_mass[li0 + gx * dyz + gy * dz + gz];
+                        return s_mass[li0 + (gx * kA + gy) * kA + gz];
                     },
                     [&](int, int gx, int gy, int gz, int mx, int my, int mz) {
-                        const int li = li0 + gx * dyz + gy * dz + gz;
-                        if (mx) atomicAdd(s_q + li, mx);
-                        if (my) atomicAdd(s_q + kArenaMax + li, my);
-                        if (mz) atomicAdd(s_q + 2 * kArenaMax + li, mz);
+                        const int li = li0 + (gx * kA + gy) * kA + gz;
+                        atomicAdd(&s_q[0][li], mx);
+                        atomicAdd(&s_q[1][li], my);
+                        atomicAdd(&s_q[2][li], mz);
                     });
             } else {
                 p2g2_particle(
-                    s, k,
-                    [&](int idx, int, int, int) -> float {
-                        if (!in_grid(g, idx)) { ++bad; return dec(0, k.fm); }
-                        return dec(__ldcg(reinterpret_cast<const int*>(grid + flat_to_addr(g, idx)) + 3),
-                                   k.fm);
-                    },
+                    s, k, GlobalMass{g, grid, k.fm, bad},
                     [&](int idx, int, int, int, int mx, int my, int mz) {
                         if (!in_grid(g, idx)) { ++bad; return; }
                         const int a = flat_to_addr(g, idx);
@@ -305,154 +303,216 @@ __global__ void __launch_bounds__(kTask) k_p2g2(Particles P, Geo g, SimConsts k,
             }
         }
         __syncthreads();
-        for (int li = threadIdx.x; li < b.cells; li += blockDim.x) {
-            const int q0 = s_q[li], q1 = s_q[li + kArenaMax], q2 = s_q[li + 2 * kArenaMax];
-            if ((q0 | q1 | q2) == 0) continue;
-            int x, y, z;
-            arena_coords(b, li, x, y, z);
-            int* c = reinterpret_cast<int*>(grid + brick_addr(g, x, y, z));
-            if (q0) atomicAdd(c + 0, q0);
-            if (q1) atomicAdd(c + 1, q1);
-            if (q2) atomicAdd(c + 2, q2);
+        if (task.brick >= 0) {
+            for (int li = threadIdx.x; li < kA3; li += kTask) {
+                const int q0 = s_q[0][li], q1 = s_q[1][li], q2 = s_q[2][li];
+                if ((q0 | q1 | q2) == 0) continue;
+                int x, y, z;
+                arena_cell<kA>(li, ox, oy, oz, x, y, z);
+                if (!cell_exists(g, x, y, z)) continue;  // unreachable for regular particles
+                int* c = reinterpret_cast<int*>(grid + brick_addr(g, x, y, z));
+                if (q0) atomicAdd(c + 0, q0);
+                if (q1) atomicAdd(c + 1, q1);
+                if (q2) atomicAdd(c + 2, q2);
+            }
         }
-        if (b.fits) mark_arena_bricks(d, g, cur, b);
         __syncthreads();
+        buf ^= 1;
+        t = s_task[buf];
     }
     if (bad) atomicAdd(oob, (unsigned long long)bad);
 }
 
 // ---------------------------------------------------------------------------
-// updateGrid + g2p + copyPosition + next p2g_1 + binning, over tasks.
-// DO_G2P = false runs p2g_1 of the current positions only (first substep).
+// updateGrid (updateGrid.wgsl:23-46) on the dirty bricks of grid `cur`, in
+// place: warp per brick, two cells per lane.
 // ---------------------------------------------------------------------------
-template <bool DO_G2P, bool POSVEL, bool COUNT>
-__global__ void __launch_bounds__(kTask) k_g2p_p2g1(Particles P, float4* __restrict__ posvel,
-                                                    Geo g, SimConsts k, Dev d, int src, int dst,
-                                                    unsigned long long* oob) {
-    __shared__ __align__(16) int s_mem[4 * kArenaMax];
-    __shared__ int s_box[6];
-    float* s_v = reinterpret_cast<float*>(s_mem);
-    int* s_a = s_mem;
+__global__ void __launch_bounds__(256) k_update(Geo g, SimConsts k, Dev d, int cur) {
+    const uint32_t nd = __ldcg(d.dirty_n + cur);
+    const int hx = wall_hi(k.real_box[0]), hy = wall_hi(k.real_box[1]), hz = wall_hi(k.real_box[2]);
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    int4* __restrict__ grid = d.grid[cur];
+    for (uint32_t i = warp; i < nd; i += nwarps) {
+        const int b = (int)__ldcg(d.dirty_list[cur] + i);
+        int bx, by, bz;
+        brick_coords(g, b, bx, by, bz);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int c = (int)lane + 32 * h;
+            const int4 raw = grid[(size_t)b * 64 + c];
+            if (raw.w > 0) {
+                const int x = 4 * bx + (c >> 4), y = 4 * by + ((c >> 2) & 3), z = 4 * bz + (c & 3);
+                grid[(size_t)b * 64 + c] = update_cell_xyz(raw, x, y, z, k, hx, hy, hz);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// g2p + copyPosition + next p2g_1 + binning, over tasks.  Reads particles
+// from Pin through the bin order and writes them, in bin order, to Pout.
+// DO_G2P = false runs p2g_1 of the current positions only (first substep;
+// Pout is not written).
+// ---------------------------------------------------------------------------
+template <bool DO_G2P, bool POSVEL>
+__global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
+    k_g2p_p2g1(Particles Pin, Particles Pout, const uint32_t* __restrict__ id_in,
+               uint32_t* __restrict__ id_out, float4* __restrict__ posvel, Geo g, SimConsts k,
+               Dev d, int src, int dst, unsigned long long* oob) {
+    __shared__ float4 s_v[kA3];
+    __shared__ int s_a[4][kB3];
+    __shared__ int s_touch[27];
+    __shared__ int s_task[2];
 
     const int4* __restrict__ gsrc = d.grid[src];
     int4* __restrict__ gdst = d.grid[dst];
-    const int hx = wall_hi(k.real_box[0]), hy = wall_hi(k.real_box[1]),
-              hz = wall_hi(k.real_box[2]);
+    const int ctr = DO_G2P ? kCtrG2P : kCtrP2G1;
     unsigned bad = 0;
-    const uint32_t ntasks = __ldcg(d.ntasks);
-    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+    const int ntasks = (int)__ldcg(d.ntasks);
+    if (threadIdx.x == 0) s_task[0] = claim_task(d, ctr);
+    __syncthreads();
+    int buf = 0;
+    int t = s_task[0];
+    while (t < ntasks) {
+        if (threadIdx.x == 0) s_task[buf ^ 1] = claim_task(d, ctr);
         const Task task = d.tasks[t];
-        const bool active = (int)threadIdx.x < task.count;
-        const int slot = active ? (int)d.order[task.first + threadIdx.x] : 0;
-        PState s;
-        int bx = 0, by = 0, bz = 0;
-        bool reg = false;
-        if (DO_G2P) {
+        int tbx = 0, tby = 0, tbz = 0;
+        if (task.brick >= 0) {
+            brick_coords(g, task.brick, tbx, tby, tbz);
+            const int ox = 4 * tbx - 1, oy = 4 * tby - 1, oz = 4 * tbz - 1;
+            if (DO_G2P) {
+                for (int li = threadIdx.x; li < kA3; li += kTask) {
+                    int x, y, z;
+                    arena_cell<kA>(li, ox, oy, oz, x, y, z);
+                    int4 c = make_int4(0, 0, 0, 0);
+                    if (cell_exists(g, x, y, z)) c = __ldcg(gsrc + brick_addr(g, x, y, z));
+                    s_v[li] = make_float4(dec(c.x, k.fm), dec(c.y, k.fm), dec(c.z, k.fm), 0.0f);
+                }
+            }
+            for (int li = threadIdx.x; li < kB3; li += kTask) {
+                s_a[0][li] = 0;
+                s_a[1][li] = 0;
+                s_a[2][li] = 0;
+                s_a[3][li] = 0;
+            }
+            if (threadIdx.x < 27) s_touch[threadIdx.x] = 0;
+        }
+        __syncthreads();
+
+        for (int base = 0; base < task.count; base += kTask) {
+            const int j = base + (int)threadIdx.x;
+            const bool active = j < task.count;
+            const int jo = task.first + j;  // the particle's position in bin order
+            const int slot = active ? (int)d.order[jo] : 0;
+            PState s;
+            if (DO_G2P) {
+                if (active) {
+                    const float4 a = Pin.p0[slot];
+                    s.x[0] = a.x; s.x[1] = a.y; s.x[2] = a.z;
+                    int bx, by, bz;
+                    base_cell(s.x, bx, by, bz);
+                    const int ax = bx - 4 * tbx, ay = by - 4 * tby, az = bz - 4 * tbz;
+                    const bool in_arena = task.brick >= 0 && regular_base(g, bx, by, bz) &&
+                                          (unsigned)ax <= 3u && (unsigned)ay <= 3u &&
+                                          (unsigned)az <= 3u;
+                    if (in_arena) {
+                        const int li0 = (ax * kA + ay) * kA + az;
+                        g2p_particle(s, k, [&](int, int gx, int gy, int gz, float out[3]) {
+                            const float4 v = s_v[li0 + (gx * kA + gy) * kA + gz];
+                            out[0] = v.x;
+                            out[1] = v.y;
+                            out[2] = v.z;
+                        });
+                    } else {
+                        g2p_particle(s, k, [&](int idx, int, int, int, float out[3]) {
+                            int4 c = make_int4(0, 0, 0, 0);
+                            if (in_grid(g, idx)) c = __ldcg(gsrc + flat_to_addr(g, idx));
+                            else ++bad;
+                            out[0] = dec(c.x, k.fm);
+                            out[1] = dec(c.y, k.fm);
+                            out[2] = dec(c.z, k.fm);
+                        });
+                    }
+                    store_particle(Pout, jo, s);
+                    const uint32_t pid = id_in[slot];
+                    id_out[jo] = pid;
+                    if (POSVEL) {
+                        posvel[2 * (size_t)pid] = make_float4(s.x[0], s.x[1], s.x[2], 0.0f);
+                        posvel[2 * (size_t)pid + 1] = make_float4(s.v[0], s.v[1], s.v[2], 0.0f);
+                    }
+                }
+            } else if (active) {
+                load_particle(Pin, slot, s);
+            }
+
+            // p2g_1 of the (new) state into grid dst, arena = brick + 2-cell halo.
+            int bx = 0, by = 0, bz = 0;
+            bool reg = false;
             if (active) {
-                const float4 a = P.p0[slot];
-                s.x[0] = a.x; s.x[1] = a.y; s.x[2] = a.z;
                 base_cell(s.x, bx, by, bz);
                 reg = regular_base(g, bx, by, bz);
+                const int ax = bx + 1 - 4 * tbx, ay = by + 1 - 4 * tby, az = bz + 1 - 4 * tbz;
+                const bool in_arena = task.brick >= 0 && reg &&
+                                      (unsigned)ax <= (unsigned)(kB - 3) &&
+                                      (unsigned)ay <= (unsigned)(kB - 3) &&
+                                      (unsigned)az <= (unsigned)(kB - 3);
+                if (in_arena) {
+                    const int li0 = (ax * kB + ay) * kB + az;
+                    p2g1_particle(s, k,
+                                  [&](int, int gx, int gy, int gz, int m, int vx, int vy, int vz) {
+                                      const int li = li0 + (gx * kB + gy) * kB + gz;
+                                      atomicAdd(&s_a[3][li], m);
+                                      atomicAdd(&s_a[0][li], vx);
+                                      atomicAdd(&s_a[1][li], vy);
+                                      atomicAdd(&s_a[2][li], vz);
+                                  });
+                } else {
+                    p2g1_particle(s, k,
+                                  [&](int idx, int, int, int, int m, int vx, int vy, int vz) {
+                                      if (!in_grid(g, idx)) { ++bad; return; }
+                                      const int a = flat_to_addr(g, idx);
+                                      int* c = reinterpret_cast<int*>(gdst + a);
+                                      atomicAdd(c + 3, m);
+                                      atomicAdd(c + 0, vx);
+                                      atomicAdd(c + 1, vy);
+                                      atomicAdd(c + 2, vz);
+                                      mark_brick(d, dst, (uint32_t)(a >> 6));
+                                  });
+                }
             }
-            const Box b = block_box(active && reg, bx, by, bz, s_box);
-            for (int li = threadIdx.x; li < b.cells; li += blockDim.x) {
+            if (DO_G2P) count_bin(d, active, jo, bin_key(g, reg, bx, by, bz));
+        }
+        __syncthreads();
+        if (task.brick >= 0) {
+            const int ox = 4 * tbx - 2, oy = 4 * tby - 2, oz = 4 * tbz - 2;
+            for (int li = threadIdx.x; li < kB3; li += kTask) {
+                const int q0 = s_a[0][li], q1 = s_a[1][li], q2 = s_a[2][li], q3 = s_a[3][li];
+                if ((q0 | q1 | q2 | q3) == 0) continue;
                 int x, y, z;
-                arena_coords(b, li, x, y, z);
-                const int4 raw = __ldcg(gsrc + brick_addr(g, x, y, z));
-                const int4 c = update_cell_xyz(raw, x, y, z, k, hx, hy, hz);
-                s_v[li] = dec(c.x, k.fm);
-                s_v[li + kArenaMax] = dec(c.y, k.fm);
-                s_v[li + 2 * kArenaMax] = dec(c.z, k.fm);
+                arena_cell<kB>(li, ox, oy, oz, x, y, z);
+                if (!cell_exists(g, x, y, z)) continue;  // unreachable for regular particles
+                int* c = reinterpret_cast<int*>(gdst + brick_addr(g, x, y, z));
+                if (q0) atomicAdd(c + 0, q0);
+                if (q1) atomicAdd(c + 1, q1);
+                if (q2) atomicAdd(c + 2, q2);
+                if (q3) atomicAdd(c + 3, q3);
+                // which of the 3x3x3 neighbouring bricks received this cell
+                const int nb = (((x >> 2) - tbx + 1) * 3 + ((y >> 2) - tby + 1)) * 3 +
+                               ((z >> 2) - tbz + 1);
+                s_touch[nb] = 1;
             }
             __syncthreads();
-            if (active) {
-                if (reg && b.fits) {
-                    const int dz = b.dim[2], dyz = b.dim[1] * b.dim[2];
-                    const int li0 = ((bx - 1 - b.lo[0]) * b.dim[1] + (by - 1 - b.lo[1])) * dz +
-                                    (bz - 1 - b.lo[2]);
-                    g2p_particle(s, k, [&](int, int gx, int gy, int gz, float out[3]) {
-                        const int li = li0 + gx * dyz + gy * dz + gz;
-                        out[0] = s_v[li];
-                        out[1] = s_v[li + kArenaMax];
-                        out[2] = s_v[li + 2 * kArenaMax];
-                    });
-                } else {
-                    g2p_particle(s, k, [&](int idx, int, int, int, float out[3]) {
-                        int4 c = make_int4(0, 0, 0, 0);
-                        if (in_grid(g, idx)) c = update_cell(__ldcg(gsrc + flat_to_addr(g, idx)), idx, k, hx, hy, hz);
-                        else ++bad;
-                        out[0] = dec(c.x, k.fm);
-                        out[1] = dec(c.y, k.fm);
-                        out[2] = dec(c.z, k.fm);
-                    });
-                }
-                store_particle(P, slot, s);
-                if (POSVEL) {
-                    posvel[2 * (size_t)slot] = make_float4(s.x[0], s.x[1], s.x[2], 0.0f);
-                    posvel[2 * (size_t)slot + 1] = make_float4(s.v[0], s.v[1], s.v[2], 0.0f);
-                }
-            }
-            __syncthreads();  // s_v is reused as s_a below
-        } else if (active) {
-            load_particle(P, slot, s);
-        }
-
-        // p2g_1 of the (new) state into grid dst.
-        bx = by = bz = 0;
-        reg = false;
-        if (active) {
-            base_cell(s.x, bx, by, bz);
-            reg = regular_base(g, bx, by, bz);
-        }
-        const Box b = block_box(active && reg, bx, by, bz, s_box);
-        for (int li = threadIdx.x; li < b.cells; li += blockDim.x) {
-            s_a[li] = 0;
-            s_a[li + kArenaMax] = 0;
-            s_a[li + 2 * kArenaMax] = 0;
-            s_a[li + 3 * kArenaMax] = 0;
-        }
-        __syncthreads();
-        if (active) {
-            if (reg && b.fits) {
-                const int dz = b.dim[2], dyz = b.dim[1] * b.dim[2];
-                const int li0 = ((bx - 1 - b.lo[0]) * b.dim[1] + (by - 1 - b.lo[1])) * dz +
-                                (bz - 1 - b.lo[2]);
-                p2g1_particle(s, k, [&](int, int gx, int gy, int gz, int m, int vx, int vy, int vz) {
-                    const int li = li0 + gx * dyz + gy * dz + gz;
-                    if (m) atomicAdd(s_a + 3 * kArenaMax + li, m);
-                    if (vx) atomicAdd(s_a + li, vx);
-                    if (vy) atomicAdd(s_a + kArenaMax + li, vy);
-                    if (vz) atomicAdd(s_a + 2 * kArenaMax + li, vz);
-                });
-            } else {
-                p2g1_particle(s, k, [&](int idx, int, int, int, int m, int vx, int vy, int vz) {
-                    if (!in_grid(g, idx)) { ++bad; return; }
-                    const int a = flat_to_addr(g, idx);
-                    int* c = reinterpret_cast<int*>(gdst + a);
-                    atomicAdd(c + 3, m);
-                    atomicAdd(c + 0, vx);
-                    atomicAdd(c + 1, vy);
-                    atomicAdd(c + 2, vz);
-                    mark_brick(d, dst, (uint32_t)(a >> 6));
-                });
+            if (threadIdx.x < 27 && s_touch[threadIdx.x]) {
+                const int i = threadIdx.x;
+                const int nbx = tbx + i / 9 - 1, nby = tby + (i / 3) % 3 - 1, nbz = tbz + i % 3 - 1;
+                mark_brick(d, dst, (uint32_t)((nbx * g.BY + nby) * g.BZ + nbz));
             }
         }
-        if (COUNT) count_bin(d, active, slot, bin_key(g, reg, bx, by, bz));
         __syncthreads();
-        for (int li = threadIdx.x; li < b.cells; li += blockDim.x) {
-            const int q0 = s_a[li], q1 = s_a[li + kArenaMax], q2 = s_a[li + 2 * kArenaMax],
-                      q3 = s_a[li + 3 * kArenaMax];
-            if ((q0 | q1 | q2 | q3) == 0) continue;
-            int x, y, z;
-            arena_coords(b, li, x, y, z);
-            int* c = reinterpret_cast<int*>(gdst + brick_addr(g, x, y, z));
-            if (q0) atomicAdd(c + 0, q0);
-            if (q1) atomicAdd(c + 1, q1);
-            if (q2) atomicAdd(c + 2, q2);
-            if (q3) atomicAdd(c + 3, q3);
-        }
-        if (b.fits) mark_arena_bricks(d, g, dst, b);
-        __syncthreads();
+        buf ^= 1;
+        t = s_task[buf];
     }
     if (bad) atomicAdd(oob, (unsigned long long)bad);
 }
@@ -473,59 +533,97 @@ __global__ void __launch_bounds__(kTask) k_bin(Particles P, Geo g, Dev d, int n)
 }
 
 // Exclusive scan of the bin counts -> bin_start and the task list; zeroes the
-// counts for the next binning.  One CTA.
-__global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, int nbins) {
-    __shared__ uint32_t s_c[kScanThreads / 32], s_t[kScanThreads / 32];
-    const int per = (nbins + kScanThreads - 1) / kScanThreads;
-    const int b0 = min(nbins, (int)threadIdx.x * per), b1 = min(nbins, b0 + per);
-    uint32_t sc = 0, stt = 0;
-    for (int b = b0; b < b1; ++b) {
-        const uint32_t c = d.bin_count[b];
-        sc += c;
-        stt += (c + kTask - 1) / kTask;
-    }
-    // block exclusive scan of (sc, stt)
+// counts for the next binning.  One CTA walks the bins in chunks of 8192:
+// coalesced loads into shared memory, 8 consecutive bins per thread, a
+// block-wide scan of (particles, tasks), coalesced stores.
+constexpr int kScanPer = 8;
+constexpr int kScanChunk = kScanThreads * kScanPer;
+
+__device__ __forceinline__ void block_scan2(uint32_t& a, uint32_t& b, uint32_t* s_a, uint32_t* s_b,
+                                            uint32_t& tot_a, uint32_t& tot_b) {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    uint32_t ic = sc, it = stt;
+    uint32_t ia = a, ib = b;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t yc = __shfl_up_sync(0xffffffffu, ic, o);
-        const uint32_t yt = __shfl_up_sync(0xffffffffu, it, o);
-        if ((int)lane >= o) { ic += yc; it += yt; }
+        const uint32_t ya = __shfl_up_sync(0xffffffffu, ia, o);
+        const uint32_t yb = __shfl_up_sync(0xffffffffu, ib, o);
+        if ((int)lane >= o) { ia += ya; ib += yb; }
     }
-    if (lane == 31) { s_c[warp] = ic; s_t[warp] = it; }
+    if (lane == 31) { s_a[warp] = ia; s_b[warp] = ib; }
     __syncthreads();
     if (warp == 0) {
-        uint32_t wc = lane < kScanThreads / 32 ? s_c[lane] : 0u;
-        uint32_t wt = lane < kScanThreads / 32 ? s_t[lane] : 0u;
+        uint32_t wa = s_a[lane], wb = s_b[lane];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t yc = __shfl_up_sync(0xffffffffu, wc, o);
-            const uint32_t yt = __shfl_up_sync(0xffffffffu, wt, o);
-            if ((int)lane >= o) { wc += yc; wt += yt; }
+            const uint32_t ya = __shfl_up_sync(0xffffffffu, wa, o);
+            const uint32_t yb = __shfl_up_sync(0xffffffffu, wb, o);
+            if ((int)lane >= o) { wa += ya; wb += yb; }
         }
-        if (lane < kScanThreads / 32) { s_c[lane] = wc; s_t[lane] = wt; }
+        s_a[lane] = wa;
+        s_b[lane] = wb;
     }
     __syncthreads();
-    uint32_t pc = ic - sc + (warp ? s_c[warp - 1] : 0u);
-    uint32_t pt = it - stt + (warp ? s_t[warp - 1] : 0u);
-    for (int b = b0; b < b1; ++b) {
-        const uint32_t c = d.bin_count[b];
-        d.bin_start[b] = pc;
-        const uint32_t nt = (c + kTask - 1) / kTask;
-        for (uint32_t j = 0; j < nt; ++j) {
-            Task tk;
-            tk.first = (int)(pc + j * kTask);
-            tk.count = (int)min((uint32_t)kTask, c - j * kTask);
-            d.tasks[pt + j] = tk;
+    tot_a = s_a[31];
+    tot_b = s_b[31];
+    const uint32_t ea = ia - a + (warp ? s_a[warp - 1] : 0u);
+    const uint32_t eb = ib - b + (warp ? s_b[warp - 1] : 0u);
+    a = ea;
+    b = eb;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, int nbins) {
+    __shared__ uint4 s_buf4[kScanChunk / 4];
+    __shared__ uint32_t s_a[32], s_b[32];
+    uint32_t* s_buf = reinterpret_cast<uint32_t*>(s_buf4);
+    uint32_t carry_p = 0, carry_t = 0;
+    for (int base = 0; base < nbins; base += kScanChunk) {
+        const int len = min(kScanChunk, nbins - base);
+        for (int i = threadIdx.x; i < kScanChunk; i += kScanThreads)
+            s_buf[i] = i < len ? d.bin_count[base + i] : 0u;
+        __syncthreads();
+        const uint4 q0 = s_buf4[2 * threadIdx.x], q1 = s_buf4[2 * threadIdx.x + 1];
+        const uint32_t c[kScanPer] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+        uint32_t sp = 0, st = 0;
+#pragma unroll
+        for (int k = 0; k < kScanPer; ++k) {
+            sp += c[k];
+            st += c[k] ? 1u : 0u;
         }
-        pc += c;
-        pt += nt;
-        d.bin_count[b] = 0u;
+        uint32_t tot_p, tot_t;
+        block_scan2(sp, st, s_a, s_b, tot_p, tot_t);
+        uint32_t pc = carry_p + sp, pt = carry_t + st;
+        uint32_t starts[kScanPer];
+#pragma unroll
+        for (int k = 0; k < kScanPer; ++k) {
+            starts[k] = pc;
+            if (c[k]) {
+                const int bin = base + (int)threadIdx.x * kScanPer + k;
+                Task tk;
+                tk.first = (int)pc;
+                tk.count = (int)c[k];
+                tk.brick = bin == nbins - 1 ? -1 : bin;
+                tk.pad = 0;
+                d.tasks[pt] = tk;
+                ++pt;
+            }
+            pc += c[k];
+        }
+        __syncthreads();  // every thread has read its counts from s_buf
+        s_buf4[2 * threadIdx.x] = make_uint4(starts[0], starts[1], starts[2], starts[3]);
+        s_buf4[2 * threadIdx.x + 1] = make_uint4(starts[4], starts[5], starts[6], starts[7]);
+        __syncthreads();
+        for (int i = threadIdx.x; i < len; i += kScanThreads) {
+            d.bin_start[base + i] = s_buf[i];
+            d.bin_count[base + i] = 0u;
+        }
+        carry_p += tot_p;
+        carry_t += tot_t;
+        __syncthreads();  // s_buf and s_a/s_b are reused by the next chunk
     }
-    if (threadIdx.x == kScanThreads - 1) {
-        d.bin_start[nbins] = pc;
-        *d.ntasks = pt;
+    if (threadIdx.x == 0) {
+        d.bin_start[nbins] = carry_p;
+        *d.ntasks = carry_t;
+        d.task_next[0] = d.task_next[1] = d.task_next[2] = 0u;
     }
 }
 
@@ -535,12 +633,12 @@ __global__ void k_scatter(Dev d, int n) {
     d.order[d.bin_start[d.bin_of[i]] + d.rank_of[i]] = (uint32_t)i;
 }
 
-// The last substep's grid as updateGrid left it, in the reference's layout.
-__global__ void k_export(const int4* __restrict__ grid, Geo g, SimConsts k, int4* __restrict__ out) {
+// The last substep's grid (already updated in place) in the reference's
+// x-major layout.
+__global__ void k_export(const int4* __restrict__ grid, Geo g, int4* __restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.grid_count) return;
-    out[i] = update_cell(grid[flat_to_addr(g, i)], i, k, wall_hi(k.real_box[0]),
-                         wall_hi(k.real_box[1]), wall_hi(k.real_box[2]));
+    out[i] = grid[flat_to_addr(g, i)];
 }
 
 }  // namespace
@@ -557,7 +655,7 @@ struct SortedEngine {
     int last = 0;         // grid read by the last substep's g2p
     bool primed = false;
     bool has_grid = false;
-    int blocks_p2g2 = 0, blocks_g2p = 0;
+    int blocks_p2g2 = 0, blocks_g2p = 0, blocks_update = 0;
 };
 
 namespace {
@@ -590,11 +688,11 @@ void free_grid_state(SortedEngine* e) {
     e->max_tasks = 0;
 }
 
-int occupancy_blocks(const void* fn) {
+int occupancy_blocks(const void* fn, int threads) {
     int dev = 0, nsm = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kTask, 0) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, 0) != cudaSuccess) return 0;
     if (per < 1) per = 1;
     return nsm * per;
 }
@@ -612,10 +710,13 @@ int sorted_create(SortedEngine** out, int max_particles) {
     if (r == cudaSuccess) r = cudaMalloc(&e->d.dirty_n, 4 * 2);
     if (r == cudaSuccess) r = cudaMalloc(&e->d.ticket, 4);
     if (r == cudaSuccess) r = cudaMalloc(&e->d.ntasks, 4);
+    if (r == cudaSuccess) r = cudaMalloc(&e->d.task_next, 4 * 3);
     if (r == cudaSuccess) {
-        e->blocks_p2g2 = occupancy_blocks((const void*)k_p2g2);
-        e->blocks_g2p = occupancy_blocks((const void*)k_g2p_p2g1<true, false, true>);
-        if (e->blocks_p2g2 <= 0 || e->blocks_g2p <= 0) r = cudaErrorInvalidValue;
+        e->blocks_p2g2 = occupancy_blocks((const void*)k_p2g2, kTask);
+        e->blocks_g2p = occupancy_blocks((const void*)k_g2p_p2g1<true, false>, kTask);
+        e->blocks_update = occupancy_blocks((const void*)k_update, 256);
+        if (e->blocks_p2g2 <= 0 || e->blocks_g2p <= 0 || e->blocks_update <= 0)
+            r = cudaErrorInvalidValue;
     }
     if (r != cudaSuccess) {
         g_err = std::string("sorted_create: ") + cudaGetErrorString(r);
@@ -635,6 +736,7 @@ void sorted_destroy(SortedEngine* e) {
     cudaFree(e->d.dirty_n);
     cudaFree(e->d.ticket);
     cudaFree(e->d.ntasks);
+    cudaFree(e->d.task_next);
     delete e;
 }
 
@@ -658,7 +760,7 @@ int sorted_configure(SortedEngine* e, const SimConsts& k) {
     if (nb * 64 > INT_MAX) return -1;
     g.nbricks = (int)nb;
     const size_t cells = (size_t)nb * 64;
-    const int max_tasks = e->max_particles / kTask + g.nbricks + 2;
+    const int max_tasks = g.nbricks + 2;
     if (cells > e->grid_cells_alloc || g.nbricks > e->bricks_alloc || max_tasks > e->max_tasks) {
         free_grid_state(e);
         for (int b = 0; b < 2; ++b) {
@@ -693,7 +795,7 @@ bool sorted_has_grid(const SortedEngine* e) { return e && e->has_grid; }
         prof->after((id), st);   \
     } while (0)
 
-int sorted_step(SortedEngine* e, const Particles& P, float4* posvel, unsigned long long* oob,
+int sorted_step(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned long long* oob,
                 const SimConsts& k, int substeps, cudaStream_t st, LaunchProfiler* prof) {
     if (!e->configured) {
         g_err = "sorted engine is not configured for this scene";
@@ -714,33 +816,43 @@ int sorted_step(SortedEngine* e, const Particles& P, float4* posvel, unsigned lo
         }
         SE_CUDA(cudaMemsetAsync(e->d.dirty_n, 0, 8, st));
         SE_CUDA(cudaMemsetAsync(e->d.ticket, 0, 4, st));
+        SE_CUDA(cudaMemsetAsync(e->d.task_next, 0, 4 * 3, st));
         SE_CUDA(cudaMemsetAsync(e->d.bin_count, 0, 4 * (size_t)nbins, st));
+        const Particles& P = ps->P[ps->cur];
         LAUNCH(KID_BIN, (k_bin<<<(n + kTask - 1) / kTask, kTask, 0, st>>>(P, g, e->d, n)));
         LAUNCH(KID_SCAN, (k_scan<<<1, kScanThreads, 0, st>>>(e->d, nbins)));
         LAUNCH(KID_SCATTER, (k_scatter<<<(n + 255) / 256, 256, 0, st>>>(e->d, n)));
         e->cur = 0;
         LAUNCH(KID_SORTED_P2G_1,
-               (k_g2p_p2g1<false, false, false>
-                <<<e->blocks_g2p, kTask, 0, st>>>(P, posvel, g, k, e->d, e->cur, e->cur, oob)));
+               (k_g2p_p2g1<false, false><<<e->blocks_g2p, kTask, 0, st>>>(
+                   P, P, ps->id[ps->cur], ps->id[ps->cur], posvel, g, k, e->d, e->cur, e->cur,
+                   oob)));
         SE_CUDA(cudaGetLastError());
         e->primed = true;
     }
     for (int s = 0; s < substeps; ++s) {
         const int cur = e->cur, nxt = cur ^ 1;
+        const int pin = ps->cur, pout = pin ^ 1;
         LAUNCH(KID_SORTED_P2G_2,
-               (k_p2g2<<<e->blocks_p2g2, kTask, 0, st>>>(P, g, k, e->d, cur, oob)));
+               (k_p2g2<<<e->blocks_p2g2, kTask, 0, st>>>(ps->P[pin], g, k, e->d, cur, oob)));
+        LAUNCH(KID_UPDATE_GRID,
+               (k_update<<<e->blocks_update, 256, 0, st>>>(g, k, e->d, cur)));
         if (s == substeps - 1)
             LAUNCH(KID_SORTED_G2P_P2G_1,
-                   (k_g2p_p2g1<true, true, true>
-                    <<<e->blocks_g2p, kTask, 0, st>>>(P, posvel, g, k, e->d, cur, nxt, oob)));
+                   (k_g2p_p2g1<true, true><<<e->blocks_g2p, kTask, 0, st>>>(
+                       ps->P[pin], ps->P[pout], ps->id[pin], ps->id[pout], posvel, g, k, e->d, cur,
+                       nxt, oob)));
         else
             LAUNCH(KID_SORTED_G2P_P2G_1,
-                   (k_g2p_p2g1<true, false, true>
-                    <<<e->blocks_g2p, kTask, 0, st>>>(P, posvel, g, k, e->d, cur, nxt, oob)));
+                   (k_g2p_p2g1<true, false><<<e->blocks_g2p, kTask, 0, st>>>(
+                       ps->P[pin], ps->P[pout], ps->id[pin], ps->id[pout], posvel, g, k, e->d, cur,
+                       nxt, oob)));
         LAUNCH(KID_SCAN, (k_scan<<<1, kScanThreads, 0, st>>>(e->d, nbins)));
         LAUNCH(KID_SCATTER, (k_scatter<<<(n + 255) / 256, 256, 0, st>>>(e->d, n)));
         e->last = cur;
         e->cur = nxt;
+        ps->cur = pout;
+        ps->canonical = false;
     }
     SE_CUDA(cudaGetLastError());
     e->has_grid = true;
@@ -749,13 +861,14 @@ int sorted_step(SortedEngine* e, const Particles& P, float4* posvel, unsigned lo
 
 int sorted_export_grid(SortedEngine* e, const SimConsts& k, int4* out, cudaStream_t st,
                        LaunchProfiler* prof) {
+    (void)k;
     if (!e->configured || !e->has_grid) {
         g_err = "no sorted-engine grid to export";
         return -1;
     }
     const Geo& g = e->geo;
     LAUNCH(KID_EXPORT,
-           (k_export<<<(g.grid_count + 255) / 256, 256, 0, st>>>(e->d.grid[e->last], g, k, out)));
+           (k_export<<<(g.grid_count + 255) / 256, 256, 0, st>>>(e->d.grid[e->last], g, out)));
     SE_CUDA(cudaGetLastError());
     return 0;
 }

@@ -7,15 +7,14 @@
 
 namespace mpm {
 
-// Device-resident scratch of the sorted (fused) engine.
-struct SortState {
-    int nbins;            // number of sort bins (bricks of BIN^3 cells)
-    int bins_x, bins_y, bins_z;
-    uint32_t* bin_of;     // [n] sort key (bin id) of each particle
-    uint32_t* rank_of;    // [n] rank of the particle within its bin
-    uint32_t* bin_count;  // [nbins]
-    uint32_t* bin_start;  // [nbins + 1] exclusive prefix sum of bin_count
-    uint32_t* order;      // [n] particle slots in bin order
+// Two sets of particle streams plus the particle id held by each slot.  P[cur]
+// holds the current state; when `canonical`, slot i holds particle i (the
+// sorted engine keeps particles physically in bin order between substeps).
+struct ParticleStore {
+    Particles P[2];
+    uint32_t* id[2];
+    int cur = 0;
+    bool canonical = true;
 };
 
 // Kernel ids for launch accounting (names in kernel_name()).
@@ -33,6 +32,7 @@ enum KernelId {
     KID_SORTED_P2G_2,
     KID_SORTED_G2P_P2G_1,
     KID_EXPORT,
+    KID_CANONICALIZE,
     KID_COUNT
 };
 
@@ -73,6 +73,11 @@ void launch_update_grid(int4* cells, const SimConsts& k, cudaStream_t st);
 void launch_g2p(const Particles& P, const int4* cells, const SimConsts& k,
                 unsigned long long* oob, cudaStream_t st);
 void launch_copy_position(const Particles& P, float4* posvel, int n, cudaStream_t st);
+
+// dst[id[j]] = src[j] for j < n, and id_dst[i] = i.
+void launch_canonicalize(const Particles& src, const uint32_t* id, const Particles& dst,
+                         uint32_t* id_dst, int n, cudaStream_t st);
+void launch_iota(uint32_t* id, int n, cudaStream_t st);
 
 // Diagnostics.
 void launch_count_nonfinite(const Particles& P, int n, unsigned long long* out, cudaStream_t st);

@@ -9,7 +9,7 @@ const char* kernel_name(int id) {
     static const char* names[KID_COUNT] = {
         "clearGrid", "p2g_1", "p2g_2", "updateGrid", "g2p", "copyPosition",
         "bin", "scan", "scatter", "sorted_p2g_1", "sorted_p2g_2", "sorted_g2p_p2g_1",
-        "export_grid"};
+        "export_grid", "canonicalize"};
     return (id >= 0 && id < KID_COUNT) ? names[id] : "?";
 }
 

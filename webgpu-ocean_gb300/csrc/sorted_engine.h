@@ -21,7 +21,10 @@ int sorted_configure(SortedEngine* e, const SimConsts& k);
 void sorted_invalidate(SortedEngine* e);
 
 // Enqueues `substeps` substeps.  posvel is written by the last one.
-int sorted_step(SortedEngine* e, const Particles& P, float4* posvel, unsigned long long* oob,
+// Enqueues `substeps` substeps on ps->P[ps->cur]; each substep writes the
+// particles, in bin order, to the other buffer and flips ps->cur.  posvel is
+// written (in particle-id order) by the last substep.
+int sorted_step(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned long long* oob,
                 const SimConsts& k, int substeps, cudaStream_t st, LaunchProfiler* prof);
 
 // True once a substep has run since configure/invalidate.
