@@ -181,6 +181,12 @@ int mpm_scene_lattice(float* out_aos80, int n_per_axis, double origin, double sp
  * f32(bits(in[i])) / fm (p2g_2.wgsl:22-24).  Synchronous, host arrays. */
 int mpm_probe_conversions(const float* in, int n, float fm, int32_t* enc_out, float* dec_out);
 
+/* Diagnostic: the packed f32x2 multiply and add the kernels use, against
+ * the scalar IEEE operations.  n (even) floats in a and b; out holds 6n
+ * floats: packed a*b, a+b, (a*b)+a, then scalar a*b, a+b, (a*b)+a (each
+ * product rounded before the add).  Synchronous. */
+int mpm_probe_packed(const float* a, const float* b, int n, float* out);
+
 #ifdef __cplusplus
 }
 #endif

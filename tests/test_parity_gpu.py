@@ -258,3 +258,34 @@ def test_lattice_1m_128(cuda, pkg, oracle_mod, engine):
         ref.execute(2, NTHREADS)
         assert_state_equal(sim, ref, f"{engine} 1M frame {frame}")
     sim.close()
+
+
+def test_packed_f32x2_matches_scalar_ieee(cuda, pkg):
+    """The sorted engine pairs independent products in mul.rn.f32x2 and adds
+    them with scalar add.rn.f32 (ptxas would contract a packed product that
+    feeds a packed add into one FMA rounding); each lane must round exactly
+    like the scalar ops, including subnormal inputs and results, signed
+    zeros, infinities and NaN."""
+    rng = np.random.default_rng(11)
+    n = 1 << 16
+    special = np.array([0.0, -0.0, 1e-45, -1e-45, 1.17549435e-38, 1e-38, 3e-39, np.inf, -np.inf,
+                        np.nan, 1.0, -1.0, 3.4e38, 2 ** -75, 2 ** -60, 1.5, 1e7], dtype=np.float32)
+    a = np.concatenate([np.repeat(special, len(special)), np.tile(special, len(special)),
+                        (rng.standard_normal(n) * np.exp(rng.uniform(-90, 90, n))).astype(np.float32)])
+    b = np.concatenate([np.tile(special, len(special)), np.repeat(special, len(special)),
+                        (rng.standard_normal(n) * np.exp(rng.uniform(-90, 90, n))).astype(np.float32)])
+    if len(a) % 2:
+        a, b = a[:-1], b[:-1]
+    pm, pa, pma, sm, sa, sma = pkg.probe_packed(a, b)
+    with np.errstate(all="ignore"):
+        want_m = (a * b).astype(np.float32)
+        want_a = (a + b).astype(np.float32)
+        want_ma = (want_m + a).astype(np.float32)
+    for got, want, what in [(pm, want_m, "packed mul"), (pa, want_a, "packed add"),
+                            (pma, want_ma, "packed mul then scalar add (no contraction)"),
+                            (sm, want_m, "scalar mul"), (sa, want_a, "scalar add"),
+                            (sma, want_ma, "scalar mul then add (no contraction)")]:
+        nan = np.isnan(want)
+        assert np.array_equal(np.isnan(got), nan), what
+        assert_bits_equal(got[~nan], want[~nan], what)
+    assert (np.abs(want_m[np.isfinite(want_m)]) < 1.17549435e-38).sum() > 0  # subnormals covered

@@ -8,7 +8,7 @@ The directory name is not a Python identifier; load it with
 """
 from . import _lib, build
 from .mlsmpm import (MLSMPMSimulator, MPMError, GridCapacityError, default_params,
-                     probe_conversions, scene_dambreak, scene_lattice)
+                     probe_conversions, probe_packed, scene_dambreak, scene_lattice)
 
 __all__ = ["MLSMPMSimulator", "MPMError", "GridCapacityError", "default_params",
-           "scene_dambreak", "scene_lattice", "probe_conversions", "build", "_lib"]
+           "scene_dambreak", "scene_lattice", "probe_conversions", "probe_packed", "build", "_lib"]

@@ -106,6 +106,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "mpm_scene_lattice": (i32, [fp, i32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_uint64]),
         "mpm_probe_conversions": (i32, [fp, i32, f32, ip, fp]),
+        "mpm_probe_packed": (i32, [fp, fp, i32, fp]),
         "mpm_set_profiling": (i32, [vp, i32]),
         "mpm_kernel_stats": (i32, [vp, ctypes.POINTER(KernelStat), i32]),
         "mpm_launch_count": (i64, [vp]),

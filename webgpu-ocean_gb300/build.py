@@ -3,7 +3,8 @@
 Each .cu file is compiled in parallel for sm_103a only, then linked into one
 shared library with the CUDA runtime linked statically.  Flags that the
 bit-exact arithmetic depends on:
-  -fmad=false                   no FMA contraction in device code
+  -fmad=false, -Xptxas=--fmad=false   no FMA contraction in device code,
+                                 also of packed f32x2 multiplies and adds
   -prec-div=true -prec-sqrt=true  IEEE division (the kernels also use
                                  explicitly rounded intrinsics)
   -Xcompiler -ffp-contract=off  no contraction in host code (scene builders)
@@ -24,10 +25,11 @@ REPO = os.path.dirname(HERE)
 INCLUDE = os.path.join(REPO, "include")
 
 SOURCES = ["capi.cu", "kernels_dispatch.cu", "kernels_sorted.cu", "profiler.cu"]
-HEADERS = ["mpm_math.cuh", "mpm_internal.h", "sorted_engine.h"]
+HEADERS = ["mpm_math.cuh", "mpm_math_x2.cuh", "mpm_internal.h", "sorted_engine.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true",
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xptxas=--fmad=false",
+              "-prec-div=true",
               "-prec-sqrt=true", "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
               "-I" + INCLUDE]
 

@@ -627,4 +627,27 @@ int mpm_probe_conversions(const float* in, int n, float fm, int32_t* enc_out, fl
     return MPM_OK;
 }
 
+int mpm_probe_packed(const float* a, const float* b, int n, float* out) {
+    if (n < 0 || (n % 2) || (n > 0 && (!a || !b || !out))) return fail(MPM_E_INVALID, "bad arguments");
+    if (n == 0) return MPM_OK;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(MPM_E_NO_DEVICE, "no CUDA device");
+    }
+    float* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(float) * 8 * (size_t)n);
+    if (e == cudaSuccess) e = cudaMemcpy(d, a, sizeof(float) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + n, b, sizeof(float) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        launch_packed_probe(d, d + n, n / 2, d + 2 * (size_t)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpy(out, d + 2 * (size_t)n, sizeof(float) * 6 * (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "mpm_probe_packed");
+    return MPM_OK;
+}
+
 }  // extern "C"

@@ -5,6 +5,7 @@
 // the sorted engine (kernels_sorted.cu) is the fast path and must agree with
 // it bit for bit.
 #include "mpm_internal.h"
+#include "mpm_math_x2.cuh"
 
 namespace mpm {
 
@@ -153,7 +154,38 @@ __global__ void k_convert_probe(const float* __restrict__ in, int n, float fm,
     dec_out[i] = dec(__float_as_int(in[i]), fm);
 }
 
+// Packed (a[2i], a[2i+1]) op (b[2i], b[2i+1]) for op = mul, add and the
+// pattern the kernels use for sums of products (packed multiply, scalar
+// adds: a*b + a), each next to the scalar operations.
+__global__ void k_packed_probe(const float* __restrict__ a, const float* __restrict__ b, int npairs,
+                               float* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npairs) return;
+    const size_t n = 2 * (size_t)npairs;
+    const f2 x = pk(a[2 * i], a[2 * i + 1]), y = pk(b[2 * i], b[2 * i + 1]);
+    upk(mul2(x, y), out[2 * i], out[2 * i + 1]);
+    upk(add2(x, y), out[n + 2 * i], out[n + 2 * i + 1]);
+    {   // the kernels' pattern: packed product, scalar adds
+        float p0, p1;
+        upk(mul2(x, y), p0, p1);
+        out[2 * n + 2 * i] = fadd(p0, a[2 * i]);
+        out[2 * n + 2 * i + 1] = fadd(p1, a[2 * i + 1]);
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const float p = a[2 * i + h], q = b[2 * i + h];
+        out[3 * n + 2 * i + h] = fmul(p, q);
+        out[4 * n + 2 * i + h] = fadd(p, q);
+        out[5 * n + 2 * i + h] = fadd(fmul(p, q), p);
+    }
+}
+
 }  // namespace
+
+void launch_packed_probe(const float* a, const float* b, int npairs, float* out6) {
+    if (npairs <= 0) return;
+    k_packed_probe<<<blocks_for(npairs), kThreads>>>(a, b, npairs, out6);
+}
 
 void launch_clear_grid(int4* cells, int grid_count, cudaStream_t st) {
     if (grid_count <= 0) return;

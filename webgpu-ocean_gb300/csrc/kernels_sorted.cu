@@ -32,25 +32,40 @@
 #include <string>
 
 #include "mpm_internal.h"
+#include "mpm_math_x2.cuh"
 #include "sorted_engine.h"
 
 namespace mpm {
 
 namespace {
 
-constexpr int kTask = 256;       // particles per task == threads per CTA
+constexpr int kTask = 256;       // particles per chunk == threads per CTA
+// Arenas are padded so that the 32 lanes of a warp, holding particles of 32
+// different cells of a brick (see deal_pos), hit 32 different banks for
+// every stencil offset: x-stride 80 = 16 (mod 32) and y-stride 12 for the
+// 6^3 arena; x-stride 68 = 4 (mod 32) and y-stride 8 for the 8^3 arena.
 constexpr int kA = 6;            // p2g_2 / g2p arena edge: brick + 1-cell halo
-constexpr int kA3 = kA * kA * kA;
+constexpr int kSYA = 12, kSXA = 80, kNA = kA * kSXA;
 constexpr int kB = 8;            // next-p2g_1 arena edge: brick + 2-cell halo
-constexpr int kB3 = kB * kB * kB;
+constexpr int kSYB = 8, kSXB = 68, kNB = kB * kSXB;
+constexpr int kMaxSort = 1024;   // bricks with more particles skip the cell sort
 constexpr int kScanThreads = 1024;
 
 // Minimum resident CTAs per SM requested from the register allocator.
 #ifndef MPM_G2P_MIN_BLOCKS
-#define MPM_G2P_MIN_BLOCKS 3
+#define MPM_G2P_MIN_BLOCKS 4
 #endif
 #ifndef MPM_P2G2_MIN_BLOCKS
 #define MPM_P2G2_MIN_BLOCKS 3
+#endif
+// 1: arena stage bodies use packed f32x2 products (mpm_math_x2.cuh).
+#ifndef MPM_PACKED_MATH
+#define MPM_PACKED_MATH 1
+#endif
+// 1: p2g_2 counting-sorts each brick's particles by cell before dealing them
+// to lanes (fewer shared-memory atomic collisions, more integer work).
+#ifndef MPM_CELL_SORT
+#define MPM_CELL_SORT 1
 #endif
 
 thread_local std::string g_err;
@@ -201,15 +216,31 @@ __device__ __forceinline__ void clear_dirty(const Dev& d, int gi) {
     }
 }
 
-// Arena cell li of an E^3 arena at origin o -> grid coordinates.
-template <int E>
-__device__ __forceinline__ void arena_cell(int li, int ox, int oy, int oz, int& x, int& y, int& z) {
-    const int ax = li / (E * E);
-    const int r = li - ax * (E * E);
-    const int ay = r / E;
+// Arena slot li (strides SX, SY, 1) at origin o -> grid coordinates; false
+// for padding slots.
+template <int E, int SX, int SY>
+__device__ __forceinline__ bool arena_cell(int li, int ox, int oy, int oz, int& x, int& y, int& z) {
+    const int ax = li / SX;
+    const int r = li - ax * SX;
+    const int ay = r / SY;
+    const int az = r - ay * SY;
     x = ox + ax;
     y = oy + ay;
-    z = oz + (r - ay * E);
+    z = oz + az;
+    return ay < E && az < E;
+}
+
+// Thread t of a chunk of m particles (bin order, cell-sorted within the
+// brick) -> the chunk position it processes, or -1.  Lane l of warp w takes
+// position l*nw + w: a warp gathers particles from ~32 different cells
+// rather than 4 cells of 8, so shared-memory atomics rarely meet at one
+// address.
+__device__ __forceinline__ int deal_pos(int t, int m) {
+    const int nw = (m + 31) >> 5;
+    const int w = t >> 5;
+    if (w >= nw) return -1;
+    const int p = (t & 31) * nw + w;
+    return p < m ? p : -1;
 }
 
 // Global-path mass source (flat indices, as the reference's shaders address).
@@ -225,12 +256,18 @@ struct GlobalMass {
 };
 
 // ---------------------------------------------------------------------------
-// p2g_2 (p2g_2.wgsl:30-94) over tasks; also clears grid `cur ^ 1`.
+// p2g_2 (p2g_2.wgsl:30-94) over tasks; also clears grid `cur ^ 1`.  Each
+// brick's particles are first counting-sorted by cell (in shared memory);
+// the sorted order is written back to `order` for g2p.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
     k_p2g2(Particles P, Geo g, SimConsts k, Dev d, int cur, unsigned long long* oob) {
-    __shared__ float s_mass[kA3];
-    __shared__ int s_q[3][kA3];
+    __shared__ float s_mass[kNA];
+    __shared__ int s_q[3][kNA];
+    __shared__ uint32_t s_slot[kMaxSort];
+    __shared__ uint32_t s_key[kMaxSort];
+    __shared__ uint32_t s_sorted[kMaxSort];
+    __shared__ int s_cnt[65], s_start[65];
     __shared__ int s_task[2];
 
     clear_dirty(d, cur ^ 1);
@@ -238,6 +275,7 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
     int4* __restrict__ grid = d.grid[cur];
     unsigned bad = 0;
     const int ntasks = (int)__ldcg(d.ntasks);
+    if (threadIdx.x < 65) s_cnt[threadIdx.x] = 0;
     if (threadIdx.x == 0) s_task[0] = claim_task(d, kCtrP2G2);
     __syncthreads();
     int buf = 0;
@@ -245,17 +283,15 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
     while (t < ntasks) {
         if (threadIdx.x == 0) s_task[buf ^ 1] = claim_task(d, kCtrP2G2);
         const Task task = d.tasks[t];
-        int ox = 0, oy = 0, oz = 0;
+        const bool sort = MPM_CELL_SORT && task.brick >= 0 && task.count <= kMaxSort;
+        int tbx = 0, tby = 0, tbz = 0;
         if (task.brick >= 0) {
-            brick_coords(g, task.brick, ox, oy, oz);
-            ox = 4 * ox - 1;
-            oy = 4 * oy - 1;
-            oz = 4 * oz - 1;
-            for (int li = threadIdx.x; li < kA3; li += kTask) {
+            brick_coords(g, task.brick, tbx, tby, tbz);
+            const int ox = 4 * tbx - 1, oy = 4 * tby - 1, oz = 4 * tbz - 1;
+            for (int li = threadIdx.x; li < kNA; li += kTask) {
                 int x, y, z;
-                arena_cell<kA>(li, ox, oy, oz, x, y, z);
                 int m = 0;
-                if (cell_exists(g, x, y, z))
+                if (arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z) && cell_exists(g, x, y, z))
                     m = __ldcg(reinterpret_cast<const int*>(grid + brick_addr(g, x, y, z)) + 3);
                 s_mass[li] = dec(m, k.fm);
                 s_q[0][li] = 0;
@@ -263,31 +299,80 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
                 s_q[2][li] = 0;
             }
         }
+        if (sort) {
+            for (int j = threadIdx.x; j < task.count; j += kTask) {
+                const uint32_t slot = d.order[task.first + j];
+                const float4 a = P.p0[slot];
+                const float x[3] = {a.x, a.y, a.z};
+                int bx, by, bz;
+                base_cell(x, bx, by, bz);
+                const int ax = bx - 4 * tbx, ay = by - 4 * tby, az = bz - 4 * tbz;
+                const bool in = regular_base(g, bx, by, bz) && (unsigned)ax <= 3u &&
+                                (unsigned)ay <= 3u && (unsigned)az <= 3u;
+                const int c = in ? (ax * 16 + ay * 4 + az) : 64;
+                const int r = atomicAdd(&s_cnt[c], 1);
+                s_slot[j] = slot;
+                s_key[j] = (uint32_t)c | ((uint32_t)r << 7);
+            }
+        }
         __syncthreads();
-        for (int j = threadIdx.x; j < task.count; j += kTask) {
-            const int slot = (int)d.order[task.first + j];
+        if (sort) {
+            if (threadIdx.x < 32) {
+                const int l = threadIdx.x;
+                const int v0 = s_cnt[2 * l], v1 = s_cnt[2 * l + 1];
+                int incl = v0 + v1;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (l >= o) incl += y;
+                }
+                const int excl = incl - v0 - v1;
+                s_start[2 * l] = excl;
+                s_start[2 * l + 1] = excl + v0;
+                if (l == 31) s_start[64] = incl;
+            }
+            __syncthreads();
+            for (int j = threadIdx.x; j < task.count; j += kTask) {
+                const uint32_t key = s_key[j];
+                const int pos = s_start[key & 127u] + (int)(key >> 7);
+                s_sorted[pos] = s_slot[j];
+                d.order[task.first + pos] = s_slot[j];
+            }
+            __syncthreads();
+        }
+        for (int base = 0; base < task.count; base += kTask) {
+            const int p = deal_pos(threadIdx.x, min(kTask, task.count - base));
+            if (p < 0) continue;
+            const int j = base + p;
+            const int slot = sort ? (int)s_sorted[j] : (int)d.order[task.first + j];
             PState s;
             unpack_xC(P.p0[slot], P.p1[slot], P.p2[slot], s);
             int bx, by, bz;
             base_cell(s.x, bx, by, bz);
-            const int ax = bx - 1 - ox, ay = by - 1 - oy, az = bz - 1 - oz;
+            const int ax = bx - 4 * tbx, ay = by - 4 * tby, az = bz - 4 * tbz;
             const bool in_arena = task.brick >= 0 && regular_base(g, bx, by, bz) &&
-                                  (unsigned)ax <= (unsigned)(kA - 3) &&
-                                  (unsigned)ay <= (unsigned)(kA - 3) &&
-                                  (unsigned)az <= (unsigned)(kA - 3);
+                                  (unsigned)ax <= 3u && (unsigned)ay <= 3u && (unsigned)az <= 3u;
             if (in_arena) {
-                const int li0 = (ax * kA + ay) * kA + az;
-                p2g2_particle(
-                    s, k,
-                    [&](int, int gx, int gy, int gz) -> float {
-                        return s_mass[li0 + (gx * kA + gy) * kA + gz];
-                    },
-                    [&](int, int gx, int gy, int gz, int mx, int my, int mz) {
-                        const int li = li0 + (gx * kA + gy) * kA + gz;
-                        atomicAdd(&s_q[0][li], mx);
-                        atomicAdd(&s_q[1][li], my);
-                        atomicAdd(&s_q[2][li], mz);
-                    });
+                // stencil corner (base - 1) relative to the arena origin (brick - 1)
+                const int li0 = ax * kSXA + ay * kSYA + az;
+                auto mass = [&](int gx, int gy, int gz) -> float {
+                    return s_mass[li0 + gx * kSXA + gy * kSYA + gz];
+                };
+                auto sink = [&](int gx, int gy, int gz, int mx, int my, int mz) {
+                    const int li = li0 + gx * kSXA + gy * kSYA + gz;
+                    atomicAdd(&s_q[0][li], mx);
+                    atomicAdd(&s_q[1][li], my);
+                    atomicAdd(&s_q[2][li], mz);
+                };
+                if (MPM_PACKED_MATH) {
+                    p2g2_particle_x2(s, k, mass, sink);
+                } else {
+                    p2g2_particle(
+                        s, k, [&](int, int gx, int gy, int gz) { return mass(gx, gy, gz); },
+                        [&](int, int gx, int gy, int gz, int mx, int my, int mz) {
+                            sink(gx, gy, gz, mx, my, mz);
+                        });
+                }
             } else {
                 p2g2_particle(
                     s, k, GlobalMass{g, grid, k.fm, bad},
@@ -304,11 +389,12 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
         }
         __syncthreads();
         if (task.brick >= 0) {
-            for (int li = threadIdx.x; li < kA3; li += kTask) {
+            const int ox = 4 * tbx - 1, oy = 4 * tby - 1, oz = 4 * tbz - 1;
+            for (int li = threadIdx.x; li < kNA; li += kTask) {
                 const int q0 = s_q[0][li], q1 = s_q[1][li], q2 = s_q[2][li];
                 if ((q0 | q1 | q2) == 0) continue;
                 int x, y, z;
-                arena_cell<kA>(li, ox, oy, oz, x, y, z);
+                if (!arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z)) continue;
                 if (!cell_exists(g, x, y, z)) continue;  // unreachable for regular particles
                 int* c = reinterpret_cast<int*>(grid + brick_addr(g, x, y, z));
                 if (q0) atomicAdd(c + 0, q0);
@@ -316,6 +402,7 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
                 if (q2) atomicAdd(c + 2, q2);
             }
         }
+        if (threadIdx.x < 65) s_cnt[threadIdx.x] = 0;
         __syncthreads();
         buf ^= 1;
         t = s_task[buf];
@@ -361,8 +448,8 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
     k_g2p_p2g1(Particles Pin, Particles Pout, const uint32_t* __restrict__ id_in,
                uint32_t* __restrict__ id_out, float4* __restrict__ posvel, Geo g, SimConsts k,
                Dev d, int src, int dst, unsigned long long* oob) {
-    __shared__ float4 s_v[kA3];
-    __shared__ int s_a[4][kB3];
+    __shared__ float4 s_v[kNA];
+    __shared__ int s_a[4][kNB];
     __shared__ int s_touch[27];
     __shared__ int s_task[2];
 
@@ -383,15 +470,17 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
             brick_coords(g, task.brick, tbx, tby, tbz);
             const int ox = 4 * tbx - 1, oy = 4 * tby - 1, oz = 4 * tbz - 1;
             if (DO_G2P) {
-                for (int li = threadIdx.x; li < kA3; li += kTask) {
+                for (int li = threadIdx.x; li < kNA; li += kTask) {
                     int x, y, z;
-                    arena_cell<kA>(li, ox, oy, oz, x, y, z);
                     int4 c = make_int4(0, 0, 0, 0);
-                    if (cell_exists(g, x, y, z)) c = __ldcg(gsrc + brick_addr(g, x, y, z));
-                    s_v[li] = make_float4(dec(c.x, k.fm), dec(c.y, k.fm), dec(c.z, k.fm), 0.0f);
+                    if (arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z) &&
+                        cell_exists(g, x, y, z))
+                        c = __ldcg(gsrc + brick_addr(g, x, y, z));
+                    const float vz = dec(c.z, k.fm);
+                    s_v[li] = make_float4(dec(c.x, k.fm), dec(c.y, k.fm), vz, vz);
                 }
             }
-            for (int li = threadIdx.x; li < kB3; li += kTask) {
+            for (int li = threadIdx.x; li < kNB; li += kTask) {
                 s_a[0][li] = 0;
                 s_a[1][li] = 0;
                 s_a[2][li] = 0;
@@ -402,9 +491,9 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
         __syncthreads();
 
         for (int base = 0; base < task.count; base += kTask) {
-            const int j = base + (int)threadIdx.x;
-            const bool active = j < task.count;
-            const int jo = task.first + j;  // the particle's position in bin order
+            const int p = deal_pos(threadIdx.x, min(kTask, task.count - base));
+            const bool active = p >= 0;
+            const int jo = task.first + base + (active ? p : 0);  // position in bin order
             const int slot = active ? (int)d.order[jo] : 0;
             PState s;
             if (DO_G2P) {
@@ -418,13 +507,21 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
                                           (unsigned)ax <= 3u && (unsigned)ay <= 3u &&
                                           (unsigned)az <= 3u;
                     if (in_arena) {
-                        const int li0 = (ax * kA + ay) * kA + az;
-                        g2p_particle(s, k, [&](int, int gx, int gy, int gz, float out[3]) {
-                            const float4 v = s_v[li0 + (gx * kA + gy) * kA + gz];
-                            out[0] = v.x;
-                            out[1] = v.y;
-                            out[2] = v.z;
-                        });
+                        const int li0 = ax * kSXA + ay * kSYA + az;
+                        if (MPM_PACKED_MATH) {
+                            g2p_particle_x2(s, k, [&](int gx, int gy, int gz, f2& gxy, f2& gzz) {
+                                const float4 v = s_v[li0 + gx * kSXA + gy * kSYA + gz];
+                                gxy = pk(v.x, v.y);
+                                gzz = pk(v.z, v.w);
+                            });
+                        } else {
+                            g2p_particle(s, k, [&](int, int gx, int gy, int gz, float out[3]) {
+                                const float4 v = s_v[li0 + gx * kSXA + gy * kSYA + gz];
+                                out[0] = v.x;
+                                out[1] = v.y;
+                                out[2] = v.z;
+                            });
+                        }
                     } else {
                         g2p_particle(s, k, [&](int idx, int, int, int, float out[3]) {
                             int4 c = make_int4(0, 0, 0, 0);
@@ -459,15 +556,21 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
                                       (unsigned)ay <= (unsigned)(kB - 3) &&
                                       (unsigned)az <= (unsigned)(kB - 3);
                 if (in_arena) {
-                    const int li0 = (ax * kB + ay) * kB + az;
-                    p2g1_particle(s, k,
-                                  [&](int, int gx, int gy, int gz, int m, int vx, int vy, int vz) {
-                                      const int li = li0 + (gx * kB + gy) * kB + gz;
-                                      atomicAdd(&s_a[3][li], m);
-                                      atomicAdd(&s_a[0][li], vx);
-                                      atomicAdd(&s_a[1][li], vy);
-                                      atomicAdd(&s_a[2][li], vz);
-                                  });
+                    const int li0 = ax * kSXB + ay * kSYB + az;
+                    auto sink = [&](int gx, int gy, int gz, int m, int vx, int vy, int vz) {
+                        const int li = li0 + gx * kSXB + gy * kSYB + gz;
+                        atomicAdd(&s_a[3][li], m);
+                        atomicAdd(&s_a[0][li], vx);
+                        atomicAdd(&s_a[1][li], vy);
+                        atomicAdd(&s_a[2][li], vz);
+                    };
+                    if (MPM_PACKED_MATH) {
+                        p2g1_particle_x2(s, k, sink);
+                    } else {
+                        p2g1_particle(s, k,
+                                      [&](int, int gx, int gy, int gz, int m, int vx, int vy,
+                                          int vz) { sink(gx, gy, gz, m, vx, vy, vz); });
+                    }
                 } else {
                     p2g1_particle(s, k,
                                   [&](int idx, int, int, int, int m, int vx, int vy, int vz) {
@@ -487,11 +590,11 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
         __syncthreads();
         if (task.brick >= 0) {
             const int ox = 4 * tbx - 2, oy = 4 * tby - 2, oz = 4 * tbz - 2;
-            for (int li = threadIdx.x; li < kB3; li += kTask) {
+            for (int li = threadIdx.x; li < kNB; li += kTask) {
                 const int q0 = s_a[0][li], q1 = s_a[1][li], q2 = s_a[2][li], q3 = s_a[3][li];
                 if ((q0 | q1 | q2 | q3) == 0) continue;
                 int x, y, z;
-                arena_cell<kB>(li, ox, oy, oz, x, y, z);
+                if (!arena_cell<kB, kSXB, kSYB>(li, ox, oy, oz, x, y, z)) continue;
                 if (!cell_exists(g, x, y, z)) continue;  // unreachable for regular particles
                 int* c = reinterpret_cast<int*>(gdst + brick_addr(g, x, y, z));
                 if (q0) atomicAdd(c + 0, q0);
@@ -532,13 +635,11 @@ __global__ void __launch_bounds__(kTask) k_bin(Particles P, Geo g, Dev d, int n)
     count_bin(d, active, active ? i : 0, bin_key(g, reg, bx, by, bz));
 }
 
-// Exclusive scan of the bin counts -> bin_start and the task list; zeroes the
-// counts for the next binning.  One CTA walks the bins in chunks of 8192:
-// coalesced loads into shared memory, 8 consecutive bins per thread, a
-// block-wide scan of (particles, tasks), coalesced stores.
-constexpr int kScanPer = 8;
-constexpr int kScanChunk = kScanThreads * kScanPer;
-
+// Exclusive scan of the bin counts -> bin_start and the task list (one task
+// per non-empty bin).  CTA c scans bins [c*1024, (c+1)*1024); it finds its
+// starting offsets by reducing all earlier counts itself (a few KB to a few
+// hundred KB from L2), so no CTA waits on another.  The counts are zeroed
+// by k_scatter, which runs next.
 __device__ __forceinline__ void block_scan2(uint32_t& a, uint32_t& b, uint32_t* s_a, uint32_t* s_b,
                                             uint32_t& tot_a, uint32_t& tot_b) {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -572,63 +673,52 @@ __device__ __forceinline__ void block_scan2(uint32_t& a, uint32_t& b, uint32_t* 
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, int nbins) {
-    __shared__ uint4 s_buf4[kScanChunk / 4];
     __shared__ uint32_t s_a[32], s_b[32];
-    uint32_t* s_buf = reinterpret_cast<uint32_t*>(s_buf4);
-    uint32_t carry_p = 0, carry_t = 0;
-    for (int base = 0; base < nbins; base += kScanChunk) {
-        const int len = min(kScanChunk, nbins - base);
-        for (int i = threadIdx.x; i < kScanChunk; i += kScanThreads)
-            s_buf[i] = i < len ? d.bin_count[base + i] : 0u;
-        __syncthreads();
-        const uint4 q0 = s_buf4[2 * threadIdx.x], q1 = s_buf4[2 * threadIdx.x + 1];
-        const uint32_t c[kScanPer] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
-        uint32_t sp = 0, st = 0;
-#pragma unroll
-        for (int k = 0; k < kScanPer; ++k) {
-            sp += c[k];
-            st += c[k] ? 1u : 0u;
+    const int base = blockIdx.x * kScanThreads;
+    // counts of all bins before this CTA's range (particles, non-empty bins)
+    uint32_t pre_p = 0, pre_t = 0;
+    {
+        const uint4* c4 = reinterpret_cast<const uint4*>(d.bin_count);
+        const int n4 = base / 4;  // base is a multiple of 1024
+        for (int i = threadIdx.x; i < n4; i += kScanThreads) {
+            const uint4 q = __ldcg(c4 + i);
+            pre_p += q.x + q.y + q.z + q.w;
+            pre_t += (q.x != 0u) + (q.y != 0u) + (q.z != 0u) + (q.w != 0u);
         }
-        uint32_t tot_p, tot_t;
-        block_scan2(sp, st, s_a, s_b, tot_p, tot_t);
-        uint32_t pc = carry_p + sp, pt = carry_t + st;
-        uint32_t starts[kScanPer];
-#pragma unroll
-        for (int k = 0; k < kScanPer; ++k) {
-            starts[k] = pc;
-            if (c[k]) {
-                const int bin = base + (int)threadIdx.x * kScanPer + k;
-                Task tk;
-                tk.first = (int)pc;
-                tk.count = (int)c[k];
-                tk.brick = bin == nbins - 1 ? -1 : bin;
-                tk.pad = 0;
-                d.tasks[pt] = tk;
-                ++pt;
-            }
-            pc += c[k];
-        }
-        __syncthreads();  // every thread has read its counts from s_buf
-        s_buf4[2 * threadIdx.x] = make_uint4(starts[0], starts[1], starts[2], starts[3]);
-        s_buf4[2 * threadIdx.x + 1] = make_uint4(starts[4], starts[5], starts[6], starts[7]);
-        __syncthreads();
-        for (int i = threadIdx.x; i < len; i += kScanThreads) {
-            d.bin_start[base + i] = s_buf[i];
-            d.bin_count[base + i] = 0u;
-        }
-        carry_p += tot_p;
-        carry_t += tot_t;
-        __syncthreads();  // s_buf and s_a/s_b are reused by the next chunk
+        uint32_t tp, tt;
+        block_scan2(pre_p, pre_t, s_a, s_b, tp, tt);
+        pre_p = tp;
+        pre_t = tt;
     }
-    if (threadIdx.x == 0) {
-        d.bin_start[nbins] = carry_p;
-        *d.ntasks = carry_t;
-        d.task_next[0] = d.task_next[1] = d.task_next[2] = 0u;
+    __syncthreads();  // s_a/s_b reused below
+    const int bin = base + (int)threadIdx.x;
+    const uint32_t c = bin < nbins ? __ldcg(d.bin_count + bin) : 0u;
+    uint32_t ep = c, et = c ? 1u : 0u, tot_p, tot_t;
+    block_scan2(ep, et, s_a, s_b, tot_p, tot_t);
+    if (bin < nbins) {
+        const uint32_t start = pre_p + ep;
+        d.bin_start[bin] = start;
+        if (c) {
+            Task tk;
+            tk.first = (int)start;
+            tk.count = (int)c;
+            tk.brick = bin == nbins - 1 ? -1 : bin;
+            tk.pad = 0;
+            d.tasks[pre_t + et] = tk;
+        }
     }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+        d.bin_start[nbins] = pre_p + tot_p;
+        *d.ntasks = pre_t + tot_t;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.task_next[0] = d.task_next[1] = d.task_next[2] = 0u;
 }
 
-__global__ void k_scatter(Dev d, int n) {
+// order[] from bin_start/bin_of/rank_of; also zeroes the bin counts for the
+// next binning.
+__global__ void k_scatter(Dev d, int n, int nbins) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nbins) d.bin_count[i] = 0u;
     if (i >= n) return;
     d.order[d.bin_start[d.bin_of[i]] + d.rank_of[i]] = (uint32_t)i;
 }
@@ -768,7 +858,7 @@ int sorted_configure(SortedEngine* e, const SimConsts& k) {
             SE_CUDA(cudaMalloc(&e->d.dirty_flag[b], 4 * (size_t)g.nbricks));
             SE_CUDA(cudaMalloc(&e->d.dirty_list[b], 4 * (size_t)g.nbricks));
         }
-        SE_CUDA(cudaMalloc(&e->d.bin_count, 4 * ((size_t)g.nbricks + 1)));
+        SE_CUDA(cudaMalloc(&e->d.bin_count, 4 * ((size_t)g.nbricks + 1 + kScanThreads)));
         SE_CUDA(cudaMalloc(&e->d.bin_start, 4 * ((size_t)g.nbricks + 2)));
         SE_CUDA(cudaMalloc(&e->d.tasks, sizeof(Task) * (size_t)max_tasks));
         e->grid_cells_alloc = cells;
@@ -820,8 +910,8 @@ int sorted_step(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned lon
         SE_CUDA(cudaMemsetAsync(e->d.bin_count, 0, 4 * (size_t)nbins, st));
         const Particles& P = ps->P[ps->cur];
         LAUNCH(KID_BIN, (k_bin<<<(n + kTask - 1) / kTask, kTask, 0, st>>>(P, g, e->d, n)));
-        LAUNCH(KID_SCAN, (k_scan<<<1, kScanThreads, 0, st>>>(e->d, nbins)));
-        LAUNCH(KID_SCATTER, (k_scatter<<<(n + 255) / 256, 256, 0, st>>>(e->d, n)));
+        LAUNCH(KID_SCAN, (k_scan<<<(nbins + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(e->d, nbins)));
+        LAUNCH(KID_SCATTER, (k_scatter<<<(max(n, nbins) + 255) / 256, 256, 0, st>>>(e->d, n, nbins)));
         e->cur = 0;
         LAUNCH(KID_SORTED_P2G_1,
                (k_g2p_p2g1<false, false><<<e->blocks_g2p, kTask, 0, st>>>(
@@ -847,8 +937,8 @@ int sorted_step(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned lon
                    (k_g2p_p2g1<true, false><<<e->blocks_g2p, kTask, 0, st>>>(
                        ps->P[pin], ps->P[pout], ps->id[pin], ps->id[pout], posvel, g, k, e->d, cur,
                        nxt, oob)));
-        LAUNCH(KID_SCAN, (k_scan<<<1, kScanThreads, 0, st>>>(e->d, nbins)));
-        LAUNCH(KID_SCATTER, (k_scatter<<<(n + 255) / 256, 256, 0, st>>>(e->d, n)));
+        LAUNCH(KID_SCAN, (k_scan<<<(nbins + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(e->d, nbins)));
+        LAUNCH(KID_SCATTER, (k_scatter<<<(max(n, nbins) + 255) / 256, 256, 0, st>>>(e->d, n, nbins)));
         e->last = cur;
         e->cur = nxt;
         ps->cur = pout;

@@ -81,6 +81,7 @@ void launch_iota(uint32_t* id, int n, cudaStream_t st);
 
 // Diagnostics.
 void launch_count_nonfinite(const Particles& P, int n, unsigned long long* out, cudaStream_t st);
+void launch_packed_probe(const float* a, const float* b, int npairs, float* out6);
 void launch_convert_probe(const float* in, int n, float fm, int* enc_out, float* dec_out,
                           cudaStream_t st);
 

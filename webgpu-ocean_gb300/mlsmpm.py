@@ -269,3 +269,17 @@ def probe_conversions(values: np.ndarray, fm: float = 1e7):
                                           enc.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
                                           dec.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
     return enc, dec
+
+
+def probe_packed(a: np.ndarray, b: np.ndarray):
+    """Packed f32x2 ops on the device vs the scalar ops: returns
+    (packed_mul, packed_add, packed_muladd, scalar_mul, scalar_add,
+    scalar_muladd), muladd = (a*b)+a with the product rounded first."""
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    b = np.ascontiguousarray(b, dtype=np.float32)
+    n = len(a)
+    out = np.zeros(6 * n, dtype=np.float32)
+    fptr = ctypes.POINTER(ctypes.c_float)
+    _check(L.load().mpm_probe_packed(a.ctypes.data_as(fptr), b.ctypes.data_as(fptr), n,
+                                     out.ctypes.data_as(fptr)))
+    return tuple(out[i * n:(i + 1) * n] for i in range(6))
