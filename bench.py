@@ -145,6 +145,22 @@ def dist_setup():
     return world, rank, local
 
 
+def reduce_max(x: float, dist, device: str) -> float:
+    """Max of a per-rank time over all ranks (identity without a process group)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world: int, particles: int, steps: int, slowest_ms: float) -> float:
+    """Whole-job particle-substeps/s when each of `world` ranks runs its own
+    replica: every rank's units over the slowest rank's time."""
+    return world * particles * SUBSTEPS * steps / (slowest_ms / 1e3)
+
+
 def run_reference(args) -> None:
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -212,11 +228,7 @@ def run_ours(args) -> None:
             dist.barrier()
 
     def max_over_ranks(x: float) -> float:
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(x, dist, "cuda")
 
     stream = torch.cuda.Stream()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
@@ -254,7 +266,7 @@ def run_ours(args) -> None:
     clocks = sampler.stop()
     dev_ms = sum(a.elapsed_time(b) for a, b in ev)
     dev_ms = max_over_ranks(dev_ms)
-    value = world * n * SUBSTEPS * K / (dev_ms / 1e3)
+    value = replica_throughput(world, n, K, dev_ms)
 
     if args.quick:
         if rank == 0:
@@ -313,7 +325,7 @@ def run_ours(args) -> None:
     torch.cuda.synchronize()
     barrier()
     e2e_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev2))
-    e2e_value = world * n * SUBSTEPS * K / (e2e_ms / 1e3)
+    e2e_value = replica_throughput(world, n, K, e2e_ms)
     assert np.isfinite(host_out[:, 0:3]).all(), "posvel read back non-finite positions"
     sim.close()
 
