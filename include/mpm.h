@@ -187,6 +187,25 @@ int mpm_probe_conversions(const float* in, int n, float fm, int32_t* enc_out, fl
  * product rounded before the add).  Synchronous. */
 int mpm_probe_packed(const float* a, const float* b, int n, float* out);
 
+/*
+ * No counterpart in the reference.  The watchdog scan of mpm_check_health
+ * over a caller-owned device buffer, allocating nothing: for callers that
+ * cannot call cudaMalloc, such as a host stepping the solver from its
+ * per-frame loop (cudaMalloc/cudaFree may synchronize the device and take
+ * unbounded time) or a plugin host that owns all device memory.  Counts the
+ * records among n (each stride_floats floats, 20 for the 80-byte particle
+ * layout) that hold a non-finite value and writes the count to *count_out
+ * (device memory), asynchronously on `stream`, on the current device.
+ * Limit: n <= 16,777,216 records; larger n returns MPM_E_CAPACITY.
+ * Scratch: a fixed 512 KiB device array inside the library, which every GPU
+ * that loads the library holds until exit.  The first call on a device looks
+ * up that array's device address (cudaGetSymbolAddress) and zeroes its
+ * ticket synchronously; make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race.
+ */
+int mpm_count_nonfinite_noalloc(const float* records, int stride_floats, int n,
+                                int64_t* count_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -107,6 +107,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
                                     ctypes.c_uint64]),
         "mpm_probe_conversions": (i32, [fp, i32, f32, ip, fp]),
         "mpm_probe_packed": (i32, [fp, fp, i32, fp]),
+        "mpm_count_nonfinite_noalloc": (i32, [vp, i32, i32, vp, vp]),
         "mpm_set_profiling": (i32, [vp, i32]),
         "mpm_kernel_stats": (i32, [vp, ctypes.POINTER(KernelStat), i32]),
         "mpm_launch_count": (i64, [vp]),

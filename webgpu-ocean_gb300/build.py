@@ -24,7 +24,7 @@ LIB = os.path.join(BUILD, "libmpm.so")
 REPO = os.path.dirname(HERE)
 INCLUDE = os.path.join(REPO, "include")
 
-SOURCES = ["capi.cu", "kernels_dispatch.cu", "kernels_sorted.cu", "profiler.cu"]
+SOURCES = ["capi.cu", "kernels_dispatch.cu", "kernels_sorted.cu", "profiler.cu", "noalloc.cu"]
 HEADERS = ["mpm_math.cuh", "mpm_math_x2.cuh", "mpm_internal.h", "sorted_engine.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

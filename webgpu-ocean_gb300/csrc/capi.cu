@@ -143,6 +143,11 @@ int f2i_trunc_sat(float x) {
 
 }  // namespace
 
+namespace mpm {
+// Lets other translation units report a message through mpm_last_error().
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace mpm
+
 // ---------------------------------------------------------------------------
 // The handle
 // ---------------------------------------------------------------------------
