@@ -192,6 +192,12 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# DRAM bytes (read + write) per launch of the dominant kernel, mean of its two
+# variants, from one ncu capture of `bench.py --quick` on this workload
+# (profiles/k_g2p_p2g1_1M_128.md).
+MEASURED_TRAFFIC_PER_LAUNCH = {"sorted_g2p_p2g_1": 100.7e6}
+
+
 def algorithmic_bytes(kernel: str, n: int, cells: int) -> float | None:
     """Unique bytes a launch must read or write (each input read once, each
     output written once, an atomic counted as one write per cell and
@@ -300,7 +306,10 @@ def run_ours(args) -> None:
         roof = {"bound": "hbm", "kernel": top_name, "achieved": achieved,
                 "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
-                "traffic": None, "algorithmic_bytes_per_launch": abytes,
+                "traffic": MEASURED_TRAFFIC_PER_LAUNCH.get(top_name),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                  "profiles/k_g2p_p2g1_1M_128.md",
+                "algorithmic_bytes_per_launch": abytes,
                 "mean_launch_us": avg_s * 1e6, "cells_touched": cells,
                 "kernel_share": top_ms / step_kernel_ms if step_kernel_ms else None}
     kernels = {k: {"launches": v[0], "mean_us": 1e3 * v[2] / v[1] if v[1] else None,
