@@ -11,7 +11,10 @@
 //    its position in the bin order of the other particle buffer (an id array
 //    rides along), so the next substep reads nearly contiguous memory.
 //  * A task is one brick's particles; CTAs claim tasks from an atomic work
-//    counter and walk a task in chunks of 256 particles.  The CTA keeps the
+//    counter and walk a task in chunks of one particle per thread.  p2g_2
+//    first reorders the brick's particles into a lane table that puts
+//    particles of 32 different shared-memory bank classes in the 32 lanes of
+//    a warp (build_lane_table); g2p reuses that order.  The CTA keeps the
 //    cells the task's stencils reach (its "arena") in shared memory: the
 //    brick plus a one-cell halo (6^3 cells) for p2g_2 and g2p, plus a
 //    two-cell halo (8^3) for the next substep's p2g_1, whose particles have
@@ -39,34 +42,40 @@ namespace mpm {
 
 namespace {
 
-constexpr int kTask = 256;       // particles per chunk == threads per CTA
-// Arenas are padded so that the 32 lanes of a warp, holding particles of 32
-// different cells of a brick (see deal_pos), hit 32 different banks for
-// every stencil offset: x-stride 80 = 16 (mod 32) and y-stride 12 for the
-// 6^3 arena; x-stride 68 = 4 (mod 32) and y-stride 8 for the 8^3 arena.
+// Particles per chunk == threads per CTA of the task kernels.  Bricks at the
+// free surface hold few particles, so smaller chunks leave fewer lanes idle.
+#ifndef MPM_TASK_THREADS
+#define MPM_TASK_THREADS 256
+#endif
+constexpr int kTask = MPM_TASK_THREADS;
+// Arena strides: with x-stride = 16 and y-stride = 12 (mod 32) the 64 cells
+// of a brick fall into 32 bank classes of exactly two cells each
+// (class = (16*x + 12*y + z) mod 32 for brick-relative x, y, z).  When the
+// 32 lanes of a warp hold particles of the 32 different classes (see
+// build_lane_table), every stencil offset hits 32 different banks (and, for
+// the float4 arena, 8 different 16-byte groups per quarter-warp), so the
+// shared-memory gathers and atomics need one wavefront each.  The 8^3 arena
+// uses congruent strides, so particles that stayed in their cell keep the
+// property there.
 constexpr int kA = 6;            // p2g_2 / g2p arena edge: brick + 1-cell halo
 constexpr int kSYA = 12, kSXA = 80, kNA = kA * kSXA;
 constexpr int kB = 8;            // next-p2g_1 arena edge: brick + 2-cell halo
-constexpr int kSYB = 8, kSXB = 68, kNB = kB * kSXB;
-constexpr int kMaxSort = 1024;   // bricks with more particles skip the cell sort
+constexpr int kSYB = 12, kSXB = 112, kNB = kB * kSXB;
+constexpr int kMaxSort = 1024;   // bricks with more particles keep the bin order
 constexpr int kScanThreads = 1024;
 
 // Minimum resident CTAs per SM requested from the register allocator.
 #ifndef MPM_G2P_MIN_BLOCKS
-#define MPM_G2P_MIN_BLOCKS 4
+#define MPM_G2P_MIN_BLOCKS (1024 / MPM_TASK_THREADS)
 #endif
 #ifndef MPM_P2G2_MIN_BLOCKS
-#define MPM_P2G2_MIN_BLOCKS 3
+#define MPM_P2G2_MIN_BLOCKS (768 / MPM_TASK_THREADS)
 #endif
 // 1: arena stage bodies use packed f32x2 products (mpm_math_x2.cuh).
 #ifndef MPM_PACKED_MATH
 #define MPM_PACKED_MATH 1
 #endif
-// 1: p2g_2 counting-sorts each brick's particles by cell before dealing them
-// to lanes (fewer shared-memory atomic collisions, more integer work).
-#ifndef MPM_CELL_SORT
-#define MPM_CELL_SORT 1
-#endif
+
 
 thread_local std::string g_err;
 
@@ -89,6 +98,7 @@ struct __align__(16) Task {
 
 struct Dev {
     int4* grid[2];
+    float4* gv[2];       // decoded velocities of each grid's dirty bricks (k_update)
     uint32_t* dirty_flag[2];
     uint32_t* dirty_list[2];
     uint32_t* dirty_n;   // [2]
@@ -202,6 +212,9 @@ __device__ __forceinline__ void clear_dirty(const Dev& d, int gi) {
         int4* base = d.grid[gi] + (size_t)b * 64;
         base[lane] = make_int4(0, 0, 0, 0);
         base[lane + 32] = make_int4(0, 0, 0, 0);
+        float4* vbase = d.gv[gi] + (size_t)b * 64;
+        vbase[lane] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        vbase[lane + 32] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (lane == 0) d.dirty_flag[gi][b] = 0u;
     }
     __syncthreads();
@@ -230,18 +243,6 @@ __device__ __forceinline__ bool arena_cell(int li, int ox, int oy, int oz, int& 
     return ay < E && az < E;
 }
 
-// Thread t of a chunk of m particles (bin order, cell-sorted within the
-// brick) -> the chunk position it processes, or -1.  Lane l of warp w takes
-// position l*nw + w: a warp gathers particles from ~32 different cells
-// rather than 4 cells of 8, so shared-memory atomics rarely meet at one
-// address.
-__device__ __forceinline__ int deal_pos(int t, int m) {
-    const int nw = (m + 31) >> 5;
-    const int w = t >> 5;
-    if (w >= nw) return -1;
-    const int p = (t & 31) * nw + w;
-    return p < m ? p : -1;
-}
 
 // Global-path mass source (flat indices, as the reference's shaders address).
 struct GlobalMass {
@@ -255,96 +256,203 @@ struct GlobalMass {
     }
 };
 
+// Async 16-byte global -> shared copies (L2 only), used to prefetch the next
+// task's arena while the current task computes.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Shared-memory scratch of build_lane_table.
+struct LaneTable {
+    uint32_t slot[kMaxSort];    // particle slots in table order
+    uint32_t key[kMaxSort];     // class | rank << 6, per particle in bin order
+    uint32_t tmp[kMaxSort];     // particle slots in bin order
+    int cnt[33];                // particles per bank class (32: not in the arena)
+    int valid[32], core[32], empty_pre[33], over_pre[33];
+};
+
+// Orders a brick's n particles into a table of ceil(n/32) rows of 32 lanes
+// in which lane k of a row holds, where possible, a particle of bank class k
+// (its base cell's class); particles of over-full classes (and particles
+// outside the arena) fill the lanes that under-full classes leave empty, in
+// order, and the unfilled lanes are the tail of the last row.  The table is
+// written to order[first .. first + n) (g2p reuses it) and to lt.slot.
+// Every thread calls it (it contains barriers).
+__device__ __forceinline__ void build_lane_table(const Particles& P, const Geo& g, const Dev& d,
+                                                 const Task& task, int tbx, int tby, int tbz,
+                                                 LaneTable& lt) {
+    const int n = task.count;
+    if (threadIdx.x < 33) lt.cnt[threadIdx.x] = 0;
+    __syncthreads();
+    for (int j = threadIdx.x; j < n; j += kTask) {
+        const uint32_t slot = d.order[task.first + j];
+        const float4 a = P.p0[slot];
+        const float x[3] = {a.x, a.y, a.z};
+        int bx, by, bz;
+        base_cell(x, bx, by, bz);
+        const int ax = bx - 4 * tbx, ay = by - 4 * tby, az = bz - 4 * tbz;
+        const bool in = regular_base(g, bx, by, bz) && (unsigned)ax <= 3u && (unsigned)ay <= 3u &&
+                        (unsigned)az <= 3u;
+        const int cls = in ? ((16 * ax + 12 * ay + az) & 31) : 32;
+        const int r = atomicAdd(&lt.cnt[cls], 1);
+        lt.tmp[j] = slot;
+        lt.key[j] = (uint32_t)cls | ((uint32_t)r << 6);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int k = threadIdx.x;
+        const int rows = (n + 31) >> 5;
+        const int last = n - 32 * (rows - 1);            // lanes used in the last row
+        const int v = rows - 1 + (k < last ? 1 : 0);     // rows lane k holds
+        const int c = lt.cnt[k];
+        const int core = min(c, v);
+        int e = v - core, o = c - core;                  // empty lanes, overflow particles
+        int ei = e, oi = o;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int ye = __shfl_up_sync(0xffffffffu, ei, off);
+            const int yo = __shfl_up_sync(0xffffffffu, oi, off);
+            if (k >= off) { ei += ye; oi += yo; }
+        }
+        lt.valid[k] = v;
+        lt.core[k] = core;
+        lt.empty_pre[k] = ei - e;
+        lt.over_pre[k] = oi - o;
+        if (k == 31) {
+            lt.empty_pre[32] = ei;
+            lt.over_pre[32] = oi;  // particles outside the arena overflow after these
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < n; j += kTask) {
+        const uint32_t key = lt.key[j];
+        const int cls = (int)(key & 63u), r = (int)(key >> 6);
+        int pos;
+        if (cls < 32 && r < lt.valid[cls]) {
+            pos = r * 32 + cls;
+        } else {
+            const int i = cls < 32 ? lt.over_pre[cls] + (r - lt.valid[cls]) : lt.over_pre[32] + r;
+            int lo = 0;                                  // last lane with empty_pre <= i
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+                if (lo + step < 32 && lt.empty_pre[lo + step] <= i) lo += step;
+            pos = (lt.core[lo] + (i - lt.empty_pre[lo])) * 32 + lo;
+        }
+        lt.slot[pos] = lt.tmp[j];
+        d.order[task.first + pos] = lt.tmp[j];
+    }
+    __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
-// p2g_2 (p2g_2.wgsl:30-94) over tasks; also clears grid `cur ^ 1`.  Each
-// brick's particles are first counting-sorted by cell (in shared memory);
-// the sorted order is written back to `order` for g2p.
+// p2g_2 (p2g_2.wgsl:30-94) over tasks; also clears grid `cur ^ 1`.
+//
+// One barrier per task: arenas are double-buffered.  While task i computes,
+// the mass words of task i+1's arena are already loading into registers
+// (decoded into the other buffer after the compute), and task i-1's momentum
+// arena is flushed (each thread reads, flushes and zeroes its own slots).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
     k_p2g2(Particles P, Geo g, SimConsts k, Dev d, int cur, unsigned long long* oob) {
-    __shared__ float s_mass[kNA];
-    __shared__ int s_q[3][kNA];
-    __shared__ uint32_t s_slot[kMaxSort];
-    __shared__ uint32_t s_key[kMaxSort];
-    __shared__ uint32_t s_sorted[kMaxSort];
-    __shared__ int s_cnt[65], s_start[65];
+    __shared__ float s_mass[2][kNA];
+    __shared__ int s_q[2][3][kNA];
     __shared__ int s_task[2];
+    __shared__ LaneTable s_lt;
+    constexpr int kPer = (kNA + kTask - 1) / kTask;  // arena slots per thread
 
     clear_dirty(d, cur ^ 1);
 
     int4* __restrict__ grid = d.grid[cur];
     unsigned bad = 0;
     const int ntasks = (int)__ldcg(d.ntasks);
-    if (threadIdx.x < 65) s_cnt[threadIdx.x] = 0;
-    if (threadIdx.x == 0) s_task[0] = claim_task(d, kCtrP2G2);
+    for (int i = threadIdx.x; i < 2 * 3 * kNA; i += kTask) (&s_q[0][0][0])[i] = 0;
+    if (threadIdx.x == 0) {
+        s_task[0] = claim_task(d, kCtrP2G2);
+        s_task[1] = claim_task(d, kCtrP2G2);
+    }
     __syncthreads();
-    int buf = 0;
-    int t = s_task[0];
-    while (t < ntasks) {
-        if (threadIdx.x == 0) s_task[buf ^ 1] = claim_task(d, kCtrP2G2);
-        const Task task = d.tasks[t];
-        const bool sort = MPM_CELL_SORT && task.brick >= 0 && task.count <= kMaxSort;
-        int tbx = 0, tby = 0, tbz = 0;
-        if (task.brick >= 0) {
-            brick_coords(g, task.brick, tbx, tby, tbz);
-            const int ox = 4 * tbx - 1, oy = 4 * tby - 1, oz = 4 * tbz - 1;
-            for (int li = threadIdx.x; li < kNA; li += kTask) {
-                int x, y, z;
-                int m = 0;
-                if (arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z) && cell_exists(g, x, y, z))
-                    m = __ldcg(reinterpret_cast<const int*>(grid + brick_addr(g, x, y, z)) + 3);
-                s_mass[li] = dec(m, k.fm);
-                s_q[0][li] = 0;
-                s_q[1][li] = 0;
-                s_q[2][li] = 0;
-            }
-        }
-        if (sort) {
-            for (int j = threadIdx.x; j < task.count; j += kTask) {
-                const uint32_t slot = d.order[task.first + j];
-                const float4 a = P.p0[slot];
-                const float x[3] = {a.x, a.y, a.z};
-                int bx, by, bz;
-                base_cell(x, bx, by, bz);
-                const int ax = bx - 4 * tbx, ay = by - 4 * tby, az = bz - 4 * tbz;
-                const bool in = regular_base(g, bx, by, bz) && (unsigned)ax <= 3u &&
-                                (unsigned)ay <= 3u && (unsigned)az <= 3u;
-                const int c = in ? (ax * 16 + ay * 4 + az) : 64;
-                const int r = atomicAdd(&s_cnt[c], 1);
-                s_slot[j] = slot;
-                s_key[j] = (uint32_t)c | ((uint32_t)r << 7);
-            }
-        }
-        __syncthreads();
-        if (sort) {
-            if (threadIdx.x < 32) {
-                const int l = threadIdx.x;
-                const int v0 = s_cnt[2 * l], v1 = s_cnt[2 * l + 1];
-                int incl = v0 + v1;
+
+    // arena origin (brick - 1 cell) of a task, or false for the irregular bin
+    auto origin = [&](const Task& tk, int& ox, int& oy, int& oz) -> bool {
+        if (tk.brick < 0) return false;
+        brick_coords(g, tk.brick, ox, oy, oz);
+        ox = 4 * ox - 1;
+        oy = 4 * oy - 1;
+        oz = 4 * oz - 1;
+        return true;
+    };
+    // raw mass words of this thread's arena slots for a task
+    auto load_mass = [&](int t, int m[kPer]) {
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int y = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (l >= o) incl += y;
-                }
-                const int excl = incl - v0 - v1;
-                s_start[2 * l] = excl;
-                s_start[2 * l + 1] = excl + v0;
-                if (l == 31) s_start[64] = incl;
-            }
-            __syncthreads();
-            for (int j = threadIdx.x; j < task.count; j += kTask) {
-                const uint32_t key = s_key[j];
-                const int pos = s_start[key & 127u] + (int)(key >> 7);
-                s_sorted[pos] = s_slot[j];
-                d.order[task.first + pos] = s_slot[j];
-            }
-            __syncthreads();
+        for (int q = 0; q < kPer; ++q) m[q] = 0;
+        if (t >= ntasks) return;
+        int ox, oy, oz;
+        if (!origin(d.tasks[t], ox, oy, oz)) return;
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const int li = (int)threadIdx.x + q * kTask;
+            int x, y, z;
+            if (li < kNA && arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z) &&
+                cell_exists(g, x, y, z))
+                m[q] = __ldcg(reinterpret_cast<const int*>(grid + brick_addr(g, x, y, z)) + 3);
         }
-        for (int base = 0; base < task.count; base += kTask) {
-            const int p = deal_pos(threadIdx.x, min(kTask, task.count - base));
-            if (p < 0) continue;
-            const int j = base + p;
-            const int slot = sort ? (int)s_sorted[j] : (int)d.order[task.first + j];
+    };
+    auto store_mass = [&](int buf, const int m[kPer]) {
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const int li = (int)threadIdx.x + q * kTask;
+            if (li < kNA) s_mass[buf][li] = dec(m[q], k.fm);
+        }
+    };
+    auto flush = [&](int buf, const Task& tk) {
+        int ox, oy, oz;
+        if (!origin(tk, ox, oy, oz)) return;
+        for (int li = threadIdx.x; li < kNA; li += kTask) {
+            const int q0 = s_q[buf][0][li], q1 = s_q[buf][1][li], q2 = s_q[buf][2][li];
+            if ((q0 | q1 | q2) == 0) continue;
+            s_q[buf][0][li] = 0;
+            s_q[buf][1][li] = 0;
+            s_q[buf][2][li] = 0;
+            int x, y, z;
+            if (!arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z)) continue;
+            if (!cell_exists(g, x, y, z)) continue;  // unreachable for regular particles
+            int* c = reinterpret_cast<int*>(grid + brick_addr(g, x, y, z));
+            if (q0) atomicAdd(c + 0, q0);
+            if (q1) atomicAdd(c + 1, q1);
+            if (q2) atomicAdd(c + 2, q2);
+        }
+    };
+
+    int t = s_task[0];
+    {
+        int m[kPer];
+        load_mass(t, m);
+        store_mass(0, m);
+    }
+    Task prev;
+    prev.brick = -1;
+    prev.count = 0;
+    bool have_prev = false;
+    int it = 0;
+    while (t < ntasks) {
+        const int buf = it & 1;
+        __syncthreads();  // arena `buf` ready; task it-1 computed
+        const int t_next = s_task[buf ^ 1];
+        if (threadIdx.x == 0) s_task[buf] = claim_task(d, kCtrP2G2);
+        int m_next[kPer];
+        load_mass(t_next, m_next);
+        if (have_prev) flush(buf ^ 1, prev);
+
+        const Task task = d.tasks[t];
+        int tbx = 0, tby = 0, tbz = 0;
+        if (task.brick >= 0) brick_coords(g, task.brick, tbx, tby, tbz);
+        const bool table = task.brick >= 0 && task.count <= kMaxSort;  // uniform
+        if (table) build_lane_table(P, g, d, task, tbx, tby, tbz, s_lt);
+        for (int j = threadIdx.x; j < task.count; j += kTask) {
+            const int slot = table ? (int)s_lt.slot[j] : (int)d.order[task.first + j];
             PState s;
             unpack_xC(P.p0[slot], P.p1[slot], P.p2[slot], s);
             int bx, by, bz;
@@ -356,13 +464,13 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
                 // stencil corner (base - 1) relative to the arena origin (brick - 1)
                 const int li0 = ax * kSXA + ay * kSYA + az;
                 auto mass = [&](int gx, int gy, int gz) -> float {
-                    return s_mass[li0 + gx * kSXA + gy * kSYA + gz];
+                    return s_mass[buf][li0 + gx * kSXA + gy * kSYA + gz];
                 };
                 auto sink = [&](int gx, int gy, int gz, int mx, int my, int mz) {
                     const int li = li0 + gx * kSXA + gy * kSYA + gz;
-                    atomicAdd(&s_q[0][li], mx);
-                    atomicAdd(&s_q[1][li], my);
-                    atomicAdd(&s_q[2][li], mz);
+                    atomicAdd(&s_q[buf][0][li], mx);
+                    atomicAdd(&s_q[buf][1][li], my);
+                    atomicAdd(&s_q[buf][2][li], mz);
                 };
                 if (MPM_PACKED_MATH) {
                     p2g2_particle_x2(s, k, mass, sink);
@@ -387,32 +495,22 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
                     });
             }
         }
-        __syncthreads();
-        if (task.brick >= 0) {
-            const int ox = 4 * tbx - 1, oy = 4 * tby - 1, oz = 4 * tbz - 1;
-            for (int li = threadIdx.x; li < kNA; li += kTask) {
-                const int q0 = s_q[0][li], q1 = s_q[1][li], q2 = s_q[2][li];
-                if ((q0 | q1 | q2) == 0) continue;
-                int x, y, z;
-                if (!arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z)) continue;
-                if (!cell_exists(g, x, y, z)) continue;  // unreachable for regular particles
-                int* c = reinterpret_cast<int*>(grid + brick_addr(g, x, y, z));
-                if (q0) atomicAdd(c + 0, q0);
-                if (q1) atomicAdd(c + 1, q1);
-                if (q2) atomicAdd(c + 2, q2);
-            }
-        }
-        if (threadIdx.x < 65) s_cnt[threadIdx.x] = 0;
-        __syncthreads();
-        buf ^= 1;
-        t = s_task[buf];
+        store_mass(buf ^ 1, m_next);
+        prev = task;
+        have_prev = true;
+        t = t_next;
+        ++it;
     }
+    __syncthreads();
+    if (have_prev) flush((it - 1) & 1, prev);
     if (bad) atomicAdd(oob, (unsigned long long)bad);
 }
 
 // ---------------------------------------------------------------------------
 // updateGrid (updateGrid.wgsl:23-46) on the dirty bricks of grid `cur`, in
-// place: warp per brick, two cells per lane.
+// place, warp per brick, two cells per lane.  Also writes every cell of
+// those bricks, decoded, to the float velocity grid g2p reads:
+// (dec(vx), dec(vy), dec(vz), dec(vz)).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_update(Geo g, SimConsts k, Dev d, int cur) {
     const uint32_t nd = __ldcg(d.dirty_n + cur);
@@ -421,6 +519,7 @@ __global__ void __launch_bounds__(256) k_update(Geo g, SimConsts k, Dev d, int c
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     int4* __restrict__ grid = d.grid[cur];
+    float4* __restrict__ gv = d.gv[cur];
     for (uint32_t i = warp; i < nd; i += nwarps) {
         const int b = (int)__ldcg(d.dirty_list[cur] + i);
         int bx, by, bz;
@@ -428,11 +527,15 @@ __global__ void __launch_bounds__(256) k_update(Geo g, SimConsts k, Dev d, int c
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int c = (int)lane + 32 * h;
-            const int4 raw = grid[(size_t)b * 64 + c];
-            if (raw.w > 0) {
+            const size_t a = (size_t)b * 64 + c;
+            int4 u = grid[a];
+            if (u.w > 0) {
                 const int x = 4 * bx + (c >> 4), y = 4 * by + ((c >> 2) & 3), z = 4 * bz + (c & 3);
-                grid[(size_t)b * 64 + c] = update_cell_xyz(raw, x, y, z, k, hx, hy, hz);
+                u = update_cell_xyz(u, x, y, z, k, hx, hy, hz);
+                grid[a] = u;
             }
+            const float vz = dec(u.z, k.fm);
+            gv[a] = make_float4(dec(u.x, k.fm), dec(u.y, k.fm), vz, vz);
         }
     }
 }
@@ -442,58 +545,106 @@ __global__ void __launch_bounds__(256) k_update(Geo g, SimConsts k, Dev d, int c
 // from Pin through the bin order and writes them, in bin order, to Pout.
 // DO_G2P = false runs p2g_1 of the current positions only (first substep;
 // Pout is not written).
+//
+// One barrier per task: while task i computes, task i+1's g2p arena is
+// copied in with cp.async and task i-1's p2g_1 arena is flushed (each thread
+// reads, flushes and zeroes its own slots); the bricks task i-1's stencils
+// reached are registered as dirty right after the barrier.
 // ---------------------------------------------------------------------------
 template <bool DO_G2P, bool POSVEL>
 __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
     k_g2p_p2g1(Particles Pin, Particles Pout, const uint32_t* __restrict__ id_in,
                uint32_t* __restrict__ id_out, float4* __restrict__ posvel, Geo g, SimConsts k,
                Dev d, int src, int dst, unsigned long long* oob) {
-    __shared__ float4 s_v[kNA];
-    __shared__ int s_a[4][kNB];
-    __shared__ int s_touch[27];
+    __shared__ __align__(16) float4 s_v[DO_G2P ? 2 : 1][DO_G2P ? kNA : 1];
+    __shared__ int s_a[2][4][kNB];
+    __shared__ int s_touch[2][27];
     __shared__ int s_task[2];
 
-    const int4* __restrict__ gsrc = d.grid[src];
+    const float4* __restrict__ gvsrc = d.gv[src];
     int4* __restrict__ gdst = d.grid[dst];
     const int ctr = DO_G2P ? kCtrG2P : kCtrP2G1;
     unsigned bad = 0;
     const int ntasks = (int)__ldcg(d.ntasks);
-    if (threadIdx.x == 0) s_task[0] = claim_task(d, ctr);
+    for (int i = threadIdx.x; i < 2 * 4 * kNB; i += kTask) (&s_a[0][0][0])[i] = 0;
+    if (threadIdx.x < 54) (&s_touch[0][0])[threadIdx.x] = 0;
+    if (threadIdx.x == 0) {
+        s_task[0] = claim_task(d, ctr);
+        s_task[1] = claim_task(d, ctr);
+    }
     __syncthreads();
-    int buf = 0;
+
+    // g2p arena of task t (velocities decoded by k_update) into s_v[buf]
+    auto prefetch = [&](int t, int buf) {
+        if (!DO_G2P || t >= ntasks) return;
+        const Task tk = d.tasks[t];
+        if (tk.brick < 0) return;
+        int ox, oy, oz;
+        brick_coords(g, tk.brick, ox, oy, oz);
+        ox = 4 * ox - 1;
+        oy = 4 * oy - 1;
+        oz = 4 * oz - 1;
+        for (int li = threadIdx.x; li < kNA; li += kTask) {
+            int x, y, z;
+            if (arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z) && cell_exists(g, x, y, z))
+                cp_async16(&s_v[buf][li], gvsrc + brick_addr(g, x, y, z));
+            else
+                s_v[buf][li] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        cp_async_commit();
+    };
+    // flush the p2g_1 arena of a task with brick coordinates tb
+    auto flush = [&](int buf, int tbx, int tby, int tbz) {
+        const int ox = 4 * tbx - 2, oy = 4 * tby - 2, oz = 4 * tbz - 2;
+        for (int li = threadIdx.x; li < kNB; li += kTask) {
+            const int q0 = s_a[buf][0][li], q1 = s_a[buf][1][li], q2 = s_a[buf][2][li],
+                      q3 = s_a[buf][3][li];
+            if ((q0 | q1 | q2 | q3) == 0) continue;
+            s_a[buf][0][li] = 0;
+            s_a[buf][1][li] = 0;
+            s_a[buf][2][li] = 0;
+            s_a[buf][3][li] = 0;
+            int x, y, z;
+            if (!arena_cell<kB, kSXB, kSYB>(li, ox, oy, oz, x, y, z)) continue;
+            if (!cell_exists(g, x, y, z)) continue;  // unreachable for regular particles
+            int* c = reinterpret_cast<int*>(gdst + brick_addr(g, x, y, z));
+            if (q0) atomicAdd(c + 0, q0);
+            if (q1) atomicAdd(c + 1, q1);
+            if (q2) atomicAdd(c + 2, q2);
+            if (q3) atomicAdd(c + 3, q3);
+        }
+    };
+    // register the bricks (3x3x3 around tb) flagged in s_touch[buf]
+    auto mark = [&](int buf, int tbx, int tby, int tbz) {
+        if (threadIdx.x < 27 && s_touch[buf][threadIdx.x]) {
+            const int i = threadIdx.x;
+            const int nbx = tbx + i / 9 - 1, nby = tby + (i / 3) % 3 - 1, nbz = tbz + i % 3 - 1;
+            mark_brick(d, dst, (uint32_t)((nbx * g.BY + nby) * g.BZ + nbz));
+            s_touch[buf][i] = 0;
+        }
+    };
+
     int t = s_task[0];
+    prefetch(t, 0);
+    bool have_prev = false, prev_arena = false;
+    int pbx = 0, pby = 0, pbz = 0;  // brick of the previous task
+    int it = 0;
     while (t < ntasks) {
-        if (threadIdx.x == 0) s_task[buf ^ 1] = claim_task(d, ctr);
+        const int buf = it & 1;
+        if (DO_G2P) cp_async_wait_all();
+        __syncthreads();  // s_v[buf] arrived; task it-1 computed everywhere
+        const int t_next = s_task[buf ^ 1];
+        if (threadIdx.x == 0) s_task[buf] = claim_task(d, ctr);
+        if (have_prev && prev_arena) mark(buf ^ 1, pbx, pby, pbz);
+        prefetch(t_next, buf ^ 1);
+        if (have_prev && prev_arena) flush(buf ^ 1, pbx, pby, pbz);
+
         const Task task = d.tasks[t];
         int tbx = 0, tby = 0, tbz = 0;
-        if (task.brick >= 0) {
-            brick_coords(g, task.brick, tbx, tby, tbz);
-            const int ox = 4 * tbx - 1, oy = 4 * tby - 1, oz = 4 * tbz - 1;
-            if (DO_G2P) {
-                for (int li = threadIdx.x; li < kNA; li += kTask) {
-                    int x, y, z;
-                    int4 c = make_int4(0, 0, 0, 0);
-                    if (arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z) &&
-                        cell_exists(g, x, y, z))
-                        c = __ldcg(gsrc + brick_addr(g, x, y, z));
-                    const float vz = dec(c.z, k.fm);
-                    s_v[li] = make_float4(dec(c.x, k.fm), dec(c.y, k.fm), vz, vz);
-                }
-            }
-            for (int li = threadIdx.x; li < kNB; li += kTask) {
-                s_a[0][li] = 0;
-                s_a[1][li] = 0;
-                s_a[2][li] = 0;
-                s_a[3][li] = 0;
-            }
-            if (threadIdx.x < 27) s_touch[threadIdx.x] = 0;
-        }
-        __syncthreads();
-
+        if (task.brick >= 0) brick_coords(g, task.brick, tbx, tby, tbz);
         for (int base = 0; base < task.count; base += kTask) {
-            const int p = deal_pos(threadIdx.x, min(kTask, task.count - base));
-            const bool active = p >= 0;
-            const int jo = task.first + base + (active ? p : 0);  // position in bin order
+            const bool active = base + (int)threadIdx.x < task.count;
+            const int jo = task.first + base + (active ? (int)threadIdx.x : 0);  // bin order
             const int slot = active ? (int)d.order[jo] : 0;
             PState s;
             if (DO_G2P) {
@@ -508,15 +659,16 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
                                           (unsigned)az <= 3u;
                     if (in_arena) {
                         const int li0 = ax * kSXA + ay * kSYA + az;
+                        const float4* sv = s_v[DO_G2P ? buf : 0];
                         if (MPM_PACKED_MATH) {
                             g2p_particle_x2(s, k, [&](int gx, int gy, int gz, f2& gxy, f2& gzz) {
-                                const float4 v = s_v[li0 + gx * kSXA + gy * kSYA + gz];
+                                const float4 v = sv[li0 + gx * kSXA + gy * kSYA + gz];
                                 gxy = pk(v.x, v.y);
                                 gzz = pk(v.z, v.w);
                             });
                         } else {
                             g2p_particle(s, k, [&](int, int gx, int gy, int gz, float out[3]) {
-                                const float4 v = s_v[li0 + gx * kSXA + gy * kSYA + gz];
+                                const float4 v = sv[li0 + gx * kSXA + gy * kSYA + gz];
                                 out[0] = v.x;
                                 out[1] = v.y;
                                 out[2] = v.z;
@@ -524,12 +676,12 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
                         }
                     } else {
                         g2p_particle(s, k, [&](int idx, int, int, int, float out[3]) {
-                            int4 c = make_int4(0, 0, 0, 0);
-                            if (in_grid(g, idx)) c = __ldcg(gsrc + flat_to_addr(g, idx));
+                            float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                            if (in_grid(g, idx)) v = __ldcg(gvsrc + flat_to_addr(g, idx));
                             else ++bad;
-                            out[0] = dec(c.x, k.fm);
-                            out[1] = dec(c.y, k.fm);
-                            out[2] = dec(c.z, k.fm);
+                            out[0] = v.x;
+                            out[1] = v.y;
+                            out[2] = v.z;
                         });
                     }
                     store_particle(Pout, jo, s);
@@ -559,10 +711,10 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
                     const int li0 = ax * kSXB + ay * kSYB + az;
                     auto sink = [&](int gx, int gy, int gz, int m, int vx, int vy, int vz) {
                         const int li = li0 + gx * kSXB + gy * kSYB + gz;
-                        atomicAdd(&s_a[3][li], m);
-                        atomicAdd(&s_a[0][li], vx);
-                        atomicAdd(&s_a[1][li], vy);
-                        atomicAdd(&s_a[2][li], vz);
+                        atomicAdd(&s_a[buf][3][li], m);
+                        atomicAdd(&s_a[buf][0][li], vx);
+                        atomicAdd(&s_a[buf][1][li], vy);
+                        atomicAdd(&s_a[buf][2][li], vz);
                     };
                     if (MPM_PACKED_MATH) {
                         p2g1_particle_x2(s, k, sink);
@@ -571,6 +723,14 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
                                       [&](int, int gx, int gy, int gz, int m, int vx, int vy,
                                           int vz) { sink(gx, gy, gz, m, vx, vy, vz); });
                     }
+                    // bricks the stencil (base-1 .. base+1) reaches, relative to the task's
+                    const int x0 = ((bx - 1) >> 2) - tbx, x1 = ((bx + 1) >> 2) - tbx;
+                    const int y0 = ((by - 1) >> 2) - tby, y1 = ((by + 1) >> 2) - tby;
+                    const int z0 = ((bz - 1) >> 2) - tbz, z1 = ((bz + 1) >> 2) - tbz;
+                    for (int xx = x0; xx <= x1; ++xx)
+                        for (int yy = y0; yy <= y1; ++yy)
+                            for (int zz = z0; zz <= z1; ++zz)
+                                s_touch[buf][((xx + 1) * 3 + (yy + 1)) * 3 + (zz + 1)] = 1;
                 } else {
                     p2g1_particle(s, k,
                                   [&](int idx, int, int, int, int m, int vx, int vy, int vz) {
@@ -587,35 +747,18 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
             }
             if (DO_G2P) count_bin(d, active, jo, bin_key(g, reg, bx, by, bz));
         }
-        __syncthreads();
-        if (task.brick >= 0) {
-            const int ox = 4 * tbx - 2, oy = 4 * tby - 2, oz = 4 * tbz - 2;
-            for (int li = threadIdx.x; li < kNB; li += kTask) {
-                const int q0 = s_a[0][li], q1 = s_a[1][li], q2 = s_a[2][li], q3 = s_a[3][li];
-                if ((q0 | q1 | q2 | q3) == 0) continue;
-                int x, y, z;
-                if (!arena_cell<kB, kSXB, kSYB>(li, ox, oy, oz, x, y, z)) continue;
-                if (!cell_exists(g, x, y, z)) continue;  // unreachable for regular particles
-                int* c = reinterpret_cast<int*>(gdst + brick_addr(g, x, y, z));
-                if (q0) atomicAdd(c + 0, q0);
-                if (q1) atomicAdd(c + 1, q1);
-                if (q2) atomicAdd(c + 2, q2);
-                if (q3) atomicAdd(c + 3, q3);
-                // which of the 3x3x3 neighbouring bricks received this cell
-                const int nb = (((x >> 2) - tbx + 1) * 3 + ((y >> 2) - tby + 1)) * 3 +
-                               ((z >> 2) - tbz + 1);
-                s_touch[nb] = 1;
-            }
-            __syncthreads();
-            if (threadIdx.x < 27 && s_touch[threadIdx.x]) {
-                const int i = threadIdx.x;
-                const int nbx = tbx + i / 9 - 1, nby = tby + (i / 3) % 3 - 1, nbz = tbz + i % 3 - 1;
-                mark_brick(d, dst, (uint32_t)((nbx * g.BY + nby) * g.BZ + nbz));
-            }
-        }
-        __syncthreads();
-        buf ^= 1;
-        t = s_task[buf];
+        have_prev = true;
+        prev_arena = task.brick >= 0;
+        pbx = tbx;
+        pby = tby;
+        pbz = tbz;
+        t = t_next;
+        ++it;
+    }
+    __syncthreads();
+    if (have_prev && prev_arena) {
+        mark((it - 1) & 1, pbx, pby, pbz);
+        flush((it - 1) & 1, pbx, pby, pbz);
     }
     if (bad) atomicAdd(oob, (unsigned long long)bad);
 }
@@ -761,6 +904,8 @@ namespace {
 
 void free_grid_state(SortedEngine* e) {
     for (int b = 0; b < 2; ++b) {
+        cudaFree(e->d.gv[b]);
+        e->d.gv[b] = nullptr;
         cudaFree(e->d.grid[b]);
         cudaFree(e->d.dirty_flag[b]);
         cudaFree(e->d.dirty_list[b]);
@@ -855,6 +1000,7 @@ int sorted_configure(SortedEngine* e, const SimConsts& k) {
         free_grid_state(e);
         for (int b = 0; b < 2; ++b) {
             SE_CUDA(cudaMalloc(&e->d.grid[b], sizeof(int4) * cells));
+            SE_CUDA(cudaMalloc(&e->d.gv[b], sizeof(float4) * cells));
             SE_CUDA(cudaMalloc(&e->d.dirty_flag[b], 4 * (size_t)g.nbricks));
             SE_CUDA(cudaMalloc(&e->d.dirty_list[b], 4 * (size_t)g.nbricks));
         }
@@ -902,6 +1048,7 @@ int sorted_step(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned lon
         const size_t cells = (size_t)g.nbricks * 64;
         for (int b = 0; b < 2; ++b) {
             SE_CUDA(cudaMemsetAsync(e->d.grid[b], 0, sizeof(int4) * cells, st));
+            SE_CUDA(cudaMemsetAsync(e->d.gv[b], 0, sizeof(float4) * cells, st));
             SE_CUDA(cudaMemsetAsync(e->d.dirty_flag[b], 0, 4 * (size_t)g.nbricks, st));
         }
         SE_CUDA(cudaMemsetAsync(e->d.dirty_n, 0, 8, st));
