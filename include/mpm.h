@@ -187,6 +187,62 @@ int mpm_probe_conversions(const float* in, int n, float fm, int32_t* enc_out, fl
  * product rounded before the add).  Synchronous. */
 int mpm_probe_packed(const float* a, const float* b, int n, float* out);
 
+/* ------------------------------------------------------------------ */
+/* Extensions beyond the reference's class                             */
+/* ------------------------------------------------------------------ */
+
+/* Body force (per unit time) added in updateGrid.  The reference hardcodes
+ * (0, -0.3, 0) (mls-mpm/updateGrid.wgsl:34), the default; components that
+ * are 0 are left untouched, so that default is bit-identical to it. */
+int mpm_set_gravity(mpm_sim* sim, const float gravity[3]);
+
+/* 1: mpm_step on the sorted engine runs its substeps as one CUDA graph,
+ * captured on first use for each substep count (and recaptured after a
+ * change of constants) -- fewer host launches for small scenes.  0 (the
+ * default): plain launches. */
+int mpm_set_graph(mpm_sim* sim, int enable);
+
+/* Batches: many independent scenes that advance together, one launch per
+ * stage for all of them (the sorted engine over the scenes' concatenated
+ * particles, bricks and bins), replayed as a CUDA graph.  Each scene gives
+ * the same results, bit for bit, as an mpm_sim holding it alone with the
+ * same constants. */
+typedef struct mpm_batch mpm_batch;
+
+typedef struct mpm_scene_desc {
+    int num_particles;            /* this scene's records in the particle array */
+    float init_box[3];            /* reset()'s initBoxSize: grid extent, flat indices */
+    float real_box[3];            /* changeBoxSize()'s realBoxSize: walls, clamp */
+    float stiffness;              /* mpm_params fields, per scene */
+    float rest_density;
+    float dynamic_viscosity;
+    float dt;
+    float fixed_point_multiplier;
+    float gravity[3];             /* see mpm_set_gravity */
+} mpm_scene_desc;
+
+/* Scene s's particles are records [sum of earlier num_particles, + its own)
+ * of aos80 (80-byte records).  Grids must be non-degenerate
+ * (i32(init_box.y), i32(init_box.z) >= 1). */
+int mpm_batch_create(const mpm_scene_desc* scenes, int num_scenes, const float* aos80,
+                     mpm_batch** out);
+int mpm_batch_destroy(mpm_batch* batch);
+int mpm_batch_num_scenes(const mpm_batch* batch);
+int64_t mpm_batch_num_particles(const mpm_batch* batch);
+/* `substeps` substeps of every scene; asynchronous on `stream`. */
+int mpm_batch_step(mpm_batch* batch, int substeps, void* stream);
+/* Replaces scene s's constants (box sizes and num_particles must stay). */
+int mpm_batch_set_scene(mpm_batch* batch, int scene, const mpm_scene_desc* desc);
+int mpm_batch_set_graph(mpm_batch* batch, int enable); /* default 1 */
+/* All scenes' particles, in input order (synchronizes). */
+int mpm_batch_download_particles(mpm_batch* batch, float* out_aos80);
+/* Scene s's grid after its last updateGrid, reference layout (synchronizes). */
+int mpm_batch_download_grid(mpm_batch* batch, int scene, int32_t* out_cells);
+/* 32-byte posvel records of all particles, written by each step's last substep. */
+void* mpm_batch_posvel_device_ptr(mpm_batch* batch);
+int mpm_batch_check_health(mpm_batch* batch, mpm_health* out);
+int64_t mpm_batch_launch_count(const mpm_batch* batch);
+
 /*
  * No counterpart in the reference.  The watchdog scan of mpm_check_health
  * over a caller-owned device buffer, allocating nothing: for callers that

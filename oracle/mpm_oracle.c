@@ -59,6 +59,11 @@ typedef struct orc_params {
     float dynamic_viscosity;      /* mls-mpm.ts:56 */
     float dt;                     /* mls-mpm.ts:57 */
     float fixed_point_multiplier; /* mls-mpm.ts:58 */
+    /* Body force added per unit time in updateGrid.  The reference adds
+       -0.3*dt to vy only (updateGrid.wgsl:34): zero components are left
+       untouched, so (0, -0.3, 0) is the reference.  Other directions are the
+       batched scenes' extension. */
+    float gravity[3];
 } orc_params;
 
 /* ------------------------------------------------------------------ */
@@ -268,7 +273,9 @@ static void p2g_2_range(const float* particles, int64_t i0, int64_t i1, int32_t*
 static void update_range(int32_t* cells, int64_t c0, int64_t c1, const float real_box[3],
                          orc_box box, const orc_params* prm) {
     const float fm = prm->fixed_point_multiplier;
-    const float gdt = -0.3f * prm->dt;
+    const float g0 = prm->gravity[0] * prm->dt;
+    const float g1 = prm->gravity[1] * prm->dt;
+    const float g2 = prm->gravity[2] * prm->dt;
     const int32_t hx = f2i_sat(ceilf(real_box[0]) - 3.0f);
     const int32_t hy = f2i_sat(ceilf(real_box[1]) - 3.0f);
     const int32_t hz = f2i_sat(ceilf(real_box[2]) - 3.0f);
@@ -280,9 +287,9 @@ static void update_range(int32_t* cells, int64_t c0, int64_t c1, const float rea
         fv0 = fv0 / m;
         fv1 = fv1 / m;
         fv2 = fv2 / m;
-        int32_t o0 = enc(fv0, fm);
-        int32_t o1 = enc(fv1 + gdt, fm);
-        int32_t o2 = enc(fv2, fm);
+        int32_t o0 = enc(prm->gravity[0] != 0.0f ? fv0 + g0 : fv0, fm);
+        int32_t o1 = enc(prm->gravity[1] != 0.0f ? fv1 + g1 : fv1, fm);
+        int32_t o2 = enc(prm->gravity[2] != 0.0f ? fv2 + g2 : fv2, fm);
         int32_t id = (int32_t)i;
         int32_t x = (box.Z != 0 && box.Y != 0) ? (id / box.Z) / box.Y : 0;
         int32_t y = (box.Z != 0 && box.Y != 0) ? (id / box.Z) % box.Y : 0;

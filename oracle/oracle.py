@@ -47,11 +47,21 @@ class Params(ctypes.Structure):
         ("dynamic_viscosity", ctypes.c_float),
         ("dt", ctypes.c_float),
         ("fixed_point_multiplier", ctypes.c_float),
+        ("gravity", ctypes.c_float * 3),
     ]
 
     @classmethod
     def reference(cls) -> "Params":
-        return cls(3.0, 4.0, 0.1, 0.2, 1e7)
+        return cls.make()
+
+    @classmethod
+    def make(cls, stiffness=3.0, rest_density=4.0, dynamic_viscosity=0.1, dt=0.2,
+             fixed_point_multiplier=1e7, gravity=(0.0, -0.3, 0.0)) -> "Params":
+        """Scene constants; gravity (0, -0.3, 0) is updateGrid.wgsl:34."""
+        p = cls(stiffness, rest_density, dynamic_viscosity, dt, fixed_point_multiplier)
+        for a in range(3):
+            p.gravity[a] = gravity[a]
+        return p
 
 
 _lib = None

@@ -71,3 +71,25 @@ def test_no_device_is_reported_not_faked(pkg):
         pytest.skip("a GPU is present")
     with pytest.raises(pkg.MPMError, match="no CUDA device"):
         pkg.MLSMPMSimulator(None, None, 1.2)
+
+
+def test_batch_scene_generator_is_seeded_and_in_range(pkg):
+    """batch_scenes: counts, sides, walls, gravity magnitude, stiffness range."""
+    d1, r1 = pkg.batch_scenes(12, seed=3)
+    d2, r2 = pkg.batch_scenes(12, seed=3)
+    assert np.array_equal(r1, r2)
+    assert [d.num_particles for d in d1] == [d.num_particles for d in d2]
+    off = 0
+    for d in d1:
+        n = d.num_particles
+        side = d.init_box[0]
+        assert 4000 <= n <= 64000 and side in (32.0, 48.0, 64.0)
+        assert tuple(d.init_box) == (side, side, side) == tuple(d.real_box)
+        pos = r1[off:off + n, :3]
+        assert pos.min() >= 3.0 and pos.max() <= side - 4.0
+        assert np.all(r1[off:off + n, 3:] == 0)
+        g = np.array(list(d.gravity), dtype=np.float64)
+        assert abs(np.linalg.norm(g) - 0.3) < 1e-6
+        assert 2.0 <= d.stiffness <= 4.0
+        off += n
+    assert off == len(r1)

@@ -47,6 +47,21 @@ class Params(ctypes.Structure):
     ]
 
 
+class SceneDesc(ctypes.Structure):
+    """mpm_scene_desc: one scene of a batch."""
+    _fields_ = [
+        ("num_particles", ctypes.c_int),
+        ("init_box", ctypes.c_float * 3),
+        ("real_box", ctypes.c_float * 3),
+        ("stiffness", ctypes.c_float),
+        ("rest_density", ctypes.c_float),
+        ("dynamic_viscosity", ctypes.c_float),
+        ("dt", ctypes.c_float),
+        ("fixed_point_multiplier", ctypes.c_float),
+        ("gravity", ctypes.c_float * 3),
+    ]
+
+
 class KernelStat(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char_p), ("launches", ctypes.c_int64),
                 ("timed_launches", ctypes.c_int64), ("total_ms", ctypes.c_double)]
@@ -111,6 +126,20 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "mpm_set_profiling": (i32, [vp, i32]),
         "mpm_kernel_stats": (i32, [vp, ctypes.POINTER(KernelStat), i32]),
         "mpm_launch_count": (i64, [vp]),
+        "mpm_set_gravity": (i32, [vp, fp]),
+        "mpm_set_graph": (i32, [vp, i32]),
+        "mpm_batch_create": (i32, [ctypes.POINTER(SceneDesc), i32, fp, ctypes.POINTER(vp)]),
+        "mpm_batch_destroy": (i32, [vp]),
+        "mpm_batch_num_scenes": (i32, [vp]),
+        "mpm_batch_num_particles": (i64, [vp]),
+        "mpm_batch_step": (i32, [vp, i32, vp]),
+        "mpm_batch_set_scene": (i32, [vp, i32, ctypes.POINTER(SceneDesc)]),
+        "mpm_batch_set_graph": (i32, [vp, i32]),
+        "mpm_batch_download_particles": (i32, [vp, fp]),
+        "mpm_batch_download_grid": (i32, [vp, i32, ip]),
+        "mpm_batch_posvel_device_ptr": (vp, [vp]),
+        "mpm_batch_check_health": (i32, [vp, ctypes.POINTER(Health)]),
+        "mpm_batch_launch_count": (i64, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

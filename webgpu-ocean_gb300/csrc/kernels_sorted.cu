@@ -30,9 +30,16 @@
 //  * Particles whose 27-cell stencil leaves the box (quirk Q1 aliasing, NaN,
 //    huge coordinates) or leaves the task's arena take a global path that
 //    uses the reference's flat indices directly.
+//  * Batches: many independent scenes advance in the same launches.  Their
+//    particles, bricks and bins are concatenated; a task belongs to one scene
+//    and reads that scene's geometry and constants from a table (BATCH
+//    instantiations).  The single-scene instantiations take them as kernel
+//    parameters.
 #include <climits>
 #include <cstdio>
+#include <cstring>
 #include <string>
+#include <vector>
 
 #include "mpm_internal.h"
 #include "mpm_math_x2.cuh"
@@ -88,12 +95,23 @@ struct Geo {
 };
 
 // A task: particles [first, first + count) of the bin order, all in `brick`
-// (-1: the bin of irregular particles).
+// (scene-local; -1: the scene's bin of irregular particles) of `scene`.
 struct __align__(16) Task {
     int first;
     int count;
     int brick;
-    int pad;
+    int scene;
+};
+
+// One scene of a batch: its geometry and constants, and where its bricks,
+// bins and particles start in the concatenated arrays.  A scene's bins are
+// its bricks followed by its irregular bin.
+struct Scene {
+    Geo g;
+    int bbase;
+    int binbase;
+    int pbase;
+    SimConsts k;
 };
 
 struct Dev {
@@ -111,7 +129,30 @@ struct Dev {
     Task* tasks;
     uint32_t* ntasks;
     uint32_t* task_next;  // [3] work counters: p2g_2, g2p+p2g_1, first p2g_1
+    // Batches only (null for one scene):
+    const Scene* scenes;
+    const uint32_t* brick_scene;  // global brick -> scene
+    const uint32_t* bin_scene;    // global bin -> scene
+    int nscenes;
 };
+
+// The scene of a task: the table entry in a batch, else the kernel's own.
+template <bool BATCH>
+__device__ __forceinline__ const Scene& scene_ref(const Dev& d, const Scene& one, int s) {
+    if constexpr (BATCH) return d.scenes[s];
+    else return one;
+}
+// First global brick / bin of a scene (0 for a single scene).
+template <bool BATCH>
+__device__ __forceinline__ int brick_base(const Scene& s) {
+    if constexpr (BATCH) return s.bbase;
+    else return 0;
+}
+template <bool BATCH>
+__device__ __forceinline__ uint32_t bin_base(const Scene& s) {
+    if constexpr (BATCH) return (uint32_t)s.binbase;
+    else return 0u;
+}
 
 enum { kCtrP2G2 = 0, kCtrG2P = 1, kCtrP2G1 = 2 };
 
@@ -196,8 +237,9 @@ __device__ __forceinline__ void count_bin(const Dev& d, bool active, int slot, u
     }
 }
 
-__device__ __forceinline__ uint32_t bin_key(const Geo& g, bool reg, int bx, int by, int bz) {
-    return reg ? (uint32_t)brick_of(g, bx, by, bz) : (uint32_t)g.nbricks;
+__device__ __forceinline__ uint32_t bin_key(const Geo& g, uint32_t base, bool reg, int bx, int by,
+                                           int bz) {
+    return base + (reg ? (uint32_t)brick_of(g, bx, by, bz) : (uint32_t)g.nbricks);
 }
 
 // Clears the dirty bricks of grid gi (warp per brick, grid-stride over the
@@ -355,8 +397,9 @@ __device__ __forceinline__ void build_lane_table(const Particles& P, const Geo& 
 // (decoded into the other buffer after the compute), and task i-1's momentum
 // arena is flushed (each thread reads, flushes and zeroes its own slots).
 // ---------------------------------------------------------------------------
+template <bool BATCH>
 __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
-    k_p2g2(Particles P, Geo g, SimConsts k, Dev d, int cur, unsigned long long* oob) {
+    k_p2g2(Particles P, Scene one, Dev d, int cur, unsigned long long* oob) {
     __shared__ float s_mass[2][kNA];
     __shared__ int s_q[2][3][kNA];
     __shared__ int s_task[2];
@@ -365,7 +408,7 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
 
     clear_dirty(d, cur ^ 1);
 
-    int4* __restrict__ grid = d.grid[cur];
+    int4* __restrict__ grid_all = d.grid[cur];
     unsigned bad = 0;
     const int ntasks = (int)__ldcg(d.ntasks);
     for (int i = threadIdx.x; i < 2 * 3 * kNA; i += kTask) (&s_q[0][0][0])[i] = 0;
@@ -375,41 +418,48 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
     }
     __syncthreads();
 
-    // arena origin (brick - 1 cell) of a task, or false for the irregular bin
-    auto origin = [&](const Task& tk, int& ox, int& oy, int& oz) -> bool {
+    // arena origin (brick - 1 cell) of a task, or false for an irregular bin
+    auto origin = [&](const Geo& tg, const Task& tk, int& ox, int& oy, int& oz) -> bool {
         if (tk.brick < 0) return false;
-        brick_coords(g, tk.brick, ox, oy, oz);
+        brick_coords(tg, tk.brick, ox, oy, oz);
         ox = 4 * ox - 1;
         oy = 4 * oy - 1;
         oz = 4 * oz - 1;
         return true;
     };
-    // raw mass words of this thread's arena slots for a task
-    auto load_mass = [&](int t, int m[kPer]) {
+    // raw mass words of this thread's arena slots for a task, and its FM
+    auto load_mass = [&](int t, int m[kPer], float& fm) {
 #pragma unroll
         for (int q = 0; q < kPer; ++q) m[q] = 0;
+        fm = one.k.fm;
         if (t >= ntasks) return;
+        const Task tk = d.tasks[t];
+        const Scene& ts = scene_ref<BATCH>(d, one, tk.scene);
+        fm = ts.k.fm;
         int ox, oy, oz;
-        if (!origin(d.tasks[t], ox, oy, oz)) return;
+        if (!origin(ts.g, tk, ox, oy, oz)) return;
+        const int4* grid = grid_all + (size_t)brick_base<BATCH>(ts) * 64;
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
             const int li = (int)threadIdx.x + q * kTask;
             int x, y, z;
             if (li < kNA && arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z) &&
-                cell_exists(g, x, y, z))
-                m[q] = __ldcg(reinterpret_cast<const int*>(grid + brick_addr(g, x, y, z)) + 3);
+                cell_exists(ts.g, x, y, z))
+                m[q] = __ldcg(reinterpret_cast<const int*>(grid + brick_addr(ts.g, x, y, z)) + 3);
         }
     };
-    auto store_mass = [&](int buf, const int m[kPer]) {
+    auto store_mass = [&](int buf, const int m[kPer], float fm) {
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
             const int li = (int)threadIdx.x + q * kTask;
-            if (li < kNA) s_mass[buf][li] = dec(m[q], k.fm);
+            if (li < kNA) s_mass[buf][li] = dec(m[q], fm);
         }
     };
     auto flush = [&](int buf, const Task& tk) {
+        const Scene& ts = scene_ref<BATCH>(d, one, tk.scene);
         int ox, oy, oz;
-        if (!origin(tk, ox, oy, oz)) return;
+        if (!origin(ts.g, tk, ox, oy, oz)) return;
+        int4* grid = grid_all + (size_t)brick_base<BATCH>(ts) * 64;
         for (int li = threadIdx.x; li < kNA; li += kTask) {
             const int q0 = s_q[buf][0][li], q1 = s_q[buf][1][li], q2 = s_q[buf][2][li];
             if ((q0 | q1 | q2) == 0) continue;
@@ -418,8 +468,8 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
             s_q[buf][2][li] = 0;
             int x, y, z;
             if (!arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z)) continue;
-            if (!cell_exists(g, x, y, z)) continue;  // unreachable for regular particles
-            int* c = reinterpret_cast<int*>(grid + brick_addr(g, x, y, z));
+            if (!cell_exists(ts.g, x, y, z)) continue;  // unreachable for regular particles
+            int* c = reinterpret_cast<int*>(grid + brick_addr(ts.g, x, y, z));
             if (q0) atomicAdd(c + 0, q0);
             if (q1) atomicAdd(c + 1, q1);
             if (q2) atomicAdd(c + 2, q2);
@@ -429,12 +479,14 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
     int t = s_task[0];
     {
         int m[kPer];
-        load_mass(t, m);
-        store_mass(0, m);
+        float fm;
+        load_mass(t, m, fm);
+        store_mass(0, m, fm);
     }
     Task prev;
     prev.brick = -1;
     prev.count = 0;
+    prev.scene = 0;
     bool have_prev = false;
     int it = 0;
     while (t < ntasks) {
@@ -443,10 +495,16 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
         const int t_next = s_task[buf ^ 1];
         if (threadIdx.x == 0) s_task[buf] = claim_task(d, kCtrP2G2);
         int m_next[kPer];
-        load_mass(t_next, m_next);
+        float fm_next;
+        load_mass(t_next, m_next, fm_next);
         if (have_prev) flush(buf ^ 1, prev);
 
         const Task task = d.tasks[t];
+        const Scene& sc = scene_ref<BATCH>(d, one, task.scene);
+        const Geo& g = sc.g;
+        const SimConsts& k = sc.k;
+        const int bb = brick_base<BATCH>(sc);
+        int4* __restrict__ grid = grid_all + (size_t)bb * 64;
         int tbx = 0, tby = 0, tbz = 0;
         if (task.brick >= 0) brick_coords(g, task.brick, tbx, tby, tbz);
         const bool table = task.brick >= 0 && task.count <= kMaxSort;  // uniform
@@ -491,11 +549,11 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
                         atomicAdd(c + 0, mx);
                         atomicAdd(c + 1, my);
                         atomicAdd(c + 2, mz);
-                        mark_brick(d, cur, (uint32_t)(a >> 6));
+                        mark_brick(d, cur, (uint32_t)(bb + (a >> 6)));
                     });
             }
         }
-        store_mass(buf ^ 1, m_next);
+        store_mass(buf ^ 1, m_next, fm_next);
         prev = task;
         have_prev = true;
         t = t_next;
@@ -512,18 +570,22 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
 // those bricks, decoded, to the float velocity grid g2p reads:
 // (dec(vx), dec(vy), dec(vz), dec(vz)).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_update(Geo g, SimConsts k, Dev d, int cur) {
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_update(Scene one, Dev d, int cur) {
     const uint32_t nd = __ldcg(d.dirty_n + cur);
-    const int hx = wall_hi(k.real_box[0]), hy = wall_hi(k.real_box[1]), hz = wall_hi(k.real_box[2]);
     const unsigned lane = threadIdx.x & 31u;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     int4* __restrict__ grid = d.grid[cur];
     float4* __restrict__ gv = d.gv[cur];
     for (uint32_t i = warp; i < nd; i += nwarps) {
-        const int b = (int)__ldcg(d.dirty_list[cur] + i);
+        const int b = (int)__ldcg(d.dirty_list[cur] + i);  // global brick
+        const Scene& sc = scene_ref<BATCH>(d, one, BATCH ? (int)__ldg(d.brick_scene + b) : 0);
+        const SimConsts& k = sc.k;
+        const int hx = wall_hi(k.real_box[0]), hy = wall_hi(k.real_box[1]),
+                  hz = wall_hi(k.real_box[2]);
         int bx, by, bz;
-        brick_coords(g, b, bx, by, bz);
+        brick_coords(sc.g, b - brick_base<BATCH>(sc), bx, by, bz);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int c = (int)lane + 32 * h;
@@ -551,18 +613,18 @@ __global__ void __launch_bounds__(256) k_update(Geo g, SimConsts k, Dev d, int c
 // reads, flushes and zeroes its own slots); the bricks task i-1's stencils
 // reached are registered as dirty right after the barrier.
 // ---------------------------------------------------------------------------
-template <bool DO_G2P, bool POSVEL>
+template <bool BATCH, bool DO_G2P, bool POSVEL>
 __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
     k_g2p_p2g1(Particles Pin, Particles Pout, const uint32_t* __restrict__ id_in,
-               uint32_t* __restrict__ id_out, float4* __restrict__ posvel, Geo g, SimConsts k,
-               Dev d, int src, int dst, unsigned long long* oob) {
+               uint32_t* __restrict__ id_out, float4* __restrict__ posvel, Scene one, Dev d,
+               int src, int dst, unsigned long long* oob) {
     __shared__ __align__(16) float4 s_v[DO_G2P ? 2 : 1][DO_G2P ? kNA : 1];
     __shared__ int s_a[2][4][kNB];
     __shared__ int s_touch[2][27];
     __shared__ int s_task[2];
 
-    const float4* __restrict__ gvsrc = d.gv[src];
-    int4* __restrict__ gdst = d.grid[dst];
+    const float4* __restrict__ gv_all = d.gv[src];
+    int4* __restrict__ gdst_all = d.grid[dst];
     const int ctr = DO_G2P ? kCtrG2P : kCtrP2G1;
     unsigned bad = 0;
     const int ntasks = (int)__ldcg(d.ntasks);
@@ -579,22 +641,25 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
         if (!DO_G2P || t >= ntasks) return;
         const Task tk = d.tasks[t];
         if (tk.brick < 0) return;
+        const Scene& ts = scene_ref<BATCH>(d, one, tk.scene);
+        const float4* gvsrc = gv_all + (size_t)brick_base<BATCH>(ts) * 64;
         int ox, oy, oz;
-        brick_coords(g, tk.brick, ox, oy, oz);
+        brick_coords(ts.g, tk.brick, ox, oy, oz);
         ox = 4 * ox - 1;
         oy = 4 * oy - 1;
         oz = 4 * oz - 1;
         for (int li = threadIdx.x; li < kNA; li += kTask) {
             int x, y, z;
-            if (arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z) && cell_exists(g, x, y, z))
-                cp_async16(&s_v[buf][li], gvsrc + brick_addr(g, x, y, z));
+            if (arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z) && cell_exists(ts.g, x, y, z))
+                cp_async16(&s_v[buf][li], gvsrc + brick_addr(ts.g, x, y, z));
             else
                 s_v[buf][li] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
         cp_async_commit();
     };
-    // flush the p2g_1 arena of a task with brick coordinates tb
-    auto flush = [&](int buf, int tbx, int tby, int tbz) {
+    // flush the p2g_1 arena of a task of scene ts with brick coordinates tb
+    auto flush = [&](int buf, const Scene& ts, int tbx, int tby, int tbz) {
+        int4* gdst = gdst_all + (size_t)brick_base<BATCH>(ts) * 64;
         const int ox = 4 * tbx - 2, oy = 4 * tby - 2, oz = 4 * tbz - 2;
         for (int li = threadIdx.x; li < kNB; li += kTask) {
             const int q0 = s_a[buf][0][li], q1 = s_a[buf][1][li], q2 = s_a[buf][2][li],
@@ -606,8 +671,8 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
             s_a[buf][3][li] = 0;
             int x, y, z;
             if (!arena_cell<kB, kSXB, kSYB>(li, ox, oy, oz, x, y, z)) continue;
-            if (!cell_exists(g, x, y, z)) continue;  // unreachable for regular particles
-            int* c = reinterpret_cast<int*>(gdst + brick_addr(g, x, y, z));
+            if (!cell_exists(ts.g, x, y, z)) continue;  // unreachable for regular particles
+            int* c = reinterpret_cast<int*>(gdst + brick_addr(ts.g, x, y, z));
             if (q0) atomicAdd(c + 0, q0);
             if (q1) atomicAdd(c + 1, q1);
             if (q2) atomicAdd(c + 2, q2);
@@ -615,11 +680,12 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
         }
     };
     // register the bricks (3x3x3 around tb) flagged in s_touch[buf]
-    auto mark = [&](int buf, int tbx, int tby, int tbz) {
+    auto mark = [&](int buf, const Scene& ts, int tbx, int tby, int tbz) {
         if (threadIdx.x < 27 && s_touch[buf][threadIdx.x]) {
             const int i = threadIdx.x;
             const int nbx = tbx + i / 9 - 1, nby = tby + (i / 3) % 3 - 1, nbz = tbz + i % 3 - 1;
-            mark_brick(d, dst, (uint32_t)((nbx * g.BY + nby) * g.BZ + nbz));
+            mark_brick(d, dst,
+                       (uint32_t)(brick_base<BATCH>(ts) + (nbx * ts.g.BY + nby) * ts.g.BZ + nbz));
             s_touch[buf][i] = 0;
         }
     };
@@ -628,6 +694,7 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
     prefetch(t, 0);
     bool have_prev = false, prev_arena = false;
     int pbx = 0, pby = 0, pbz = 0;  // brick of the previous task
+    int pscene = 0;                 // and its scene
     int it = 0;
     while (t < ntasks) {
         const int buf = it & 1;
@@ -635,11 +702,19 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
         __syncthreads();  // s_v[buf] arrived; task it-1 computed everywhere
         const int t_next = s_task[buf ^ 1];
         if (threadIdx.x == 0) s_task[buf] = claim_task(d, ctr);
-        if (have_prev && prev_arena) mark(buf ^ 1, pbx, pby, pbz);
+        if (have_prev && prev_arena) mark(buf ^ 1, scene_ref<BATCH>(d, one, pscene), pbx, pby, pbz);
         prefetch(t_next, buf ^ 1);
-        if (have_prev && prev_arena) flush(buf ^ 1, pbx, pby, pbz);
+        if (have_prev && prev_arena)
+            flush(buf ^ 1, scene_ref<BATCH>(d, one, pscene), pbx, pby, pbz);
 
         const Task task = d.tasks[t];
+        const Scene& sc = scene_ref<BATCH>(d, one, task.scene);
+        const Geo& g = sc.g;
+        const SimConsts& k = sc.k;
+        const int bb = brick_base<BATCH>(sc);
+        const uint32_t binb = bin_base<BATCH>(sc);
+        const float4* __restrict__ gvsrc = gv_all + (size_t)bb * 64;
+        int4* __restrict__ gdst = gdst_all + (size_t)bb * 64;
         int tbx = 0, tby = 0, tbz = 0;
         if (task.brick >= 0) brick_coords(g, task.brick, tbx, tby, tbz);
         for (int base = 0; base < task.count; base += kTask) {
@@ -741,41 +816,55 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
                                       atomicAdd(c + 0, vx);
                                       atomicAdd(c + 1, vy);
                                       atomicAdd(c + 2, vz);
-                                      mark_brick(d, dst, (uint32_t)(a >> 6));
+                                      mark_brick(d, dst, (uint32_t)(bb + (a >> 6)));
                                   });
                 }
             }
-            if (DO_G2P) count_bin(d, active, jo, bin_key(g, reg, bx, by, bz));
+            if (DO_G2P) count_bin(d, active, jo, bin_key(g, binb, reg, bx, by, bz));
         }
         have_prev = true;
         prev_arena = task.brick >= 0;
         pbx = tbx;
         pby = tby;
         pbz = tbz;
+        pscene = task.scene;
         t = t_next;
         ++it;
     }
     __syncthreads();
     if (have_prev && prev_arena) {
-        mark((it - 1) & 1, pbx, pby, pbz);
-        flush((it - 1) & 1, pbx, pby, pbz);
+        mark((it - 1) & 1, scene_ref<BATCH>(d, one, pscene), pbx, pby, pbz);
+        flush((it - 1) & 1, scene_ref<BATCH>(d, one, pscene), pbx, pby, pbz);
     }
     if (bad) atomicAdd(oob, (unsigned long long)bad);
 }
 
-// Bins the particles at their current positions (slot order).
-__global__ void __launch_bounds__(kTask) k_bin(Particles P, Geo g, Dev d, int n) {
+// Bins the particles at their current positions (slot order).  In a batch
+// the scene of slot i is found by bisecting the scenes' first particles.
+template <bool BATCH>
+__global__ void __launch_bounds__(kTask) k_bin(Particles P, Scene one, Dev d, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = i < n;
+    int s = 0;
+    if (BATCH && active) {
+        int lo = 0, hi = d.nscenes - 1;  // last scene with pbase <= i
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (d.scenes[mid].pbase <= i) lo = mid;
+            else hi = mid - 1;
+        }
+        s = lo;
+    }
+    const Scene& sc = scene_ref<BATCH>(d, one, s);
     int bx = 0, by = 0, bz = 0;
     bool reg = false;
     if (active) {
         const float4 a = P.p0[i];
         const float x[3] = {a.x, a.y, a.z};
         base_cell(x, bx, by, bz);
-        reg = regular_base(g, bx, by, bz);
+        reg = regular_base(sc.g, bx, by, bz);
     }
-    count_bin(d, active, active ? i : 0, bin_key(g, reg, bx, by, bz));
+    count_bin(d, active, active ? i : 0, bin_key(sc.g, bin_base<BATCH>(sc), reg, bx, by, bz));
 }
 
 // Exclusive scan of the bin counts -> bin_start and the task list (one task
@@ -845,8 +934,15 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, int nbins) {
             Task tk;
             tk.first = (int)start;
             tk.count = (int)c;
-            tk.brick = bin == nbins - 1 ? -1 : bin;
-            tk.pad = 0;
+            if (d.bin_scene) {
+                const int sc = (int)__ldg(d.bin_scene + bin);
+                const int local = bin - d.scenes[sc].binbase;
+                tk.brick = local == d.scenes[sc].g.nbricks ? -1 : local;
+                tk.scene = sc;
+            } else {
+                tk.brick = bin == nbins - 1 ? -1 : bin;
+                tk.scene = 0;
+            }
             d.tasks[pre_t + et] = tk;
         }
     }
@@ -876,11 +972,29 @@ __global__ void k_export(const int4* __restrict__ grid, Geo g, int4* __restrict_
 
 }  // namespace
 
+// A captured run of substeps and the engine state it starts from / ends in.
+struct GraphEntry {
+    int substeps = 0;
+    int cur0 = 0, pcur0 = 0;     // e->cur, ps->cur before
+    float4* posvel = nullptr;
+    unsigned long long* oob = nullptr;
+    int cur1 = 0, last1 = 0, pcur1 = 0;
+    long long launches[KID_COUNT] = {};
+    cudaGraphExec_t exec = nullptr;
+};
+
 struct SortedEngine {
     int max_particles = 0;
-    Geo geo{};
     bool configured = false;
+    bool batch = false;
+    Scene one{};                 // the scene (single) or scene 0 (batch)
+    std::vector<Scene> scenes;   // batch: host copy of the table
+    int nbins = 0;               // all scenes' bins
+    int nbricks = 0;             // all scenes' bricks
     Dev d{};
+    Scene* scenes_d = nullptr;
+    uint32_t* brick_scene_d = nullptr;
+    uint32_t* bin_scene_d = nullptr;
     size_t grid_cells_alloc = 0;  // cells per grid buffer
     int bricks_alloc = 0;
     int max_tasks = 0;
@@ -889,6 +1003,7 @@ struct SortedEngine {
     bool primed = false;
     bool has_grid = false;
     int blocks_p2g2 = 0, blocks_g2p = 0, blocks_update = 0;
+    std::vector<GraphEntry> graphs;
 };
 
 namespace {
@@ -902,7 +1017,14 @@ namespace {
         }                                                                    \
     } while (0)
 
+void drop_graphs(SortedEngine* e) {
+    for (GraphEntry& g : e->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    e->graphs.clear();
+}
+
 void free_grid_state(SortedEngine* e) {
+    drop_graphs(e);
     for (int b = 0; b < 2; ++b) {
         cudaFree(e->d.gv[b]);
         e->d.gv[b] = nullptr;
@@ -923,6 +1045,17 @@ void free_grid_state(SortedEngine* e) {
     e->max_tasks = 0;
 }
 
+void free_tables(SortedEngine* e) {
+    cudaFree(e->scenes_d);
+    cudaFree(e->brick_scene_d);
+    cudaFree(e->bin_scene_d);
+    e->scenes_d = nullptr;
+    e->brick_scene_d = e->bin_scene_d = nullptr;
+    e->d.scenes = nullptr;
+    e->d.brick_scene = e->d.bin_scene = nullptr;
+    e->d.nscenes = 1;
+}
+
 int occupancy_blocks(const void* fn, int threads) {
     int dev = 0, nsm = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
@@ -932,12 +1065,57 @@ int occupancy_blocks(const void* fn, int threads) {
     return nsm * per;
 }
 
+// Brick geometry of one scene; false for a degenerate box.
+bool make_geo(const SimConsts& k, Geo& g) {
+    if (k.Y <= 0 || k.Z <= 0 || k.grid_count <= 0) return false;
+    g = Geo{};
+    g.Y = k.Y;
+    g.Z = k.Z;
+    const long long yz = (long long)k.Y * k.Z;
+    if (yz > INT_MAX) return false;
+    g.YZ = (int)yz;
+    g.grid_count = k.grid_count;
+    g.Xi = (int)(((long long)k.grid_count + yz - 1) / yz);
+    g.BX = (g.Xi + 3) / 4;
+    g.BY = (g.Y + 3) / 4;
+    g.BZ = (g.Z + 3) / 4;
+    const long long nb = (long long)g.BX * g.BY * g.BZ;
+    if (nb * 64 > INT_MAX) return false;
+    g.nbricks = (int)nb;
+    return true;
+}
+
+// Grids, dirty lists, bin arrays and the task list for `bricks` bricks and
+// `bins` bins (kept when large enough).
+int ensure_grid_state(SortedEngine* e, long long bricks, long long bins) {
+    const size_t cells = (size_t)bricks * 64;
+    const long long max_tasks = bins + 1;
+    drop_graphs(e);
+    if (cells <= e->grid_cells_alloc && bricks <= e->bricks_alloc && max_tasks <= e->max_tasks)
+        return 0;
+    free_grid_state(e);
+    for (int b = 0; b < 2; ++b) {
+        SE_CUDA(cudaMalloc(&e->d.grid[b], sizeof(int4) * cells));
+        SE_CUDA(cudaMalloc(&e->d.gv[b], sizeof(float4) * cells));
+        SE_CUDA(cudaMalloc(&e->d.dirty_flag[b], 4 * (size_t)bricks));
+        SE_CUDA(cudaMalloc(&e->d.dirty_list[b], 4 * (size_t)bricks));
+    }
+    SE_CUDA(cudaMalloc(&e->d.bin_count, 4 * ((size_t)bins + kScanThreads)));
+    SE_CUDA(cudaMalloc(&e->d.bin_start, 4 * ((size_t)bins + 1)));
+    SE_CUDA(cudaMalloc(&e->d.tasks, sizeof(Task) * (size_t)max_tasks));
+    e->grid_cells_alloc = cells;
+    e->bricks_alloc = (int)bricks;
+    e->max_tasks = (int)max_tasks;
+    return 0;
+}
+
 }  // namespace
 
 int sorted_create(SortedEngine** out, int max_particles) {
     *out = nullptr;
     SortedEngine* e = new SortedEngine();
     e->max_particles = max_particles;
+    e->d.nscenes = 1;
     const size_t np = (size_t)(max_particles > 0 ? max_particles : 1);
     cudaError_t r = cudaMalloc(&e->d.bin_of, 4 * np);
     if (r == cudaSuccess) r = cudaMalloc(&e->d.rank_of, 4 * np);
@@ -947,9 +1125,9 @@ int sorted_create(SortedEngine** out, int max_particles) {
     if (r == cudaSuccess) r = cudaMalloc(&e->d.ntasks, 4);
     if (r == cudaSuccess) r = cudaMalloc(&e->d.task_next, 4 * 3);
     if (r == cudaSuccess) {
-        e->blocks_p2g2 = occupancy_blocks((const void*)k_p2g2, kTask);
-        e->blocks_g2p = occupancy_blocks((const void*)k_g2p_p2g1<true, false>, kTask);
-        e->blocks_update = occupancy_blocks((const void*)k_update, 256);
+        e->blocks_p2g2 = occupancy_blocks((const void*)k_p2g2<false>, kTask);
+        e->blocks_g2p = occupancy_blocks((const void*)k_g2p_p2g1<false, true, false>, kTask);
+        e->blocks_update = occupancy_blocks((const void*)k_update<false>, 256);
         if (e->blocks_p2g2 <= 0 || e->blocks_g2p <= 0 || e->blocks_update <= 0)
             r = cudaErrorInvalidValue;
     }
@@ -965,6 +1143,7 @@ int sorted_create(SortedEngine** out, int max_particles) {
 void sorted_destroy(SortedEngine* e) {
     if (!e) return;
     free_grid_state(e);
+    free_tables(e);
     cudaFree(e->d.bin_of);
     cudaFree(e->d.rank_of);
     cudaFree(e->d.order);
@@ -979,40 +1158,86 @@ int sorted_configure(SortedEngine* e, const SimConsts& k) {
     e->configured = false;
     e->primed = false;
     e->has_grid = false;
-    if (k.Y <= 0 || k.Z <= 0 || k.grid_count <= 0) return -1;
-    Geo g{};
-    g.Y = k.Y;
-    g.Z = k.Z;
-    const long long yz = (long long)k.Y * k.Z;
-    if (yz > INT_MAX) return -1;
-    g.YZ = (int)yz;
-    g.grid_count = k.grid_count;
-    g.Xi = (int)(((long long)k.grid_count + yz - 1) / yz);
-    g.BX = (g.Xi + 3) / 4;
-    g.BY = (g.Y + 3) / 4;
-    g.BZ = (g.Z + 3) / 4;
-    const long long nb = (long long)g.BX * g.BY * g.BZ;
-    if (nb * 64 > INT_MAX) return -1;
-    g.nbricks = (int)nb;
-    const size_t cells = (size_t)nb * 64;
-    const int max_tasks = g.nbricks + 2;
-    if (cells > e->grid_cells_alloc || g.nbricks > e->bricks_alloc || max_tasks > e->max_tasks) {
-        free_grid_state(e);
-        for (int b = 0; b < 2; ++b) {
-            SE_CUDA(cudaMalloc(&e->d.grid[b], sizeof(int4) * cells));
-            SE_CUDA(cudaMalloc(&e->d.gv[b], sizeof(float4) * cells));
-            SE_CUDA(cudaMalloc(&e->d.dirty_flag[b], 4 * (size_t)g.nbricks));
-            SE_CUDA(cudaMalloc(&e->d.dirty_list[b], 4 * (size_t)g.nbricks));
-        }
-        SE_CUDA(cudaMalloc(&e->d.bin_count, 4 * ((size_t)g.nbricks + 1 + kScanThreads)));
-        SE_CUDA(cudaMalloc(&e->d.bin_start, 4 * ((size_t)g.nbricks + 2)));
-        SE_CUDA(cudaMalloc(&e->d.tasks, sizeof(Task) * (size_t)max_tasks));
-        e->grid_cells_alloc = cells;
-        e->bricks_alloc = g.nbricks;
-        e->max_tasks = max_tasks;
-    }
-    e->geo = g;
+    Geo g;
+    if (!make_geo(k, g)) return -1;
+    if (ensure_grid_state(e, g.nbricks, (long long)g.nbricks + 1)) return -1;
+    free_tables(e);
+    e->batch = false;
+    e->scenes.clear();
+    e->one = Scene{};
+    e->one.g = g;
+    e->one.k = k;
+    e->nbricks = g.nbricks;
+    e->nbins = g.nbricks + 1;
     e->configured = true;
+    return 0;
+}
+
+int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes) {
+    e->configured = false;
+    e->primed = false;
+    e->has_grid = false;
+    if (nscenes < 1) {
+        g_err = "a batch needs at least one scene";
+        return -1;
+    }
+    std::vector<Scene> hs((size_t)nscenes);
+    long long bricks = 0, bins = 0, parts = 0;
+    for (int s = 0; s < nscenes; ++s) {
+        if (!make_geo(ks[s], hs[s].g)) {
+            g_err = "scene " + std::to_string(s) + " has a degenerate box";
+            return -1;
+        }
+        hs[s].bbase = (int)bricks;
+        hs[s].binbase = (int)bins;
+        hs[s].pbase = (int)parts;
+        hs[s].k = ks[s];
+        bricks += hs[s].g.nbricks;
+        bins += (long long)hs[s].g.nbricks + 1;
+        parts += ks[s].n;
+        if (bricks * 64 > INT_MAX || parts > e->max_particles) {
+            g_err = "batch exceeds the engine's capacity";
+            return -1;
+        }
+    }
+    if (ensure_grid_state(e, bricks, bins)) return -1;
+    free_tables(e);
+    std::vector<uint32_t> brick_scene((size_t)bricks), bin_scene((size_t)bins);
+    for (int s = 0; s < nscenes; ++s) {
+        for (int b = 0; b < hs[s].g.nbricks; ++b) brick_scene[(size_t)hs[s].bbase + b] = (uint32_t)s;
+        for (int b = 0; b <= hs[s].g.nbricks; ++b) bin_scene[(size_t)hs[s].binbase + b] = (uint32_t)s;
+    }
+    SE_CUDA(cudaMalloc(&e->scenes_d, sizeof(Scene) * (size_t)nscenes));
+    SE_CUDA(cudaMalloc(&e->brick_scene_d, 4 * (size_t)bricks));
+    SE_CUDA(cudaMalloc(&e->bin_scene_d, 4 * (size_t)bins));
+    SE_CUDA(cudaMemcpy(e->scenes_d, hs.data(), sizeof(Scene) * (size_t)nscenes, cudaMemcpyHostToDevice));
+    SE_CUDA(cudaMemcpy(e->brick_scene_d, brick_scene.data(), 4 * (size_t)bricks, cudaMemcpyHostToDevice));
+    SE_CUDA(cudaMemcpy(e->bin_scene_d, bin_scene.data(), 4 * (size_t)bins, cudaMemcpyHostToDevice));
+    e->d.scenes = e->scenes_d;
+    e->d.brick_scene = e->brick_scene_d;
+    e->d.bin_scene = e->bin_scene_d;
+    e->d.nscenes = nscenes;
+    e->batch = true;
+    e->scenes = hs;
+    e->one = hs[0];
+    e->nbricks = (int)bricks;
+    e->nbins = (int)bins;
+    e->configured = true;
+    return 0;
+}
+
+int sorted_set_scene_consts(SortedEngine* e, int scene, const SimConsts& k, cudaStream_t st) {
+    if (!e->configured || !e->batch || scene < 0 || scene >= (int)e->scenes.size()) {
+        g_err = "no such scene in the batch";
+        return -1;
+    }
+    Scene& sc = e->scenes[(size_t)scene];
+    if (k.Y != sc.k.Y || k.Z != sc.k.Z || k.grid_count != sc.k.grid_count || k.n != sc.k.n) {
+        g_err = "a scene's geometry and particle count are fixed at batch creation";
+        return -1;
+    }
+    sc.k = k;
+    SE_CUDA(cudaMemcpyAsync(&e->scenes_d[scene].k, &sc.k, sizeof(SimConsts), cudaMemcpyHostToDevice, st));
     return 0;
 }
 
@@ -1031,58 +1256,28 @@ bool sorted_has_grid(const SortedEngine* e) { return e && e->has_grid; }
         prof->after((id), st);   \
     } while (0)
 
-int sorted_step(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned long long* oob,
-                const SimConsts& k, int substeps, cudaStream_t st, LaunchProfiler* prof) {
-    if (!e->configured) {
-        g_err = "sorted engine is not configured for this scene";
-        return -1;
-    }
-    const Geo& g = e->geo;
-    const int n = k.n;
-    const int nbins = g.nbricks + 1;
-    if (n == 0 || substeps == 0) {
-        if (n == 0 && substeps > 0) e->has_grid = false;
-        return 0;
-    }
-    if (!e->primed) {
-        const size_t cells = (size_t)g.nbricks * 64;
-        for (int b = 0; b < 2; ++b) {
-            SE_CUDA(cudaMemsetAsync(e->d.grid[b], 0, sizeof(int4) * cells, st));
-            SE_CUDA(cudaMemsetAsync(e->d.gv[b], 0, sizeof(float4) * cells, st));
-            SE_CUDA(cudaMemsetAsync(e->d.dirty_flag[b], 0, 4 * (size_t)g.nbricks, st));
-        }
-        SE_CUDA(cudaMemsetAsync(e->d.dirty_n, 0, 8, st));
-        SE_CUDA(cudaMemsetAsync(e->d.ticket, 0, 4, st));
-        SE_CUDA(cudaMemsetAsync(e->d.task_next, 0, 4 * 3, st));
-        SE_CUDA(cudaMemsetAsync(e->d.bin_count, 0, 4 * (size_t)nbins, st));
-        const Particles& P = ps->P[ps->cur];
-        LAUNCH(KID_BIN, (k_bin<<<(n + kTask - 1) / kTask, kTask, 0, st>>>(P, g, e->d, n)));
-        LAUNCH(KID_SCAN, (k_scan<<<(nbins + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(e->d, nbins)));
-        LAUNCH(KID_SCATTER, (k_scatter<<<(max(n, nbins) + 255) / 256, 256, 0, st>>>(e->d, n, nbins)));
-        e->cur = 0;
-        LAUNCH(KID_SORTED_P2G_1,
-               (k_g2p_p2g1<false, false><<<e->blocks_g2p, kTask, 0, st>>>(
-                   P, P, ps->id[ps->cur], ps->id[ps->cur], posvel, g, k, e->d, e->cur, e->cur,
-                   oob)));
-        SE_CUDA(cudaGetLastError());
-        e->primed = true;
-    }
+namespace {
+
+// Issues the kernels of `substeps` substeps and advances the engine state.
+template <bool BATCH>
+int enqueue_substeps(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned long long* oob,
+                     const Scene& one, int n, int substeps, cudaStream_t st, LaunchProfiler* prof) {
+    const int nbins = e->nbins;
     for (int s = 0; s < substeps; ++s) {
         const int cur = e->cur, nxt = cur ^ 1;
         const int pin = ps->cur, pout = pin ^ 1;
         LAUNCH(KID_SORTED_P2G_2,
-               (k_p2g2<<<e->blocks_p2g2, kTask, 0, st>>>(ps->P[pin], g, k, e->d, cur, oob)));
-        LAUNCH(KID_UPDATE_GRID,
-               (k_update<<<e->blocks_update, 256, 0, st>>>(g, k, e->d, cur)));
+               (k_p2g2<BATCH><<<e->blocks_p2g2, kTask, 0, st>>>(ps->P[pin], one, e->d, cur, oob)));
+        LAUNCH(KID_UPDATE_GRID, (k_update<BATCH><<<e->blocks_update, 256, 0, st>>>(one, e->d, cur)));
         if (s == substeps - 1)
             LAUNCH(KID_SORTED_G2P_P2G_1,
-                   (k_g2p_p2g1<true, true><<<e->blocks_g2p, kTask, 0, st>>>(
-                       ps->P[pin], ps->P[pout], ps->id[pin], ps->id[pout], posvel, g, k, e->d, cur,
+                   (k_g2p_p2g1<BATCH, true, true><<<e->blocks_g2p, kTask, 0, st>>>(
+                       ps->P[pin], ps->P[pout], ps->id[pin], ps->id[pout], posvel, one, e->d, cur,
                        nxt, oob)));
         else
             LAUNCH(KID_SORTED_G2P_P2G_1,
-                   (k_g2p_p2g1<true, false><<<e->blocks_g2p, kTask, 0, st>>>(
-                       ps->P[pin], ps->P[pout], ps->id[pin], ps->id[pout], posvel, g, k, e->d, cur,
+                   (k_g2p_p2g1<BATCH, true, false><<<e->blocks_g2p, kTask, 0, st>>>(
+                       ps->P[pin], ps->P[pout], ps->id[pin], ps->id[pout], posvel, one, e->d, cur,
                        nxt, oob)));
         LAUNCH(KID_SCAN, (k_scan<<<(nbins + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(e->d, nbins)));
         LAUNCH(KID_SCATTER, (k_scatter<<<(max(n, nbins) + 255) / 256, 256, 0, st>>>(e->d, n, nbins)));
@@ -1092,20 +1287,150 @@ int sorted_step(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned lon
         ps->canonical = false;
     }
     SE_CUDA(cudaGetLastError());
+    return 0;
+}
+
+template <bool BATCH>
+int prime(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned long long* oob,
+          const Scene& one, int n, cudaStream_t st, LaunchProfiler* prof) {
+    const int nbins = e->nbins;
+    const size_t cells = (size_t)e->nbricks * 64;
+    for (int b = 0; b < 2; ++b) {
+        SE_CUDA(cudaMemsetAsync(e->d.grid[b], 0, sizeof(int4) * cells, st));
+        SE_CUDA(cudaMemsetAsync(e->d.gv[b], 0, sizeof(float4) * cells, st));
+        SE_CUDA(cudaMemsetAsync(e->d.dirty_flag[b], 0, 4 * (size_t)e->nbricks, st));
+    }
+    SE_CUDA(cudaMemsetAsync(e->d.dirty_n, 0, 8, st));
+    SE_CUDA(cudaMemsetAsync(e->d.ticket, 0, 4, st));
+    SE_CUDA(cudaMemsetAsync(e->d.task_next, 0, 4 * 3, st));
+    SE_CUDA(cudaMemsetAsync(e->d.bin_count, 0, 4 * (size_t)nbins, st));
+    const Particles& P = ps->P[ps->cur];
+    LAUNCH(KID_BIN, (k_bin<BATCH><<<(n + kTask - 1) / kTask, kTask, 0, st>>>(P, one, e->d, n)));
+    LAUNCH(KID_SCAN, (k_scan<<<(nbins + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(e->d, nbins)));
+    LAUNCH(KID_SCATTER, (k_scatter<<<(max(n, nbins) + 255) / 256, 256, 0, st>>>(e->d, n, nbins)));
+    e->cur = 0;
+    LAUNCH(KID_SORTED_P2G_1,
+           (k_g2p_p2g1<BATCH, false, false><<<e->blocks_g2p, kTask, 0, st>>>(
+               P, P, ps->id[ps->cur], ps->id[ps->cur], posvel, one, e->d, e->cur, e->cur, oob)));
+    SE_CUDA(cudaGetLastError());
+    e->primed = true;
+    return 0;
+}
+
+// Replays (capturing on first use) `substeps` substeps as one CUDA graph.
+template <bool BATCH>
+int enqueue_graph(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned long long* oob,
+                  const Scene& one, int n, int substeps, cudaStream_t st, LaunchProfiler* prof) {
+    GraphEntry* hit = nullptr;
+    for (GraphEntry& g : e->graphs)
+        if (g.substeps == substeps && g.cur0 == e->cur && g.pcur0 == ps->cur &&
+            g.posvel == posvel && g.oob == oob)
+            hit = &g;
+    if (!hit) {
+        GraphEntry ent;
+        ent.substeps = substeps;
+        ent.cur0 = e->cur;
+        ent.pcur0 = ps->cur;
+        ent.posvel = posvel;
+        ent.oob = oob;
+        const int cur0 = e->cur, last0 = e->last, pcur0 = ps->cur;
+        const bool canon0 = ps->canonical;
+        LaunchProfiler counter;  // counts the captured launches
+        cudaStream_t cs = nullptr;
+        SE_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        cudaGraph_t graph = nullptr;
+        int rc = 0;
+        cudaError_t r = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (r == cudaSuccess) {
+            rc = enqueue_substeps<BATCH>(e, ps, posvel, oob, one, n, substeps, cs, &counter);
+            r = cudaStreamEndCapture(cs, &graph);
+        }
+        if (r == cudaSuccess && rc == 0) r = cudaGraphInstantiate(&ent.exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        cudaStreamDestroy(cs);
+        ent.cur1 = e->cur;
+        ent.last1 = e->last;
+        ent.pcur1 = ps->cur;
+        e->cur = cur0;  // the capture only recorded; the replay below runs it
+        e->last = last0;
+        ps->cur = pcur0;
+        ps->canonical = canon0;
+        if (r != cudaSuccess || rc != 0) {
+            if (ent.exec) cudaGraphExecDestroy(ent.exec);
+            if (r != cudaSuccess) g_err = std::string("graph capture: ") + cudaGetErrorString(r);
+            cudaGetLastError();
+            return -1;
+        }
+        for (int i = 0; i < KID_COUNT; ++i) ent.launches[i] = counter.launches[i];
+        counter.release();
+        e->graphs.push_back(ent);
+        hit = &e->graphs.back();
+    }
+    SE_CUDA(cudaGraphLaunch(hit->exec, st));
+    for (int i = 0; i < KID_COUNT; ++i) prof->launches[i] += hit->launches[i];
+    e->cur = hit->cur1;
+    e->last = hit->last1;
+    ps->cur = hit->pcur1;
+    ps->canonical = false;
+    return 0;
+}
+
+template <bool BATCH>
+int step_impl(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned long long* oob,
+              const Scene& one, int n, int substeps, bool graph, cudaStream_t st,
+              LaunchProfiler* prof) {
+    if (!e->primed && prime<BATCH>(e, ps, posvel, oob, one, n, st, prof)) return -1;
+    const int rc = (graph && !prof->enabled)
+                       ? enqueue_graph<BATCH>(e, ps, posvel, oob, one, n, substeps, st, prof)
+                       : enqueue_substeps<BATCH>(e, ps, posvel, oob, one, n, substeps, st, prof);
+    if (rc) return rc;
     e->has_grid = true;
     return 0;
+}
+
+}  // namespace
+
+int sorted_step(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned long long* oob,
+                const SimConsts& k, int substeps, cudaStream_t st, LaunchProfiler* prof,
+                bool graph) {
+    if (!e->configured) {
+        g_err = "sorted engine is not configured for this scene";
+        return -1;
+    }
+    if (e->batch) {
+        long long n = 0;
+        for (const Scene& sc : e->scenes) n += sc.k.n;
+        if (n == 0 || substeps == 0) return 0;
+        return step_impl<true>(e, ps, posvel, oob, e->one, (int)n, substeps, graph, st, prof);
+    }
+    const int n = k.n;
+    if (n == 0 || substeps == 0) {
+        if (n == 0 && substeps > 0) e->has_grid = false;
+        return 0;
+    }
+    // A single scene's constants are kernel parameters: graphs captured with
+    // other constants are stale.
+    if (graph && memcmp(&e->one.k, &k, sizeof(SimConsts)) != 0) drop_graphs(e);
+    e->one.k = k;
+    return step_impl<false>(e, ps, posvel, oob, e->one, n, substeps, graph, st, prof);
 }
 
 int sorted_export_grid(SortedEngine* e, const SimConsts& k, int4* out, cudaStream_t st,
                        LaunchProfiler* prof) {
     (void)k;
+    return sorted_export_scene_grid(e, 0, out, st, prof);
+}
+
+int sorted_export_scene_grid(SortedEngine* e, int scene, int4* out, cudaStream_t st,
+                             LaunchProfiler* prof) {
     if (!e->configured || !e->has_grid) {
         g_err = "no sorted-engine grid to export";
         return -1;
     }
-    const Geo& g = e->geo;
-    LAUNCH(KID_EXPORT,
-           (k_export<<<(g.grid_count + 255) / 256, 256, 0, st>>>(e->d.grid[e->last], g, out)));
+    const Scene& sc = e->batch ? e->scenes.at((size_t)scene) : e->one;
+    const Geo& g = sc.g;
+    const int4* grid = e->d.grid[e->last] + (size_t)(e->batch ? sc.bbase : 0) * 64;
+    LAUNCH(KID_EXPORT, (k_export<<<(g.grid_count + 255) / 256, 256, 0, st>>>(grid, g, out)));
     SE_CUDA(cudaGetLastError());
     return 0;
 }

@@ -80,6 +80,10 @@ struct SimConsts {
     int Y, Z;              // i32(init_box.y), i32(init_box.z)
     int grid_count;
     int n;
+    // Body force per unit time added in updateGrid.  The reference adds
+    // -0.3*dt to vy only (updateGrid.wgsl:34); components that are 0 are not
+    // touched, so (0, -0.3, 0) reproduces it exactly.
+    float gravity[3];
 };
 
 // Particle state in HBM: four float4 streams (SoA, 64 B per particle).
@@ -308,9 +312,9 @@ __device__ __forceinline__ int4 update_cell_xyz(int4 c, int x, int y, int z, con
     const float fv0 = fdiv(dec(c.x, k.fm), m);
     const float fv1 = fdiv(dec(c.y, k.fm), m);
     const float fv2 = fdiv(dec(c.z, k.fm), m);
-    int o0 = enc(fv0, k.fm);
-    int o1 = enc(fadd(fv1, fmul(-0.3f, k.dt)), k.fm);
-    int o2 = enc(fv2, k.fm);
+    int o0 = enc(k.gravity[0] != 0.0f ? fadd(fv0, fmul(k.gravity[0], k.dt)) : fv0, k.fm);
+    int o1 = enc(k.gravity[1] != 0.0f ? fadd(fv1, fmul(k.gravity[1], k.dt)) : fv1, k.fm);
+    int o2 = enc(k.gravity[2] != 0.0f ? fadd(fv2, fmul(k.gravity[2], k.dt)) : fv2, k.fm);
     if (x < 2 || x > hx) o0 = 0;
     if (y < 2 || y > hy) o1 = 0;
     if (z < 2 || z > hz) o2 = 0;

@@ -17,15 +17,28 @@ void sorted_destroy(SortedEngine* e);
 // must use the dispatch engine.
 int sorted_configure(SortedEngine* e, const SimConsts& k);
 
+// Sizes the engine for a batch of independent scenes (ks[s].n particles of
+// scene s, stored after those of scenes 0..s-1).  Returns -1 when a box is
+// degenerate or the batch exceeds max_particles.
+int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes);
+
+// Batch: replaces scene s's constants (real box, stiffness, gravity, ...);
+// its geometry and particle count must stay.  Stream-ordered.
+int sorted_set_scene_consts(SortedEngine* e, int scene, const SimConsts& k, cudaStream_t st);
+
 // Forgets the carried-over state (the next step re-bins and redoes p2g_1).
 void sorted_invalidate(SortedEngine* e);
 
-// Enqueues `substeps` substeps.  posvel is written by the last one.
 // Enqueues `substeps` substeps on ps->P[ps->cur]; each substep writes the
 // particles, in bin order, to the other buffer and flips ps->cur.  posvel is
-// written (in particle-id order) by the last substep.
+// written (in particle-id order) by the last substep.  k is the scene's
+// constants (ignored for a batch, which uses its table).  With `graph` the
+// substeps run as one CUDA graph, captured on first use for this substep
+// count and engine state and replayed afterwards (not while prof times
+// launches).
 int sorted_step(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned long long* oob,
-                const SimConsts& k, int substeps, cudaStream_t st, LaunchProfiler* prof);
+                const SimConsts& k, int substeps, cudaStream_t st, LaunchProfiler* prof,
+                bool graph = false);
 
 // True once a substep has run since configure/invalidate.
 bool sorted_has_grid(const SortedEngine* e);
@@ -34,6 +47,10 @@ bool sorted_has_grid(const SortedEngine* e);
 // x-major layout (grid_count int4 cells) to device memory `out`.
 int sorted_export_grid(SortedEngine* e, const SimConsts& k, int4* out, cudaStream_t st,
                        LaunchProfiler* prof);
+
+// The same for scene `scene` of a batch.
+int sorted_export_scene_grid(SortedEngine* e, int scene, int4* out, cudaStream_t st,
+                             LaunchProfiler* prof);
 
 const char* sorted_error();
 

@@ -202,6 +202,15 @@ class MLSMPMSimulator:
     def posvelDevicePtr(self) -> int:
         return int(self._lib.mpm_posvel_device_ptr(self._handle) or 0)
 
+    def setGravity(self, gravity) -> None:
+        """Body force per unit time (default (0, -0.3, 0), updateGrid.wgsl:34)."""
+        g = (ctypes.c_float * 3)(*[float(x) for x in gravity])
+        _check(self._lib.mpm_set_gravity(self._handle, g), "setGravity")
+
+    def setGraph(self, enable: bool) -> None:
+        """Run execute()'s substeps as one CUDA graph (sorted engine)."""
+        _check(self._lib.mpm_set_graph(self._handle, int(bool(enable))), "setGraph")
+
     def checkHealth(self) -> dict:
         h = L.Health()
         code = self._lib.mpm_check_health(self._handle, ctypes.byref(h))
@@ -283,3 +292,167 @@ def probe_packed(a: np.ndarray, b: np.ndarray):
     _check(L.load().mpm_probe_packed(a.ctypes.data_as(fptr), b.ctypes.data_as(fptr), n,
                                      out.ctypes.data_as(fptr)))
     return tuple(out[i * n:(i + 1) * n] for i in range(6))
+
+
+# ---------------------------------------------------------------------------
+# Batches of independent scenes
+# ---------------------------------------------------------------------------
+
+def scene_desc(num_particles: int, init_box, real_box=None, *, stiffness: float = 3.0,
+               rest_density: float = 4.0, dynamic_viscosity: float = 0.1, dt: float = 0.2,
+               fixed_point_multiplier: float = 1e7, gravity=(0.0, -0.3, 0.0)) -> L.SceneDesc:
+    """One scene of a batch; the defaults are mls-mpm/mls-mpm.ts:53-59."""
+    d = L.SceneDesc()
+    d.num_particles = int(num_particles)
+    real_box = init_box if real_box is None else real_box
+    for a in range(3):
+        d.init_box[a] = float(init_box[a])
+        d.real_box[a] = float(real_box[a])
+        d.gravity[a] = float(gravity[a])
+    d.stiffness = stiffness
+    d.rest_density = rest_density
+    d.dynamic_viscosity = dynamic_viscosity
+    d.dt = dt
+    d.fixed_point_multiplier = fixed_point_multiplier
+    return d
+
+
+def batch_scenes(num_scenes: int = 256, seed: int = 0, n_range=(4000, 64000), sides=(32, 48, 64),
+                 spacing: float = 0.5, jitter: float = 0.05, stiffness_range=(2.0, 4.0),
+                 gravity_magnitude: float = 0.3):
+    """Independent dam-break-like scenes of uneven sizes (numpy PCG64(seed)).
+
+    Per scene: n uniform in n_range; a cubic grid whose side is drawn from
+    `sides`; the first n points (x-major) of a jittered cubic lattice with
+    ceil(cbrt(n)) points per axis, spacing `spacing`, placed at a uniform
+    origin with the block inside the walls [3, side - 4]; gravity a uniform
+    random direction times `gravity_magnitude`; stiffness uniform in
+    stiffness_range; the other constants are the reference's.
+    Returns (list of SceneDesc, (sum n, 20) float32 records).
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    descs, recs = [], []
+    for _ in range(num_scenes):
+        n = int(rng.integers(n_range[0], n_range[1] + 1))
+        side = int(sides[int(rng.integers(0, len(sides)))])
+        a = 1
+        while a * a * a < n:
+            a += 1
+        extent = (a - 1) * spacing + 2 * jitter
+        lo, hi = 3.0 + jitter, side - 4.0 - extent
+        origin = lo + rng.random(3) * max(hi - lo, 0.0)
+        idx = np.arange(n)
+        lat = np.stack([idx // (a * a), (idx // a) % a, idx % a], axis=1).astype(np.float64)
+        pos = origin + spacing * lat + jitter * (2.0 * rng.random((n, 3)) - 1.0)
+        g = rng.normal(size=3)
+        g = gravity_magnitude * g / np.linalg.norm(g)
+        k = float(rng.uniform(*stiffness_range))
+        r = np.zeros((n, 20), dtype=np.float32)
+        r[:, 0:3] = pos.astype(np.float32)
+        descs.append(scene_desc(n, (side, side, side), stiffness=k, gravity=tuple(np.float32(g))))
+        recs.append(r)
+    return descs, np.concatenate(recs) if recs else np.zeros((0, 20), np.float32)
+
+
+class MLSMPMBatch:
+    """Many independent scenes advanced together: one launch per stage for
+    all scenes, replayed as a CUDA graph.  Scene s behaves exactly like an
+    MLSMPMSimulator holding it alone with the same constants."""
+
+    def __init__(self, scenes, particles: np.ndarray, device=None, graph: bool = True):
+        self._lib = L.load()
+        self._device = device
+        descs = list(scenes)
+        self._descs = descs
+        arr = (L.SceneDesc * len(descs))(*descs)
+        recs = np.ascontiguousarray(particles, dtype=np.float32).reshape(-1, 20)
+        counts = np.array([d.num_particles for d in descs], dtype=np.int64)
+        if recs.shape[0] != int(counts.sum()):
+            raise ValueError("particle array does not match the scenes' particle counts")
+        self.sceneOffsets = np.concatenate([[0], np.cumsum(counts)])
+        self._handle = ctypes.c_void_p()
+        with self._on_device():
+            _check(self._lib.mpm_batch_create(arr, len(descs),
+                                              recs.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                              ctypes.byref(self._handle)), "MLSMPMBatch")
+        self.setGraph(graph)
+
+    def _on_device(self):
+        if self._device is None:
+            import contextlib
+            return contextlib.nullcontext()
+        import torch
+        return torch.cuda.device(self._device)
+
+    @property
+    def numScenes(self) -> int:
+        return int(self._lib.mpm_batch_num_scenes(self._handle))
+
+    @property
+    def numParticles(self) -> int:
+        return int(self._lib.mpm_batch_num_particles(self._handle))
+
+    def gridCount(self, scene: int) -> int:
+        d = self._descs[scene]
+        return int(np.prod([np.ceil(np.float64(d.init_box[a])) for a in range(3)]))
+
+    def step(self, substeps: int = 2, commandEncoder=None) -> None:
+        _check(self._lib.mpm_batch_step(self._handle, int(substeps),
+                                        _stream_handle(commandEncoder)), "step")
+
+    def execute(self, commandEncoder=None) -> None:
+        """Two substeps of every scene (mls-mpm/mls-mpm.ts:245-268)."""
+        self.step(2, commandEncoder)
+
+    def setScene(self, scene: int, desc: L.SceneDesc) -> None:
+        _check(self._lib.mpm_batch_set_scene(self._handle, int(scene), ctypes.byref(desc)),
+               "setScene")
+        self._descs[scene] = desc
+
+    def changeBoxSize(self, scene: int, realBoxSize) -> None:
+        d = L.SceneDesc.from_buffer_copy(self._descs[scene])
+        for a in range(3):
+            d.real_box[a] = float(realBoxSize[a])
+        self.setScene(scene, d)
+
+    def setGraph(self, enable: bool) -> None:
+        _check(self._lib.mpm_batch_set_graph(self._handle, int(bool(enable))), "setGraph")
+
+    def downloadParticles(self) -> np.ndarray:
+        out = np.zeros((self.numParticles, 20), dtype=np.float32)
+        _check(self._lib.mpm_batch_download_particles(
+            self._handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))), "downloadParticles")
+        return out
+
+    def downloadGrid(self, scene: int) -> np.ndarray:
+        out = np.zeros((self.gridCount(scene), 4), dtype=np.int32)
+        _check(self._lib.mpm_batch_download_grid(
+            self._handle, int(scene), out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))),
+            "downloadGrid")
+        return out
+
+    def posvelDevicePtr(self) -> int:
+        return int(self._lib.mpm_batch_posvel_device_ptr(self._handle) or 0)
+
+    def checkHealth(self) -> dict:
+        h = L.Health()
+        code = self._lib.mpm_batch_check_health(self._handle, ctypes.byref(h))
+        if code not in (L.MPM_OK, L.MPM_E_NONFINITE):
+            _check(code, "checkHealth")
+        return {"nonfinite_particles": int(h.nonfinite_particles),
+                "out_of_range_accesses": int(h.out_of_range_accesses),
+                "ok": code == L.MPM_OK}
+
+    def launchCount(self) -> int:
+        return int(self._lib.mpm_batch_launch_count(self._handle))
+
+    def close(self) -> None:
+        if self._handle:
+            self._lib.mpm_batch_destroy(self._handle)
+            self._handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
