@@ -212,6 +212,105 @@ def algorithmic_bytes(kernel: str, n: int, cells: int) -> float | None:
     return None
 
 
+BATCH_SCENES, BATCH_SUBSTEPS, BATCH_SEED = 256, 100, 20240601
+BATCH_WORKLOAD = ("256 independent scenes, particles uniform in [4000, 64000], cubic grids of "
+                  "side 32/48/64, lattice blocks at uniform origins, random gravity direction "
+                  "x0.3, stiffness uniform [2, 4]; 100 substeps per rollout")
+
+
+def measure_batched(pkg, torch, stream, repeats: int = 3) -> dict:
+    """Scene-substeps/s of one batch (one launch per stage for all scenes,
+    CUDA graph) against looping single-scene simulators over the same scenes."""
+    import numpy as np
+    descs, recs = pkg.batch_scenes(BATCH_SCENES, seed=BATCH_SEED)
+    S, K = len(descs), BATCH_SUBSTEPS
+    batch = pkg.MLSMPMBatch(descs, recs, graph=True)
+    batch.step(K, stream)  # captures the graph and warms up
+    stream.synchronize()
+    l0 = batch.launchCount()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(repeats)]
+    for a, b in evs:
+        a.record(stream)
+        batch.step(K, stream)
+        b.record(stream)
+    torch.cuda.synchronize()
+    batch_ms = min(a.elapsed_time(b) for a, b in evs)
+    batch_launches = (batch.launchCount() - l0) // repeats
+
+    offs = np.concatenate([[0], np.cumsum([d.num_particles for d in descs])])
+    sims = []
+    for s, d in enumerate(descs):
+        prm = pkg._lib.Params(d.stiffness, d.rest_density, d.dynamic_viscosity, d.dt,
+                              d.fixed_point_multiplier)
+        side = int(d.init_box[0])
+        sim = pkg.MLSMPMSimulator(None, None, 1.2, maxParticles=d.num_particles,
+                                  maxGrid=(side, side, side), params=prm)
+        sim.setGravity(list(d.gravity))
+        sim.upload(recs[offs[s]:offs[s + 1]], list(d.init_box))
+        sims.append(sim)
+
+    def loop_ms(graph: bool) -> float:
+        for sim in sims:
+            sim.setGraph(graph)
+            sim.execute(stream, substeps=K)  # warm-up (and capture)
+        stream.synchronize()
+        best = None
+        for _ in range(repeats):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for sim in sims:
+                sim.execute(stream, substeps=K)
+            b.record(stream)
+            torch.cuda.synchronize()
+            t = a.elapsed_time(b)
+            best = t if best is None else min(best, t)
+        return best
+
+    plain_ms = loop_ms(False)
+    graph_ms = loop_ms(True)
+    for sim in sims:
+        sim.close()
+    batch.close()
+    # parity: the first four scenes as a fresh batch vs fresh single-scene
+    # simulators, one rollout each
+    fresh = pkg.MLSMPMBatch(descs[:4], recs[:offs[4]], graph=True)
+    fresh.step(K, stream)
+    stream.synchronize()
+    got = fresh.downloadParticles()
+    fresh.close()
+    exact = True
+    for s in range(4):
+        d = descs[s]
+        prm = pkg._lib.Params(d.stiffness, d.rest_density, d.dynamic_viscosity, d.dt,
+                              d.fixed_point_multiplier)
+        side = int(d.init_box[0])
+        sim = pkg.MLSMPMSimulator(None, None, 1.2, maxParticles=d.num_particles,
+                                  maxGrid=(side, side, side), params=prm)
+        sim.setGravity(list(d.gravity))
+        sim.upload(recs[offs[s]:offs[s + 1]], list(d.init_box))
+        sim.execute(stream, substeps=K)
+        exact &= bool(np.array_equal(got[offs[s]:offs[s + 1]].view(np.uint32),
+                                     sim.downloadParticles().view(np.uint32)))
+        sim.close()
+    total = int(offs[-1])
+    return {
+        "workload": BATCH_WORKLOAD, "scenes": S, "particles": total, "substeps": K,
+        "seed": BATCH_SEED,
+        "scene_substeps_per_s": S * K / (batch_ms / 1e3),
+        "particle_substeps_per_s": total * K / (batch_ms / 1e3),
+        "ms_per_rollout": batch_ms,
+        "gpu_launches_per_rollout": batch_launches,
+        "loop_plain_scene_substeps_per_s": S * K / (plain_ms / 1e3),
+        "loop_graph_scene_substeps_per_s": S * K / (graph_ms / 1e3),
+        "speedup_vs_loop_plain": plain_ms / batch_ms,
+        "speedup_vs_loop_graph": graph_ms / batch_ms,
+        "bit_exact_vs_single_scene": bool(exact),
+        "timing": f"CUDA events around each {K}-substep rollout, best of {repeats}; "
+                  "loop = MLSMPMSimulator.execute(substeps=100) per scene, back to back",
+    }
+
+
 def run_ours(args) -> None:
     import numpy as np
     import torch
@@ -338,6 +437,8 @@ def run_ours(args) -> None:
     assert np.isfinite(host_out[:, 0:3]).all(), "posvel read back non-finite positions"
     sim.close()
 
+    batched = None if args.skip_batched else measure_batched(pkg, torch, stream)
+
     # --- bit-exactness self-check: sorted engine vs dispatch engine -------
     outs = []
     for engine in ("sorted", "dispatch"):
@@ -384,6 +485,7 @@ def run_ours(args) -> None:
         "gpu_launches": launches,
         "wall_s_timed_region": wall,
         "kernels": kernels,
+        "batched": batched,
         "parity": {"grid_bit_exact_vs_dispatch_engine": grid_exact,
                    "particles_bit_exact_vs_dispatch_engine": parts_exact, "steps": 3},
     }
@@ -399,6 +501,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-batched", action="store_true",
+                    help="leave out the batched-scenes measurement")
     ap.add_argument("--quick", action="store_true",
                     help="time the device-resident steps only (for profiler captures)")
     args = ap.parse_args()
