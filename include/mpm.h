@@ -243,6 +243,46 @@ void* mpm_batch_posvel_device_ptr(mpm_batch* batch);
 int mpm_batch_check_health(mpm_batch* batch, mpm_health* out);
 int64_t mpm_batch_launch_count(const mpm_batch* batch);
 
+/* Differentiation: a forward / backward pair over a batch of scenes (one
+ * scene for a single simulation).  The derivative is that of the continuous
+ * model the fixed-point solver discretises (enc/dec taken as the identity),
+ * evaluated along the solver's own trajectory.  mpm_forward_ckpt runs the
+ * solver and keeps the state every `checkpoint_every` substeps; mpm_backward
+ * recomputes each segment from its checkpoint (states and updated grids of
+ * every substep) and runs the adjoint substeps in reverse. */
+typedef struct mpm_adjoint mpm_adjoint;
+
+/* Tapes (the trajectory the derivative is evaluated along):
+ *   MPM_TAPE_FP64        the continuous model integrated in FP64 on the GPU
+ *                        (double grid sums, no fixed point): its trajectory
+ *                        tracks an FP64 reference over hundreds of substeps,
+ *                        so gradients match FP64 finite differences (default)
+ *   MPM_TAPE_FIXED_POINT the solver's own bit-exact fixed-point trajectory
+ *                        (sorted engine); over long horizons it drifts from
+ *                        the continuous model by the i32 truncation bias */
+enum { MPM_TAPE_FIXED_POINT = 0, MPM_TAPE_FP64 = 1 };
+
+int mpm_adjoint_create(const mpm_scene_desc* scenes, int num_scenes, int max_substeps,
+                       int checkpoint_every, mpm_adjoint** out);
+int mpm_adjoint_destroy(mpm_adjoint* adj);
+/* Selects the tape (invalidates the forward). */
+int mpm_adjoint_set_tape(mpm_adjoint* adj, int tape);
+/* New constants for scene s (e.g. stiffness, viscosity between optimizer
+ * steps); box sizes and num_particles must stay.  Invalidates the forward. */
+int mpm_adjoint_set_scene(mpm_adjoint* adj, int scene, const mpm_scene_desc* desc);
+/* Runs `substeps` substeps from init_aos80 (all scenes' 80-byte records). */
+int mpm_forward_ckpt(mpm_adjoint* adj, const float* init_aos80, int substeps, void* stream);
+/* The state after `substep` substeps of the last forward; substep must be a
+ * multiple of checkpoint_every or the final substep (synchronizes). */
+int mpm_adjoint_state(mpm_adjoint* adj, int substep, float* out_aos80);
+/* seeds_aos80: num_seeds blocks of 80-byte records, block j = dL/d(state
+ * after seed_substeps[j] substeps) (fields as in the particle record: position,
+ * velocity, C).  Writes dL/d(initial state) to grad_init_aos80 and, per scene,
+ * (dL/d stiffness, dL/d dynamic_viscosity) to grad_params[2 * s + 0/1]
+ * (synchronizes). */
+int mpm_backward(mpm_adjoint* adj, const float* seeds_aos80, const int* seed_substeps,
+                 int num_seeds, float* grad_init_aos80, double* grad_params, void* stream);
+
 /*
  * No counterpart in the reference.  The watchdog scan of mpm_check_health
  * over a caller-owned device buffer, allocating nothing: for callers that

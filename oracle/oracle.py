@@ -1,4 +1,5 @@
-"""ctypes front end of the C oracle (oracle/mpm_oracle.c).
+"""ctypes front end of the C oracle (oracle/mpm_oracle.c, and the FP64
+continuous restatement oracle/mpm_oracle64.c used for finite differences).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
 bench.py (cpu_baseline leg and `--impl reference`) as the checker or the
@@ -19,7 +20,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "build")
 LIB_PATH = os.path.join(BUILD_DIR, "libmpm_oracle.so")
-SOURCES = [os.path.join(HERE, "mpm_oracle.c")]
+SOURCES = [os.path.join(HERE, "mpm_oracle.c"), os.path.join(HERE, "mpm_oracle64.c")]
 
 # -ffp-contract=off: every float op rounds separately, as the WGSL restatement
 # requires; no -ffast-math (keeps IEEE division, NaN and denormal semantics).
@@ -178,3 +179,59 @@ def enc(f: float, fm: float = 1e7) -> int:
 
 def dec(i: int, fm: float = 1e7) -> float:
     return float(lib().orc_dec(i, fm))
+
+
+# ---------------------------------------------------------------------------
+# FP64 continuous model (mpm_oracle64.c): the function the adjoint
+# differentiates, for central finite differences.
+# ---------------------------------------------------------------------------
+
+class Params64(ctypes.Structure):
+    _fields_ = [
+        ("stiffness", ctypes.c_double),
+        ("rest_density", ctypes.c_double),
+        ("dynamic_viscosity", ctypes.c_double),
+        ("dt", ctypes.c_double),
+        ("gravity", ctypes.c_double * 3),
+        ("init_box", ctypes.c_double * 3),
+        ("real_box", ctypes.c_double * 3),
+    ]
+
+    @classmethod
+    def make(cls, init_box, real_box=None, stiffness=3.0, rest_density=4.0,
+             dynamic_viscosity=0.1, dt=0.2, gravity=(0.0, -0.3, 0.0)) -> "Params64":
+        """Constants as f32 values widened to double (the f32 solver's)."""
+        f = lambda v: float(np.float32(v))
+        p = cls(f(stiffness), f(rest_density), f(dynamic_viscosity), f(dt))
+        real_box = init_box if real_box is None else real_box
+        for a in range(3):
+            p.gravity[a] = f(gravity[a])
+            p.init_box[a] = f(init_box[a])
+            p.real_box[a] = f(real_box[a])
+        return p
+
+
+def records_to_state64(recs: np.ndarray) -> np.ndarray:
+    """(n, 20) float32 particle records -> (n, 15) float64 state
+    (x, v, C by columns)."""
+    r = np.asarray(recs, dtype=np.float32).reshape(-1, 20).astype(np.float64)
+    out = np.empty((len(r), 15), dtype=np.float64)
+    out[:, 0:3] = r[:, 0:3]
+    out[:, 3:6] = r[:, 4:7]
+    for c in range(3):
+        out[:, 6 + 3 * c:9 + 3 * c] = r[:, 8 + 4 * c:11 + 4 * c]
+    return out
+
+
+def run64(state: np.ndarray, params: Params64, substeps: int) -> np.ndarray:
+    """Returns the state after `substeps` substeps of the FP64 model."""
+    L = lib()
+    if not getattr(L, "_orc64_ready", False):
+        L.orc64_run.argtypes = [np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS"),
+                                ctypes.c_int64, ctypes.POINTER(Params64), ctypes.c_int]
+        L.orc64_run.restype = ctypes.c_int64
+        L._orc64_ready = True
+    st = np.ascontiguousarray(state, dtype=np.float64).copy()
+    if L.orc64_run(st, len(st), ctypes.byref(params), int(substeps)) < 0:
+        raise MemoryError("orc64_run")
+    return st

@@ -201,3 +201,21 @@ def test_grid_is_permutation_invariant(oracle_mod, seed):
     b.execute(2)
     assert_bits_equal(a.cells, b.cells, "grid")
     assert_bits_equal(a.particles[perm], b.particles, "particles")
+
+
+def test_fp64_model_tracks_the_fixed_point_oracle(oracle_mod):
+    """The FP64 continuous restatement (finite-difference reference of the
+    derivative path) stays within the fixed-point quantisation of the f32
+    oracle over 20 substeps."""
+    from oracle import scene
+    recs = scene.lattice(12, 9.0, 0.5, 0.05, 3)
+    box = [32.0, 32.0, 32.0]
+    ref = oracle_mod.OracleSim(recs, box)
+    ref.execute(20, 2)
+    st = oracle_mod.run64(oracle_mod.records_to_state64(recs), oracle_mod.Params64.make(box), 20)
+    assert np.abs(ref.particles[:, 0:3] - st[:, 0:3]).max() < 5e-4
+    assert np.abs(ref.particles[:, 4:7] - st[:, 3:6]).max() < 5e-4
+    # gravity vector and stiffness reach the FP64 model
+    st2 = oracle_mod.run64(oracle_mod.records_to_state64(recs),
+                           oracle_mod.Params64.make(box, gravity=(0.3, 0.0, 0.0)), 5)
+    assert st2[:, 3].mean() > 0.0 > st[:, 4].mean()

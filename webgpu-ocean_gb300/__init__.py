@@ -7,10 +7,10 @@ The directory name is not a Python identifier; load it with
 `webgpu_ocean_gb300`.
 """
 from . import _lib, build
-from .mlsmpm import (MLSMPMBatch, MLSMPMSimulator, MPMError, GridCapacityError, batch_scenes,
-                     default_params, probe_conversions, probe_packed, scene_dambreak,
-                     scene_desc, scene_lattice)
+from .mlsmpm import (MLSMPMAdjoint, MLSMPMBatch, MLSMPMSimulator, MPMError, GridCapacityError,
+                     batch_scenes, centroid_loss, default_params, probe_conversions, probe_packed,
+                     scene_dambreak, scene_desc, scene_lattice)
 
-__all__ = ["MLSMPMSimulator", "MLSMPMBatch", "MPMError", "GridCapacityError", "default_params",
+__all__ = ["MLSMPMSimulator", "MLSMPMBatch", "MLSMPMAdjoint", "centroid_loss", "MPMError", "GridCapacityError", "default_params",
            "scene_dambreak", "scene_lattice", "scene_desc", "batch_scenes", "probe_conversions",
            "probe_packed", "build", "_lib"]

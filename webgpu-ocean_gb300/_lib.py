@@ -26,6 +26,9 @@ MPM_E_NONFINITE = -7
 MPM_ENGINE_SORTED = 0
 MPM_ENGINE_DISPATCH = 1
 
+MPM_TAPE_FIXED_POINT = 0
+MPM_TAPE_FP64 = 1
+
 KERNELS = {
     "clearGrid": 0,
     "p2g_1": 1,
@@ -140,6 +143,13 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "mpm_batch_posvel_device_ptr": (vp, [vp]),
         "mpm_batch_check_health": (i32, [vp, ctypes.POINTER(Health)]),
         "mpm_batch_launch_count": (i64, [vp]),
+        "mpm_adjoint_create": (i32, [ctypes.POINTER(SceneDesc), i32, i32, i32, ctypes.POINTER(vp)]),
+        "mpm_adjoint_destroy": (i32, [vp]),
+        "mpm_adjoint_set_tape": (i32, [vp, i32]),
+        "mpm_adjoint_set_scene": (i32, [vp, i32, ctypes.POINTER(SceneDesc)]),
+        "mpm_forward_ckpt": (i32, [vp, fp, i32, vp]),
+        "mpm_adjoint_state": (i32, [vp, i32, fp]),
+        "mpm_backward": (i32, [vp, fp, ip, i32, fp, dp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

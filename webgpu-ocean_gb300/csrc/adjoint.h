@@ -1,0 +1,46 @@
+// adjoint.h -- reverse-mode substep kernels (adjoint.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "mpm_internal.h"
+
+namespace mpm {
+
+// Doubles per particle record of the FP64 tape: x[0..2], v[3..5], C[6..14]
+// (C[c][r] at 6 + 3c + r), padding [15].
+constexpr int kRec64 = 16;
+
+// One scene of an adjoint batch: its constants and the first cell of its
+// grid in the linear (reference-layout) concatenation of all scenes' grids.
+struct AdjScene {
+    SimConsts k;
+    int lbase;
+    int pad[3];
+};
+
+// One substep backward.  S: the substep's input state (particle order of the
+// batch); G: its grid after updateGrid, reference layout, all scenes
+// concatenated (ncells cells); Aout: adjoint of the substep's output state;
+// Anew: receives the adjoint of S; gadj: ncells float4 of scratch; pgrad:
+// per-scene (stiffness, dynamic_viscosity) adjoints, accumulated.
+void launch_adjoint_substep(const Particles& S, const int4* G, const Particles& Aout,
+                            const Particles& Anew, float4* gadj, const AdjScene* scenes,
+                            int nscenes, const int* pscene, int n, int ncells, double* pgrad,
+                            cudaStream_t st);
+
+// The same on the FP64 tape (S: kRec64 doubles per particle; G: double4
+// cells {v or momentum, mass}).
+void launch_adjoint_substep64(const double* S, const double4* G, const Particles& Aout,
+                              const Particles& Anew, float4* gadj, const AdjScene* scenes,
+                              int nscenes, const int* pscene, int n, int ncells, double* pgrad,
+                              cudaStream_t st);
+
+// One FP64 substep of the continuous model: S -> Sout, leaving the updated
+// grid in G (ncells double4, all scenes).
+void launch_substep64(const double* S, double4* G, double* Sout, const AdjScene* scenes,
+                      int nscenes, const int* pscene, int n, int ncells, cudaStream_t st);
+
+// A += B, record-wise over n particles.
+void launch_particles_axpy(const Particles& A, const Particles& B, int n, cudaStream_t st);
+
+}  // namespace mpm

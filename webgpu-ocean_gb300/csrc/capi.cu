@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/mpm.h"
+#include "adjoint.h"
 #include "mpm_internal.h"
 #include "sorted_engine.h"
 
@@ -930,6 +931,470 @@ int64_t mpm_batch_launch_count(const mpm_batch* b) {
     long long t = 0;
     for (int id = 0; id < KID_COUNT; ++id) t += b->prof.launches[id];
     return t;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Differentiation (forward with checkpoints, backward with recompute)
+// ---------------------------------------------------------------------------
+
+struct mpm_adjoint {
+    mpm_batch* b = nullptr;
+    int max_substeps = 0;
+    int every = 1;
+    int tape = MPM_TAPE_FP64;
+    int T = -1;                      // substeps of the last forward; -1: none
+    int nck = 0;                     // checkpoint slots
+    // fixed-point tape
+    std::vector<Particles> ckpt;     // states after 0, every, 2*every, ..., T substeps
+    std::vector<Particles> seg;      // states inside a segment (seg[0] unused)
+    int4* gtape = nullptr;           // every x ncells: updated grids of a segment
+    // FP64 tape
+    std::vector<double*> ckpt64;
+    std::vector<double*> seg64;
+    double* scratch64[2] = {nullptr, nullptr};
+    double4* gtape64 = nullptr;
+    // adjoint state
+    Particles adj[2]{};
+    float4* gadj = nullptr;
+    AdjScene* scenes_d = nullptr;
+    int* pscene_d = nullptr;
+    double* pgrad_d = nullptr;
+    int ncells = 0;
+    std::vector<int> lbase;
+};
+
+namespace {
+
+cudaError_t alloc_particles(Particles& P, size_t n) {
+    P = Particles{};
+    float4** pp[4] = {&P.p0, &P.p1, &P.p2, &P.p3};
+    for (int q = 0; q < 4; ++q) {
+        const cudaError_t e = cudaMalloc(pp[q], sizeof(float4) * (n ? n : 1));
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+void free_particles(Particles& P) {
+    cudaFree(P.p0);
+    cudaFree(P.p1);
+    cudaFree(P.p2);
+    cudaFree(P.p3);
+    P = Particles{};
+}
+
+cudaError_t copy_particles(const Particles& dst, const Particles& src, int n, cudaStream_t st) {
+    const float4* s[4] = {src.p0, src.p1, src.p2, src.p3};
+    float4* d[4] = {dst.p0, dst.p1, dst.p2, dst.p3};
+    for (int q = 0; q < 4; ++q) {
+        const cudaError_t e = cudaMemcpyAsync(d[q], s[q], sizeof(float4) * (size_t)n,
+                                              cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t upload_aos80(const Particles& dst, const float* aos80, int n) {
+    std::vector<float4> q[4];
+    aos80_to_soa(aos80, n, q);
+    float4* d[4] = {dst.p0, dst.p1, dst.p2, dst.p3};
+    for (int k = 0; k < 4; ++k) {
+        if (!n) break;
+        const cudaError_t e =
+            cudaMemcpy(d[k], q[k].data(), sizeof(float4) * (size_t)n, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t download_aos80(const Particles& src, int n, float* aos80) {
+    std::vector<float4> q[4];
+    const float4* s[4] = {src.p0, src.p1, src.p2, src.p3};
+    for (int k = 0; k < 4; ++k) {
+        q[k].resize((size_t)n);
+        if (!n) continue;
+        const cudaError_t e =
+            cudaMemcpy(q[k].data(), s[k], sizeof(float4) * (size_t)n, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return e;
+    }
+    soa_to_aos80(q, n, aos80);
+    return cudaSuccess;
+}
+
+// 80-byte records <-> FP64 tape records (kRec64 doubles).
+cudaError_t upload_aos80_64(double* dst, const float* aos80, int n) {
+    std::vector<double> h((size_t)kRec64 * (size_t)(n > 0 ? n : 1), 0.0);
+    for (int i = 0; i < n; ++i) {
+        const float* P = aos80 + 20 * (size_t)i;
+        double* q = h.data() + (size_t)kRec64 * i;
+        for (int a = 0; a < 3; ++a) {
+            q[a] = P[a];
+            q[3 + a] = P[4 + a];
+        }
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < 3; ++r) q[6 + 3 * c + r] = P[8 + 4 * c + r];
+    }
+    if (!n) return cudaSuccess;
+    return cudaMemcpy(dst, h.data(), sizeof(double) * kRec64 * (size_t)n, cudaMemcpyHostToDevice);
+}
+
+cudaError_t download_aos80_64(const double* src, int n, float* aos80) {
+    std::vector<double> h((size_t)kRec64 * (size_t)(n > 0 ? n : 1));
+    if (n) {
+        const cudaError_t e = cudaMemcpy(h.data(), src, sizeof(double) * kRec64 * (size_t)n,
+                                         cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return e;
+    }
+    for (int i = 0; i < n; ++i) {
+        float* P = aos80 + 20 * (size_t)i;
+        const double* q = h.data() + (size_t)kRec64 * i;
+        std::memset(P, 0, 80);
+        for (int a = 0; a < 3; ++a) {
+            P[a] = (float)q[a];
+            P[4 + a] = (float)q[3 + a];
+        }
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < 3; ++r) P[8 + 4 * c + r] = (float)q[6 + 3 * c + r];
+    }
+    return cudaSuccess;
+}
+
+// Puts a canonical state into the batch's particle store and forgets the
+// sorted engine's carried state.
+cudaError_t batch_load_device(mpm_batch* b, const Particles& src, cudaStream_t st) {
+    b->ps.cur = 0;
+    b->ps.canonical = true;
+    cudaError_t e = copy_particles(b->ps.P[0], src, b->n, st);
+    if (e != cudaSuccess) return e;
+    launch_iota(b->ps.id[0], b->n, st);
+    sorted_invalidate(b->sorted);
+    b->stepped = false;
+    return cudaGetLastError();
+}
+
+// The batch's current state, in particle order, into dst.
+void batch_canonical_to(mpm_batch* b, const Particles& dst, cudaStream_t st) {
+    const int c = b->ps.cur;
+    if (b->ps.canonical) {
+        copy_particles(dst, b->ps.P[c], b->n, st);
+        return;
+    }
+    launch_canonicalize(b->ps.P[c], b->ps.id[c], dst, nullptr, b->n, st);
+}
+
+void free_tapes(mpm_adjoint* a) {
+    for (Particles& P : a->ckpt) free_particles(P);
+    for (Particles& P : a->seg) free_particles(P);
+    a->ckpt.clear();
+    a->seg.clear();
+    cudaFree(a->gtape);
+    a->gtape = nullptr;
+    for (double* p : a->ckpt64) cudaFree(p);
+    for (double* p : a->seg64) cudaFree(p);
+    a->ckpt64.clear();
+    a->seg64.clear();
+    for (double*& p : a->scratch64) {
+        cudaFree(p);
+        p = nullptr;
+    }
+    cudaFree(a->gtape64);
+    a->gtape64 = nullptr;
+}
+
+// Allocates the buffers of the selected tape (and frees the other's).
+cudaError_t alloc_tape(mpm_adjoint* a) {
+    free_tapes(a);
+    const size_t np = (size_t)(a->b->n > 0 ? a->b->n : 1);
+    const size_t nc = (size_t)a->ncells;
+    cudaError_t e = cudaSuccess;
+    if (a->tape == MPM_TAPE_FIXED_POINT) {
+        a->ckpt.resize((size_t)a->nck);
+        for (int i = 0; i < a->nck && e == cudaSuccess; ++i) e = alloc_particles(a->ckpt[(size_t)i], np);
+        a->seg.resize((size_t)a->every);
+        for (int i = 1; i < a->every && e == cudaSuccess; ++i)
+            e = alloc_particles(a->seg[(size_t)i], np);
+        if (e == cudaSuccess) e = cudaMalloc(&a->gtape, sizeof(int4) * (size_t)a->every * nc);
+    } else {
+        a->ckpt64.assign((size_t)a->nck, nullptr);
+        for (int i = 0; i < a->nck && e == cudaSuccess; ++i)
+            e = cudaMalloc(&a->ckpt64[(size_t)i], sizeof(double) * kRec64 * np);
+        a->seg64.assign((size_t)a->every, nullptr);
+        for (int i = 1; i < a->every && e == cudaSuccess; ++i)
+            e = cudaMalloc(&a->seg64[(size_t)i], sizeof(double) * kRec64 * np);
+        for (int i = 0; i < 2 && e == cudaSuccess; ++i)
+            e = cudaMalloc(&a->scratch64[i], sizeof(double) * kRec64 * np);
+        if (e == cudaSuccess) e = cudaMalloc(&a->gtape64, sizeof(double4) * (size_t)a->every * nc);
+    }
+    return e;
+}
+
+void free_adjoint(mpm_adjoint* a) {
+    free_tapes(a);
+    free_particles(a->adj[0]);
+    free_particles(a->adj[1]);
+    cudaFree(a->gadj);
+    cudaFree(a->scenes_d);
+    cudaFree(a->pscene_d);
+    cudaFree(a->pgrad_d);
+    if (a->b) mpm_batch_destroy(a->b);
+    delete a;
+}
+
+int upload_adj_scenes(mpm_adjoint* a) {
+    const int S = (int)a->b->consts.size();
+    std::vector<AdjScene> hs((size_t)S);
+    for (int s = 0; s < S; ++s) {
+        hs[(size_t)s].k = a->b->consts[(size_t)s];
+        hs[(size_t)s].lbase = a->lbase[(size_t)s];
+    }
+    MPM_CUDA(cudaMemcpy(a->scenes_d, hs.data(), sizeof(AdjScene) * (size_t)S, cudaMemcpyHostToDevice));
+    return MPM_OK;
+}
+
+// Checkpoint slot of the state after `step` substeps of a T-substep forward
+// (-1: not kept).
+int ckpt_slot(const mpm_adjoint* a, int step, int T) {
+    if (step == T) return (T + a->every - 1) / a->every;
+    if (step >= 0 && step < T && step % a->every == 0) return step / a->every;
+    return -1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpm_adjoint_create(const mpm_scene_desc* scenes, int num_scenes, int max_substeps,
+                       int checkpoint_every, mpm_adjoint** out) {
+    if (!out) return fail(MPM_E_INVALID, "out is null");
+    *out = nullptr;
+    if (max_substeps < 1 || checkpoint_every < 1)
+        return fail(MPM_E_INVALID, "max_substeps and checkpoint_every must be positive");
+    if (!scenes || num_scenes < 1) return fail(MPM_E_INVALID, "a batch needs at least one scene");
+    long long n = 0, cells = 0;
+    std::vector<int> lbase((size_t)num_scenes);
+    std::vector<int> pscene;
+    for (int s = 0; s < num_scenes; ++s) {
+        SimConsts k;
+        if (int rc = scene_consts(scenes[s], k)) return rc;
+        lbase[(size_t)s] = (int)cells;
+        cells += k.grid_count;
+        n += scenes[s].num_particles;
+        if (cells > 0x7fffffffLL || n > 0x3fffffffLL) return fail(MPM_E_CAPACITY, "batch too large");
+        pscene.insert(pscene.end(), (size_t)scenes[s].num_particles, s);
+    }
+    // the engine starts from zeros; mpm_forward_ckpt loads the real state
+    std::vector<float> zeros((size_t)20 * (size_t)(n > 0 ? n : 1), 0.0f);
+    mpm_batch* b = nullptr;
+    if (int rc = mpm_batch_create(scenes, num_scenes, zeros.data(), &b)) return rc;
+    mpm_adjoint* a = new (std::nothrow) mpm_adjoint();
+    if (!a) {
+        mpm_batch_destroy(b);
+        return fail(MPM_E_INVALID, "out of host memory");
+    }
+    a->b = b;
+    a->max_substeps = max_substeps;
+    a->every = checkpoint_every < max_substeps ? checkpoint_every : max_substeps;
+    a->nck = (max_substeps + a->every - 1) / a->every + 1;
+    a->ncells = (int)cells;
+    a->lbase = lbase;
+    DeviceGuard g(b->device);
+    const size_t np = (size_t)(n > 0 ? n : 1);
+    cudaError_t e = alloc_tape(a);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = alloc_particles(a->adj[i], np);
+    if (e == cudaSuccess) e = cudaMalloc(&a->gadj, sizeof(float4) * (size_t)cells);
+    if (e == cudaSuccess) e = cudaMalloc(&a->scenes_d, sizeof(AdjScene) * (size_t)num_scenes);
+    if (e == cudaSuccess) e = cudaMalloc(&a->pscene_d, sizeof(int) * np);
+    if (e == cudaSuccess) e = cudaMalloc(&a->pgrad_d, sizeof(double) * 2 * (size_t)num_scenes);
+    if (e == cudaSuccess && n)
+        e = cudaMemcpy(a->pscene_d, pscene.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        const int rc = cuda_fail(e, "mpm_adjoint_create");
+        free_adjoint(a);
+        return rc;
+    }
+    if (int rc = upload_adj_scenes(a)) {
+        free_adjoint(a);
+        return rc;
+    }
+    *out = a;
+    return MPM_OK;
+}
+
+int mpm_adjoint_destroy(mpm_adjoint* a) {
+    if (!a) return MPM_OK;
+    DeviceGuard g(a->b->device);
+    cudaDeviceSynchronize();
+    free_adjoint(a);
+    return MPM_OK;
+}
+
+int mpm_adjoint_set_tape(mpm_adjoint* a, int tape) {
+    if (!a) return fail(MPM_E_INVALID, "null adjoint handle");
+    if (tape != MPM_TAPE_FIXED_POINT && tape != MPM_TAPE_FP64) return fail(MPM_E_INVALID, "unknown tape");
+    if (tape == a->tape) return MPM_OK;
+    DeviceGuard g(a->b->device);
+    MPM_CUDA(cudaDeviceSynchronize());
+    a->tape = tape;
+    a->T = -1;
+    MPM_CUDA(alloc_tape(a));
+    return MPM_OK;
+}
+
+int mpm_adjoint_set_scene(mpm_adjoint* a, int scene, const mpm_scene_desc* desc) {
+    if (!a) return fail(MPM_E_INVALID, "null adjoint handle");
+    if (int rc = mpm_batch_set_scene(a->b, scene, desc)) return rc;
+    DeviceGuard g(a->b->device);
+    MPM_CUDA(cudaDeviceSynchronize());
+    a->T = -1;
+    return upload_adj_scenes(a);
+}
+
+int mpm_forward_ckpt(mpm_adjoint* a, const float* init, int substeps, void* stream) {
+    if (!a) return fail(MPM_E_INVALID, "null adjoint handle");
+    mpm_batch* b = a->b;
+    if (substeps < 0 || substeps > a->max_substeps)
+        return fail(MPM_E_INVALID, "substeps outside [0, max_substeps]");
+    if (!init && b->n) return fail(MPM_E_INVALID, "initial state is null");
+    DeviceGuard g(b->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int n = b->n, S = (int)b->consts.size();
+    a->T = -1;
+    MPM_CUDA(cudaStreamSynchronize(st));
+    if (a->tape == MPM_TAPE_FP64) {
+        MPM_CUDA(upload_aos80_64(a->ckpt64[0], init, n));
+        const double* cur = a->ckpt64[0];
+        for (int t = 0; t < substeps; ++t) {
+            const int slot = ckpt_slot(a, t + 1, substeps);
+            double* dst = slot >= 0 ? a->ckpt64[(size_t)slot] : a->scratch64[t & 1];
+            launch_substep64(cur, a->gtape64, dst, a->scenes_d, S, a->pscene_d, n, a->ncells, st);
+            cur = dst;
+        }
+    } else {
+        MPM_CUDA(upload_aos80(a->ckpt[0], init, n));
+        MPM_CUDA(batch_load_device(b, a->ckpt[0], st));
+        int t = 0;
+        while (t < substeps) {
+            const int ns = substeps - t < a->every ? substeps - t : a->every;
+            if (sorted_step(b->sorted, &b->ps, b->posvel, b->counters, b->consts[0], ns, st,
+                            &b->prof, b->graph) != 0)
+                return fail(MPM_E_CUDA, std::string("forward: ") + sorted_error());
+            b->stepped = true;
+            t += ns;
+            batch_canonical_to(b, a->ckpt[(size_t)ckpt_slot(a, t, substeps)], st);
+        }
+    }
+    MPM_CUDA(cudaGetLastError());
+    a->T = substeps;
+    return MPM_OK;
+}
+
+int mpm_adjoint_state(mpm_adjoint* a, int substep, float* out) {
+    if (!a) return fail(MPM_E_INVALID, "null adjoint handle");
+    if (a->T < 0) return fail(MPM_E_STATE, "no forward run");
+    if (!out && a->b->n) return fail(MPM_E_INVALID, "null output");
+    const int j = ckpt_slot(a, substep, a->T);
+    if (j < 0) return fail(MPM_E_INVALID, "substep is not a checkpoint");
+    DeviceGuard g(a->b->device);
+    MPM_CUDA(cudaDeviceSynchronize());
+    if (a->tape == MPM_TAPE_FP64) MPM_CUDA(download_aos80_64(a->ckpt64[(size_t)j], a->b->n, out));
+    else MPM_CUDA(download_aos80(a->ckpt[(size_t)j], a->b->n, out));
+    return MPM_OK;
+}
+
+int mpm_backward(mpm_adjoint* a, const float* seeds, const int* seed_steps, int nseeds,
+                 float* grad_init, double* grad_params, void* stream) {
+    if (!a) return fail(MPM_E_INVALID, "null adjoint handle");
+    mpm_batch* b = a->b;
+    if (a->T < 0) return fail(MPM_E_STATE, "no forward run");
+    if (nseeds < 0 || (nseeds > 0 && (!seeds || !seed_steps)))
+        return fail(MPM_E_INVALID, "bad seeds");
+    for (int i = 0; i < nseeds; ++i)
+        if (seed_steps[i] < 0 || seed_steps[i] > a->T)
+            return fail(MPM_E_INVALID, "seed substep outside [0, T]");
+    DeviceGuard g(b->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int n = b->n, S = (int)b->consts.size();
+    const bool f64 = a->tape == MPM_TAPE_FP64;
+    MPM_CUDA(cudaStreamSynchronize(st));
+    std::vector<Particles> sbuf((size_t)nseeds);
+    auto release = [&]() {
+        for (Particles& P : sbuf) free_particles(P);
+    };
+    for (int i = 0; i < nseeds; ++i) {
+        cudaError_t e = alloc_particles(sbuf[(size_t)i], (size_t)(n > 0 ? n : 1));
+        if (e == cudaSuccess) e = upload_aos80(sbuf[(size_t)i], seeds + (size_t)i * 20 * (size_t)n, n);
+        if (e != cudaSuccess) {
+            release();
+            return cuda_fail(e, "mpm_backward seeds");
+        }
+    }
+    auto add_seeds = [&](int step, const Particles& A) {
+        for (int i = 0; i < nseeds; ++i)
+            if (seed_steps[i] == step) launch_particles_axpy(A, sbuf[(size_t)i], n, st);
+    };
+    int cur = 0;
+    float4* z[4] = {a->adj[0].p0, a->adj[0].p1, a->adj[0].p2, a->adj[0].p3};
+    for (int q = 0; q < 4; ++q) MPM_CUDA(cudaMemsetAsync(z[q], 0, sizeof(float4) * (size_t)n, st));
+    MPM_CUDA(cudaMemsetAsync(a->pgrad_d, 0, sizeof(double) * 2 * (size_t)S, st));
+    add_seeds(a->T, a->adj[cur]);
+    const int nseg = (a->T + a->every - 1) / a->every;
+    const size_t nc = (size_t)a->ncells;
+    for (int j = nseg - 1; j >= 0; --j) {
+        const int t0 = j * a->every;
+        const int t1 = t0 + a->every < a->T ? t0 + a->every : a->T;
+        // recompute the segment: states and updated grids of every substep
+        if (f64) {
+            const double* curS = a->ckpt64[(size_t)j];
+            for (int t = t0; t < t1; ++t) {
+                double* dst = t + 1 < t1 ? a->seg64[(size_t)(t + 1 - t0)] : a->scratch64[0];
+                launch_substep64(curS, a->gtape64 + (size_t)(t - t0) * nc, dst, a->scenes_d, S,
+                                 a->pscene_d, n, a->ncells, st);
+                curS = dst;
+            }
+        } else {
+            if (cudaError_t e = batch_load_device(b, a->ckpt[(size_t)j], st); e != cudaSuccess) {
+                release();
+                return cuda_fail(e, "mpm_backward recompute");
+            }
+            for (int t = t0; t < t1; ++t) {
+                if (sorted_step(b->sorted, &b->ps, b->posvel, b->counters, b->consts[0], 1, st,
+                                &b->prof, b->graph) != 0 ||
+                    sorted_export_all(b->sorted, a->gtape + (size_t)(t - t0) * nc, st, &b->prof) != 0) {
+                    release();
+                    return fail(MPM_E_CUDA, std::string("backward recompute: ") + sorted_error());
+                }
+                b->stepped = true;
+                if (t + 1 < t1) batch_canonical_to(b, a->seg[(size_t)(t + 1 - t0)], st);
+            }
+        }
+        // adjoint substeps in reverse
+        for (int t = t1 - 1; t >= t0; --t) {
+            if (f64) {
+                const double* Sx = t == t0 ? a->ckpt64[(size_t)j] : a->seg64[(size_t)(t - t0)];
+                launch_adjoint_substep64(Sx, a->gtape64 + (size_t)(t - t0) * nc, a->adj[cur],
+                                         a->adj[cur ^ 1], a->gadj, a->scenes_d, S, a->pscene_d, n,
+                                         a->ncells, a->pgrad_d, st);
+            } else {
+                const Particles& Sx = t == t0 ? a->ckpt[(size_t)j] : a->seg[(size_t)(t - t0)];
+                launch_adjoint_substep(Sx, a->gtape + (size_t)(t - t0) * nc, a->adj[cur],
+                                       a->adj[cur ^ 1], a->gadj, a->scenes_d, S, a->pscene_d, n,
+                                       a->ncells, a->pgrad_d, st);
+            }
+            cur ^= 1;
+            add_seeds(t, a->adj[cur]);
+        }
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    release();
+    if (e != cudaSuccess) return cuda_fail(e, "mpm_backward");
+    if (grad_init) MPM_CUDA(download_aos80(a->adj[cur], n, grad_init));
+    if (grad_params)
+        MPM_CUDA(cudaMemcpy(grad_params, a->pgrad_d, sizeof(double) * 2 * (size_t)S,
+                            cudaMemcpyDeviceToHost));
+    return MPM_OK;
 }
 
 }  // extern "C"

@@ -111,6 +111,7 @@ struct Scene {
     int bbase;
     int binbase;
     int pbase;
+    int lbase;   // first cell in the reference-layout concatenation of all grids
     SimConsts k;
 };
 
@@ -970,6 +971,22 @@ __global__ void k_export(const int4* __restrict__ grid, Geo g, int4* __restrict_
     out[i] = grid[flat_to_addr(g, i)];
 }
 
+// The same for every scene of a batch, into the concatenation of their
+// reference-layout grids (scene s at lbase).
+__global__ void k_export_all(const int4* __restrict__ grid, Dev d, int ncells,
+                             int4* __restrict__ out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= ncells) return;
+    int lo = 0, hi = d.nscenes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (d.scenes[mid].lbase <= j) lo = mid;
+        else hi = mid - 1;
+    }
+    const Scene& sc = d.scenes[lo];
+    out[j] = grid[(size_t)sc.bbase * 64 + flat_to_addr(sc.g, j - sc.lbase)];
+}
+
 }  // namespace
 
 // A captured run of substeps and the engine state it starts from / ends in.
@@ -1003,6 +1020,7 @@ struct SortedEngine {
     bool primed = false;
     bool has_grid = false;
     int blocks_p2g2 = 0, blocks_g2p = 0, blocks_update = 0;
+    int ncells_linear = 0;       // batch: cells of all scenes' reference-layout grids
     std::vector<GraphEntry> graphs;
 };
 
@@ -1182,7 +1200,7 @@ int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes) {
         return -1;
     }
     std::vector<Scene> hs((size_t)nscenes);
-    long long bricks = 0, bins = 0, parts = 0;
+    long long bricks = 0, bins = 0, parts = 0, lcells = 0;
     for (int s = 0; s < nscenes; ++s) {
         if (!make_geo(ks[s], hs[s].g)) {
             g_err = "scene " + std::to_string(s) + " has a degenerate box";
@@ -1191,11 +1209,13 @@ int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes) {
         hs[s].bbase = (int)bricks;
         hs[s].binbase = (int)bins;
         hs[s].pbase = (int)parts;
+        hs[s].lbase = (int)lcells;
         hs[s].k = ks[s];
         bricks += hs[s].g.nbricks;
         bins += (long long)hs[s].g.nbricks + 1;
         parts += ks[s].n;
-        if (bricks * 64 > INT_MAX || parts > e->max_particles) {
+        lcells += ks[s].grid_count;
+        if (bricks * 64 > INT_MAX || parts > e->max_particles || lcells > INT_MAX) {
             g_err = "batch exceeds the engine's capacity";
             return -1;
         }
@@ -1222,6 +1242,7 @@ int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes) {
     e->one = hs[0];
     e->nbricks = (int)bricks;
     e->nbins = (int)bins;
+    e->ncells_linear = (int)lcells;
     e->configured = true;
     return 0;
 }
@@ -1431,6 +1452,18 @@ int sorted_export_scene_grid(SortedEngine* e, int scene, int4* out, cudaStream_t
     const Geo& g = sc.g;
     const int4* grid = e->d.grid[e->last] + (size_t)(e->batch ? sc.bbase : 0) * 64;
     LAUNCH(KID_EXPORT, (k_export<<<(g.grid_count + 255) / 256, 256, 0, st>>>(grid, g, out)));
+    SE_CUDA(cudaGetLastError());
+    return 0;
+}
+
+int sorted_export_all(SortedEngine* e, int4* out, cudaStream_t st, LaunchProfiler* prof) {
+    if (!e->configured || !e->has_grid || !e->batch) {
+        g_err = "no batched sorted-engine grid to export";
+        return -1;
+    }
+    const int nc = e->ncells_linear;
+    LAUNCH(KID_EXPORT,
+           (k_export_all<<<(nc + 255) / 256, 256, 0, st>>>(e->d.grid[e->last], e->d, nc, out)));
     SE_CUDA(cudaGetLastError());
     return 0;
 }

@@ -52,6 +52,10 @@ int sorted_export_grid(SortedEngine* e, const SimConsts& k, int4* out, cudaStrea
 int sorted_export_scene_grid(SortedEngine* e, int scene, int4* out, cudaStream_t st,
                              LaunchProfiler* prof);
 
+// Batch: every scene's grid, as sorted_export_grid, into the concatenation of
+// the scenes' reference-layout grids (scene order).
+int sorted_export_all(SortedEngine* e, int4* out, cudaStream_t st, LaunchProfiler* prof);
+
 const char* sorted_error();
 
 }  // namespace mpm

@@ -456,3 +456,130 @@ class MLSMPMBatch:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------
+# Differentiation
+# ---------------------------------------------------------------------------
+
+class MLSMPMAdjoint:
+    """Forward with checkpoints and reverse-mode backward over a batch of
+    scenes (pass one scene for a single simulation).
+
+    forward(init, substeps) runs the fixed-point solver from `init` ((N, 20)
+    particle records of all scenes) and keeps the state every
+    `checkpointEvery` substeps.  backward(seeds) takes {substep: dL/dstate}
+    ((N, 20) arrays in the particle-record layout) and returns
+    (dL/d initial state (N, 20), dL/d (stiffness, dynamic_viscosity) per
+    scene (S, 2)).  The derivative is that of the continuous model the solver
+    discretises, along the solver's trajectory."""
+
+    def __init__(self, scenes, maxSubsteps: int, checkpointEvery: int = 20, device=None,
+                 tape: str = "fp64"):
+        self._lib = L.load()
+        self._device = device
+        self._descs = list(scenes)
+        arr = (L.SceneDesc * len(self._descs))(*self._descs)
+        counts = np.array([d.num_particles for d in self._descs], dtype=np.int64)
+        self.sceneOffsets = np.concatenate([[0], np.cumsum(counts)])
+        self.numParticles = int(self.sceneOffsets[-1])
+        self.maxSubsteps = int(maxSubsteps)
+        self.checkpointEvery = min(int(checkpointEvery), self.maxSubsteps)
+        self.substeps = None
+        self._handle = ctypes.c_void_p()
+        with self._on_device():
+            _check(self._lib.mpm_adjoint_create(arr, len(self._descs), self.maxSubsteps,
+                                                int(checkpointEvery), ctypes.byref(self._handle)),
+                   "MLSMPMAdjoint")
+        self.tape = tape
+
+    @property
+    def tape(self) -> str:
+        return self._tape
+
+    @tape.setter
+    def tape(self, name: str) -> None:
+        """"fp64": the continuous model integrated in FP64 (default);
+        "fixed": the solver's own fixed-point trajectory."""
+        code = {"fixed": L.MPM_TAPE_FIXED_POINT, "fp64": L.MPM_TAPE_FP64}[name]
+        _check(self._lib.mpm_adjoint_set_tape(self._handle, code), "tape")
+        self._tape = name
+        self.substeps = None
+
+    def _on_device(self):
+        if self._device is None:
+            import contextlib
+            return contextlib.nullcontext()
+        import torch
+        return torch.cuda.device(self._device)
+
+    @property
+    def numScenes(self) -> int:
+        return len(self._descs)
+
+    def setScene(self, scene: int, desc: L.SceneDesc) -> None:
+        _check(self._lib.mpm_adjoint_set_scene(self._handle, int(scene), ctypes.byref(desc)),
+               "setScene")
+        self._descs[scene] = desc
+        self.substeps = None
+
+    def forward(self, init: np.ndarray, substeps: int, commandEncoder=None) -> None:
+        recs = np.ascontiguousarray(init, dtype=np.float32).reshape(-1, 20)
+        if len(recs) != self.numParticles:
+            raise ValueError("initial state does not match the scenes' particle counts")
+        _check(self._lib.mpm_forward_ckpt(self._handle,
+                                          recs.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                          int(substeps), _stream_handle(commandEncoder)),
+               "forward")
+        self.substeps = int(substeps)
+
+    def state(self, substep: int) -> np.ndarray:
+        out = np.zeros((self.numParticles, 20), dtype=np.float32)
+        _check(self._lib.mpm_adjoint_state(self._handle, int(substep),
+                                           out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+               "state")
+        return out
+
+    def backward(self, seeds: dict, commandEncoder=None):
+        steps = sorted(seeds)
+        n = self.numParticles
+        block = np.zeros((max(len(steps), 1), n, 20), dtype=np.float32)
+        for j, t in enumerate(steps):
+            block[j] = np.asarray(seeds[t], dtype=np.float32).reshape(n, 20)
+        st = (ctypes.c_int32 * max(len(steps), 1))(*[int(t) for t in steps])
+        grad = np.zeros((n, 20), dtype=np.float32)
+        pgrad = np.zeros((self.numScenes, 2), dtype=np.float64)
+        _check(self._lib.mpm_backward(self._handle,
+                                      block.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), st,
+                                      len(steps), grad.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                      pgrad.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                      _stream_handle(commandEncoder)), "backward")
+        return grad, pgrad
+
+    def close(self) -> None:
+        if self._handle:
+            self._lib.mpm_adjoint_destroy(self._handle)
+            self._handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def centroid_loss(state: np.ndarray, target, offsets=None):
+    """Squared distance of each scene's particle centroid to `target`:
+    returns (loss per scene, dL/dstate (N, 20) with the position columns set)."""
+    state = np.asarray(state, dtype=np.float32).reshape(-1, 20)
+    offsets = [0, len(state)] if offsets is None else list(offsets)
+    t = np.asarray(target, dtype=np.float64)
+    seed = np.zeros_like(state)
+    losses = []
+    for s in range(len(offsets) - 1):
+        lo, hi = int(offsets[s]), int(offsets[s + 1])
+        x = state[lo:hi, 0:3].astype(np.float64)
+        c = x.mean(axis=0)
+        losses.append(float(np.sum((c - t) ** 2)))
+        seed[lo:hi, 0:3] = (2.0 * (c - t) / (hi - lo)).astype(np.float32)
+    return np.array(losses), seed
