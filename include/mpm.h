@@ -202,6 +202,18 @@ int mpm_set_gravity(mpm_sim* sim, const float gravity[3]);
  * default): plain launches. */
 int mpm_set_graph(mpm_sim* sim, int enable);
 
+/* Sorted engine: most particles per task.  A bin (4x4x4-cell brick) with
+ * more particles is split into several tasks, so that small scenes still
+ * spread over every SM.  0 (the default) picks it from the particle count;
+ * otherwise 64 ... 2^30.  Results do not depend on it. */
+int mpm_set_task_size(mpm_sim* sim, int task_size);
+int mpm_get_task_size(const mpm_sim* sim);
+/* Autotuner: times `substeps` substeps for each task size in {64, 128, 256,
+ * 512, 1024} from the current state, keeps the fastest and restores the
+ * state (particles, posvel, counters and grid are as before the call).
+ * Writes the choice to *chosen_task_size when non-null.  Synchronizes. */
+int mpm_autotune(mpm_sim* sim, int substeps, int* chosen_task_size);
+
 /* Batches: many independent scenes that advance together, one launch per
  * stage for all of them (the sorted engine over the scenes' concatenated
  * particles, bricks and bins), replayed as a CUDA graph.  Each scene gives
@@ -234,6 +246,10 @@ int mpm_batch_step(mpm_batch* batch, int substeps, void* stream);
 /* Replaces scene s's constants (box sizes and num_particles must stay). */
 int mpm_batch_set_scene(mpm_batch* batch, int scene, const mpm_scene_desc* desc);
 int mpm_batch_set_graph(mpm_batch* batch, int enable); /* default 1 */
+int mpm_batch_set_task_size(mpm_batch* batch, int task_size); /* see mpm_set_task_size */
+/* See mpm_autotune: the batch's particles and posvel are as before the call;
+ * mpm_batch_download_grid returns zeros until the next step. */
+int mpm_batch_autotune(mpm_batch* batch, int substeps, int* chosen_task_size);
 /* All scenes' particles, in input order (synchronizes). */
 int mpm_batch_download_particles(mpm_batch* batch, float* out_aos80);
 /* Scene s's grid after its last updateGrid, reference layout (synchronizes). */

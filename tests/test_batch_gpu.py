@@ -155,3 +155,25 @@ def test_full_size_batch_spot_check(cuda, pkg, oracle_mod):
     assert h["ok"] and h["out_of_range_accesses"] == 0
     assert batch.launchCount() > 0
     batch.close()
+
+
+def test_batch_task_size_and_autotune(cuda, pkg, oracle_mod):
+    from oracle import scene as scene_mod
+    descs, recs = mixed_scenes(pkg, scene_mod)
+    offs = np.concatenate([[0], np.cumsum([d.num_particles for d in descs])])
+    results = []
+    for cap in (64, 1024):
+        batch = pkg.MLSMPMBatch(descs, recs)
+        batch.setTaskSize(cap)
+        batch.step(6)
+        results.append(batch.downloadParticles())
+        batch.close()
+    assert_bits_equal(results[0], results[1], "task sizes 64 vs 1024")
+    batch = pkg.MLSMPMBatch(descs, recs)
+    batch.step(2)
+    before = batch.downloadParticles()
+    assert batch.autotune(2) in (64, 128, 256, 512, 1024)
+    assert_bits_equal(batch.downloadParticles(), before, "particles after autotune")
+    batch.step(4)
+    assert_bits_equal(batch.downloadParticles(), results[0], "after autotune")
+    batch.close()

@@ -289,3 +289,40 @@ def test_packed_f32x2_matches_scalar_ieee(cuda, pkg):
         assert np.array_equal(np.isnan(got), nan), what
         assert_bits_equal(got[~nan], want[~nan], what)
     assert (np.abs(want_m[np.isfinite(want_m)]) < 1.17549435e-38).sum() > 0  # subnormals covered
+
+
+@pytest.mark.parametrize("cap", [64, 200, 1024, 0])
+def test_task_size_does_not_change_results(cuda, pkg, oracle_mod, cap):
+    """Bins split into tasks of at most `cap` particles: same bits."""
+    box = [40.0, 30.0, 60.0]
+    sim = make_sim(pkg, "sorted")
+    sim.reset(70000, box)
+    sim.taskSize = cap
+    assert cap == 0 or sim.taskSize == cap
+    ref = oracle_mod.OracleSim(sim.downloadParticles(), box)
+    for _ in range(5):
+        sim.execute()
+        ref.execute(2, NTHREADS)
+    assert_state_equal(sim, ref, f"task size {cap}")
+    sim.close()
+
+
+def test_autotune_keeps_the_state(cuda, pkg, oracle_mod):
+    box = [40.0, 30.0, 60.0]
+    sim = make_sim(pkg, "sorted")
+    sim.reset(70000, box)
+    ref = oracle_mod.OracleSim(sim.downloadParticles(), box)
+    for _ in range(3):
+        sim.execute()
+        ref.execute(2, NTHREADS)
+    before = (sim.downloadParticles(), sim.downloadGrid(), sim.downloadPosvel())
+    chosen = sim.autotune(4)
+    assert chosen in (64, 128, 256, 512, 1024) and sim.taskSize == chosen
+    assert_bits_equal(sim.downloadParticles(), before[0], "particles after autotune")
+    assert_bits_equal(sim.downloadGrid(), before[1], "grid after autotune")
+    assert_bits_equal(sim.downloadPosvel(), before[2], "posvel after autotune")
+    for _ in range(3):
+        sim.execute()
+        ref.execute(2, NTHREADS)
+    assert_state_equal(sim, ref, "after autotune")
+    sim.close()

@@ -131,6 +131,11 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "mpm_launch_count": (i64, [vp]),
         "mpm_set_gravity": (i32, [vp, fp]),
         "mpm_set_graph": (i32, [vp, i32]),
+        "mpm_set_task_size": (i32, [vp, i32]),
+        "mpm_get_task_size": (i32, [vp]),
+        "mpm_autotune": (i32, [vp, i32, ctypes.POINTER(ctypes.c_int)]),
+        "mpm_batch_set_task_size": (i32, [vp, i32]),
+        "mpm_batch_autotune": (i32, [vp, i32, ctypes.POINTER(ctypes.c_int)]),
         "mpm_batch_create": (i32, [ctypes.POINTER(SceneDesc), i32, fp, ctypes.POINTER(vp)]),
         "mpm_batch_destroy": (i32, [vp]),
         "mpm_batch_num_scenes": (i32, [vp]),

@@ -188,6 +188,20 @@ __device__ __forceinline__ void add_param_grads(double* pg, int scene, bool acti
     }
 }
 
+// Lanes per particle in the particle-parallel adjoint kernels: lane q of a
+// group of kLanes consecutive lanes takes stencil cells q, q + kLanes, ...
+// of the 27, and the group sums its partial results with shuffles.  Small
+// scenes then still fill the GPU.
+constexpr int kLanes = 4;
+
+template <class R, int N>
+__device__ __forceinline__ void group_sum(R (&v)[N]) {
+#pragma unroll
+    for (int o = 1; o < kLanes; o <<= 1)
+#pragma unroll
+        for (int j = 0; j < N; ++j) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
+}
+
 // ---------------------------------------------------------------------------
 // g2p backward (g2p.wgsl:26-92).  Aout: adjoint of S_{t+1}; writes the g2p
 // part of the position adjoint of S_t into Anew (velocity and C adjoints
@@ -197,8 +211,10 @@ template <class Tape>
 __global__ void __launch_bounds__(kThreads)
     k_adj_g2p(Tape tp, Particles Aout, Particles Anew, float4* __restrict__ gadj,
               const AdjScene* __restrict__ scenes, const int* __restrict__ pscene, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = gi & (kLanes - 1);
+    const bool active = gi / kLanes < n;
+    const int i = active ? gi / kLanes : n - 1;
     const AdjScene& sc = scenes[pscene[i]];
     const SimConsts& k = sc.k;
     const int lb = sc.lbase;
@@ -209,17 +225,16 @@ __global__ void __launch_bounds__(kThreads)
     make_sten(x, st);
 
     float vg[3] = {0.0f, 0.0f, 0.0f};
-    for (int gx = 0; gx < 3; ++gx)
-        for (int gy = 0; gy < 3; ++gy)
-            for (int gz = 0; gz < 3; ++gz) {
-                Node nd;
-                if (!node(st, x, gx, gy, gz, k, nd)) continue;
-                float vi[3];
-                tp.vel(lb + nd.idx, k.fm, vi);
-                vg[0] += nd.w * vi[0];
-                vg[1] += nd.w * vi[1];
-                vg[2] += nd.w * vi[2];
-            }
+    for (int nn = lane; nn < 27; nn += kLanes) {
+        Node nd;
+        if (!node(st, x, nn / 9, (nn / 3) % 3, nn % 3, k, nd)) continue;
+        float vi[3];
+        tp.vel(lb + nd.idx, k.fm, vi);
+        vg[0] += nd.w * vi[0];
+        vg[1] += nd.w * vi[1];
+        vg[2] += nd.w * vi[2];
+    }
+    group_sum(vg);
 
     const Rec ao = load_rec(Aout, i);
     float xbar[3], vgbar[3];
@@ -234,37 +249,40 @@ __global__ void __launch_bounds__(kThreads)
         const float xcbar = ao.x[a] - 0.3f * nw * ao.v[a];
         const float xtbar = inside ? xcbar : 0.0f;
         vgbar[a] = ao.v[a] * (1.0f - 0.9f * k.dt * nw) + k.dt * xtbar;
-        xbar[a] = xtbar;
+        xbar[a] = lane == 0 ? xtbar : 0.0f;
     }
 
-    for (int gx = 0; gx < 3; ++gx)
-        for (int gy = 0; gy < 3; ++gy)
-            for (int gz = 0; gz < 3; ++gz) {
-                Node nd;
-                if (!node(st, x, gx, gy, gz, k, nd)) continue;
-                float vi[3];
-                tp.vel(lb + nd.idx, k.fm, vi);
-                float q[3];
+    for (int nn = lane; nn < 27; nn += kLanes) {
+        Node nd;
+        if (!node(st, x, nn / 9, (nn / 3) % 3, nn % 3, k, nd)) continue;
+        float vi[3];
+        tp.vel(lb + nd.idx, k.fm, vi);
+        float q[3];
 #pragma unroll
-                for (int r = 0; r < 3; ++r)
-                    q[r] = vgbar[r] + 4.0f * (ao.C[0][r] * nd.dist[0] + ao.C[1][r] * nd.dist[1] +
-                                              ao.C[2][r] * nd.dist[2]);
-                float* cell = reinterpret_cast<float*>(ga + nd.idx);
-                atomicAdd(cell + 0, nd.w * q[0]);
-                atomicAdd(cell + 1, nd.w * q[1]);
-                atomicAdd(cell + 2, nd.w * q[2]);
-                const float s = vi[0] * q[0] + vi[1] * q[1] + vi[2] * q[2];
+        for (int r = 0; r < 3; ++r)
+            q[r] = vgbar[r] + 4.0f * (ao.C[0][r] * nd.dist[0] + ao.C[1][r] * nd.dist[1] +
+                                      ao.C[2][r] * nd.dist[2]);
+        if (active) {
+            float* cell = reinterpret_cast<float*>(ga + nd.idx);
+            atomicAdd(cell + 0, nd.w * q[0]);
+            atomicAdd(cell + 1, nd.w * q[1]);
+            atomicAdd(cell + 2, nd.w * q[2]);
+        }
+        const float s = vi[0] * q[0] + vi[1] * q[1] + vi[2] * q[2];
 #pragma unroll
-                for (int a = 0; a < 3; ++a)
-                    xbar[a] += nd.gw[a] * s - 4.0f * nd.w *
-                                                  (ao.C[a][0] * vi[0] + ao.C[a][1] * vi[1] +
-                                                   ao.C[a][2] * vi[2]);
-            }
+        for (int a = 0; a < 3; ++a)
+            xbar[a] += nd.gw[a] * s - 4.0f * nd.w *
+                                          (ao.C[a][0] * vi[0] + ao.C[a][1] * vi[1] +
+                                           ao.C[a][2] * vi[2]);
+    }
+    group_sum(xbar);
 
-    Rec an{};
+    if (active && lane == 0) {
+        Rec an{};
 #pragma unroll
-    for (int a = 0; a < 3; ++a) an.x[a] = xbar[a];
-    store_rec(Anew, i, an);
+        for (int a = 0; a < 3; ++a) an.x[a] = xbar[a];
+        store_rec(Anew, i, an);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -321,100 +339,103 @@ __global__ void __launch_bounds__(kThreads)
     k_adj_p2g2(Tape tp, Particles Anew, float4* __restrict__ gadj,
                const AdjScene* __restrict__ scenes, const int* __restrict__ pscene, int n,
                double* __restrict__ pgrad) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = i < n;
-    const int scene = active ? pscene[i] : 0;
+    const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = gi & (kLanes - 1);
+    const bool active = gi / kLanes < n;
+    const int i = active ? gi / kLanes : n - 1;
+    const int scene = pscene[i];
+    const AdjScene& sc = scenes[scene];
+    const SimConsts& k = sc.k;
+    const int lb = sc.lbase;
+    float4* ga = gadj + lb;
+    const Rec p = tp.rec(i);
+    Sten st;
+    make_sten(p.x, st);
+    float rho[1] = {0.0f};
+    for (int nn = lane; nn < 27; nn += kLanes) {
+        Node nd;
+        if (!node(st, p.x, nn / 9, (nn / 3) % 3, nn % 3, k, nd)) continue;
+        rho[0] += tp.mass(lb + nd.idx, k.fm) * nd.w;
+    }
+    group_sum(rho);
+    const float V = 1.0f / rho[0];
+    const float r = rho[0] / k.rest_density;
+    const float r4 = (r * r) * (r * r);
+    const float pterm = k.stiffness * (r4 * r - 1.0f);
+    const float pres = fmaxf(pterm, 0.0f);
+    float T[3][3], sig[3][3], strain[3][3];  // [row][col]
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            strain[a][b] = p.C[b][a] + p.C[a][b];
+            sig[a][b] = (a == b ? -pres : 0.0f) + k.dynamic_viscosity * strain[a][b];
+            T[a][b] = -4.0f * V * k.dt * sig[a][b];
+        }
+    float acc[12] = {};  // Tb (row-major 9), then the position adjoint (3)
+    for (int nn = lane; nn < 27; nn += kLanes) {
+        Node nd;
+        if (!node(st, p.x, nn / 9, (nn / 3) % 3, nn % 3, k, nd)) continue;
+        const float4 g4 = ga[nd.idx];
+        const float g[3] = {g4.x, g4.y, g4.z};
+        float s = 0.0f;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float td = T[a][0] * nd.dist[0] + T[a][1] * nd.dist[1] + T[a][2] * nd.dist[2];
+            s += g[a] * td;
+#pragma unroll
+            for (int b = 0; b < 3; ++b) acc[3 * a + b] += nd.w * g[a] * nd.dist[b];
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            acc[9 + c] += nd.gw[c] * s - nd.w * (T[0][c] * g[0] + T[1][c] * g[1] + T[2][c] * g[2]);
+    }
+    group_sum(acc);
+    float sb[3][3], Vbar = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            sb[a][b] = -4.0f * V * k.dt * acc[3 * a + b];
+            Vbar += -4.0f * k.dt * sig[a][b] * acc[3 * a + b];
+        }
     float gk = 0.0f, gmu = 0.0f;
-    if (active) {
-        const AdjScene& sc = scenes[scene];
-        const SimConsts& k = sc.k;
-        const int lb = sc.lbase;
-        float4* ga = gadj + lb;
-        const Rec p = tp.rec(i);
-        Sten st;
-        make_sten(p.x, st);
-        float rho = 0.0f;
-        for (int gx = 0; gx < 3; ++gx)
-            for (int gy = 0; gy < 3; ++gy)
-                for (int gz = 0; gz < 3; ++gz) {
-                    Node nd;
-                    if (!node(st, p.x, gx, gy, gz, k, nd)) continue;
-                    rho += tp.mass(lb + nd.idx, k.fm) * nd.w;
-                }
-        const float V = 1.0f / rho;
-        const float r = rho / k.rest_density;
-        const float r4 = (r * r) * (r * r);
-        const float pterm = k.stiffness * (r4 * r - 1.0f);
-        const float pres = fmaxf(pterm, 0.0f);
-        float T[3][3], sig[3][3], strain[3][3];  // [row][col]
+    float Cb[3][3];
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
+    for (int a = 0; a < 3; ++a)
 #pragma unroll
-            for (int b = 0; b < 3; ++b) {
-                strain[a][b] = p.C[b][a] + p.C[a][b];
-                sig[a][b] = (a == b ? -pres : 0.0f) + k.dynamic_viscosity * strain[a][b];
-                T[a][b] = -4.0f * V * k.dt * sig[a][b];
-            }
-        float Tb[3][3] = {};
-        float xbar[3] = {0.0f, 0.0f, 0.0f};
-        for (int gx = 0; gx < 3; ++gx)
-            for (int gy = 0; gy < 3; ++gy)
-                for (int gz = 0; gz < 3; ++gz) {
-                    Node nd;
-                    if (!node(st, p.x, gx, gy, gz, k, nd)) continue;
-                    const float4 g4 = ga[nd.idx];
-                    const float g[3] = {g4.x, g4.y, g4.z};
-                    float s = 0.0f;
+        for (int b = 0; b < 3; ++b) {
+            Cb[b][a] = k.dynamic_viscosity * (sb[a][b] + sb[b][a]);  // M(a, b) = C[b][a]
+            gmu += strain[a][b] * sb[a][b];
+        }
+    const float pbar = -(sb[0][0] + sb[1][1] + sb[2][2]);
+    float rhobar = -Vbar / (rho[0] * rho[0]);
+    if (pterm > 0.0f) {
+        gk = pbar * (r4 * r - 1.0f);
+        rhobar += pbar * k.stiffness * 5.0f * r4 / k.rest_density;
+    }
+    float xb[3] = {0.0f, 0.0f, 0.0f};
+    for (int nn = lane; nn < 27; nn += kLanes) {
+        Node nd;
+        if (!node(st, p.x, nn / 9, (nn / 3) % 3, nn % 3, k, nd)) continue;
+        if (active) atomicAdd(reinterpret_cast<float*>(ga + nd.idx) + 3, rhobar * nd.w);
+        const float m = tp.mass(lb + nd.idx, k.fm);
 #pragma unroll
-                    for (int a = 0; a < 3; ++a) {
-                        const float td = T[a][0] * nd.dist[0] + T[a][1] * nd.dist[1] +
-                                         T[a][2] * nd.dist[2];
-                        s += g[a] * td;
-#pragma unroll
-                        for (int b = 0; b < 3; ++b) Tb[a][b] += nd.w * g[a] * nd.dist[b];
-                    }
-#pragma unroll
-                    for (int c = 0; c < 3; ++c)
-                        xbar[c] += nd.gw[c] * s -
-                                   nd.w * (T[0][c] * g[0] + T[1][c] * g[1] + T[2][c] * g[2]);
-                }
-        float sb[3][3], Vbar = 0.0f;
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int b = 0; b < 3; ++b) {
-                sb[a][b] = -4.0f * V * k.dt * Tb[a][b];
-                Vbar += -4.0f * k.dt * sig[a][b] * Tb[a][b];
-            }
+        for (int c = 0; c < 3; ++c) xb[c] += rhobar * m * nd.gw[c];
+    }
+    group_sum(xb);
+    const bool leader = active && lane == 0;
+    if (leader) {
         Rec an = load_rec(Anew, i);
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
+        for (int a = 0; a < 3; ++a) {
+            an.x[a] += acc[9 + a] + xb[a];
 #pragma unroll
-            for (int b = 0; b < 3; ++b) {
-                an.C[b][a] += k.dynamic_viscosity * (sb[a][b] + sb[b][a]);  // M(a, b) = C[b][a]
-                gmu += strain[a][b] * sb[a][b];
-            }
-        const float pbar = -(sb[0][0] + sb[1][1] + sb[2][2]);
-        float rhobar = -Vbar / (rho * rho);
-        if (pterm > 0.0f) {
-            gk = pbar * (r4 * r - 1.0f);
-            rhobar += pbar * k.stiffness * 5.0f * r4 / k.rest_density;
+            for (int b = 0; b < 3; ++b) an.C[a][b] += Cb[a][b];
         }
-        for (int gx = 0; gx < 3; ++gx)
-            for (int gy = 0; gy < 3; ++gy)
-                for (int gz = 0; gz < 3; ++gz) {
-                    Node nd;
-                    if (!node(st, p.x, gx, gy, gz, k, nd)) continue;
-                    atomicAdd(reinterpret_cast<float*>(ga + nd.idx) + 3, rhobar * nd.w);
-                    const float m = tp.mass(lb + nd.idx, k.fm);
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) xbar[c] += rhobar * m * nd.gw[c];
-                }
-#pragma unroll
-        for (int a = 0; a < 3; ++a) an.x[a] += xbar[a];
         store_rec(Anew, i, an);
     }
-    add_param_grads(pgrad, scene, active, gk, gmu);
+    add_param_grads(pgrad, scene, leader, gk, gmu);
 }
 
 // ---------------------------------------------------------------------------
@@ -425,40 +446,47 @@ template <class Tape>
 __global__ void __launch_bounds__(kThreads)
     k_adj_p2g1(Tape tp, Particles Anew, const float4* __restrict__ gadj,
                const AdjScene* __restrict__ scenes, const int* __restrict__ pscene, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = gi & (kLanes - 1);
+    const bool active = gi / kLanes < n;
+    const int i = active ? gi / kLanes : n - 1;
     const AdjScene& sc = scenes[pscene[i]];
     const SimConsts& k = sc.k;
     const float4* ga = gadj + sc.lbase;
     const Rec p = tp.rec(i);
     Sten st;
     make_sten(p.x, st);
+    float acc[15] = {};  // v adjoint (3), C adjoint C[b][a] at 3 + 3b + a (9), x adjoint (3)
+    for (int nn = lane; nn < 27; nn += kLanes) {
+        Node nd;
+        if (!node(st, p.x, nn / 9, (nn / 3) % 3, nn % 3, k, nd)) continue;
+        const float4 g4 = __ldg(ga + nd.idx);
+        const float g[3] = {g4.x, g4.y, g4.z};
+        float s = g4.w;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float q = p.v[a] + (p.C[0][a] * nd.dist[0] + p.C[1][a] * nd.dist[1] +
+                                      p.C[2][a] * nd.dist[2]);
+            s += g[a] * q;
+            acc[a] += nd.w * g[a];
+#pragma unroll
+            for (int b = 0; b < 3; ++b) acc[3 + 3 * b + a] += nd.w * g[a] * nd.dist[b];
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            acc[12 + c] += nd.gw[c] * s -
+                           nd.w * (p.C[c][0] * g[0] + p.C[c][1] * g[1] + p.C[c][2] * g[2]);
+    }
+    group_sum(acc);
+    if (!(active && lane == 0)) return;
     Rec an = load_rec(Anew, i);
-    float vbar[3] = {0.0f, 0.0f, 0.0f};
-    for (int gx = 0; gx < 3; ++gx)
-        for (int gy = 0; gy < 3; ++gy)
-            for (int gz = 0; gz < 3; ++gz) {
-                Node nd;
-                if (!node(st, p.x, gx, gy, gz, k, nd)) continue;
-                const float4 g4 = __ldg(ga + nd.idx);
-                const float g[3] = {g4.x, g4.y, g4.z};
-                float s = g4.w;
 #pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    const float q = p.v[a] + (p.C[0][a] * nd.dist[0] + p.C[1][a] * nd.dist[1] +
-                                              p.C[2][a] * nd.dist[2]);
-                    s += g[a] * q;
-                    vbar[a] += nd.w * g[a];
+    for (int a = 0; a < 3; ++a) {
+        an.v[a] = acc[a];
+        an.x[a] += acc[12 + a];
 #pragma unroll
-                    for (int b = 0; b < 3; ++b) an.C[b][a] += nd.w * g[a] * nd.dist[b];
-                }
-#pragma unroll
-                for (int c = 0; c < 3; ++c)
-                    an.x[c] += nd.gw[c] * s -
-                               nd.w * (p.C[c][0] * g[0] + p.C[c][1] * g[1] + p.C[c][2] * g[2]);
-            }
-#pragma unroll
-    for (int a = 0; a < 3; ++a) an.v[a] = vbar[a];
+        for (int b = 0; b < 3; ++b) an.C[b][a] += acc[3 + 3 * b + a];
+    }
     store_rec(Anew, i, an);
 }
 
@@ -506,6 +534,9 @@ __device__ __forceinline__ void weights64(const double* x, double ci[3], double 
     }
 }
 
+// One thread per particle: these kernels are bound by FP64 arithmetic, so
+// splitting a particle's stencil over lanes (which repeats the weights)
+// only adds work.
 __global__ void __launch_bounds__(kThreads)
     k64_p2g(const double* __restrict__ S, double4* __restrict__ G,
             const AdjScene* __restrict__ scenes, const int* __restrict__ pscene, int n, int stage) {
@@ -521,15 +552,13 @@ __global__ void __launch_bounds__(kThreads)
     double T[3][3];  // stage 2: [row][col]
     if (stage == 2) {
         double rho = 0.0;
-        for (int gx = 0; gx < 3; ++gx)
-            for (int gy = 0; gy < 3; ++gy)
-                for (int gz = 0; gz < 3; ++gz) {
-                    const double wt = w[0][gx] * w[1][gy] * w[2][gz];
-                    const int idx = flat64(ci[0] + gx - 1.0, ci[1] + gy - 1.0, ci[2] + gz - 1.0,
-                                           k.Y, k.Z);
-                    if ((unsigned)idx >= (unsigned)k.grid_count) continue;
-                    rho += grid[4 * (size_t)idx + 3] * wt;
-                }
+        for (int nn = 0; nn < 27; ++nn) {
+            const int gx = nn / 9, gy = (nn / 3) % 3, gz = nn % 3;
+            const double wt = w[0][gx] * w[1][gy] * w[2][gz];
+            const int idx = flat64(ci[0] + gx - 1.0, ci[1] + gy - 1.0, ci[2] + gz - 1.0, k.Y, k.Z);
+            if ((unsigned)idx >= (unsigned)k.grid_count) continue;
+            rho += grid[4 * (size_t)idx + 3] * wt;
+        }
         const double V = 1.0 / rho;
         const double rr = rho / (double)k.rest_density;
         const double pterm = (double)k.stiffness * (rr * rr * rr * rr * rr - 1.0);
@@ -541,9 +570,8 @@ __global__ void __launch_bounds__(kThreads)
                 T[a][b] = -V * 4.0 * sig * (double)k.dt;
             }
     }
-    for (int gx = 0; gx < 3; ++gx)
-        for (int gy = 0; gy < 3; ++gy)
-            for (int gz = 0; gz < 3; ++gz) {
+    for (int nn = 0; nn < 27; ++nn) {
+                const int gx = nn / 9, gy = (nn / 3) % 3, gz = nn % 3;
                 const double wt = w[0][gx] * w[1][gy] * w[2][gz];
                 const double c[3] = {ci[0] + gx - 1.0, ci[1] + gy - 1.0, ci[2] + gz - 1.0};
                 double d[3];
@@ -610,10 +638,9 @@ __global__ void __launch_bounds__(kThreads)
     const double x[3] = {P[0], P[1], P[2]};
     double ci[3], w[3][3];
     weights64(x, ci, w);
-    double v[3] = {0.0, 0.0, 0.0}, B[3][3] = {{0.0}};  // B[c][r]
-    for (int gx = 0; gx < 3; ++gx)
-        for (int gy = 0; gy < 3; ++gy)
-            for (int gz = 0; gz < 3; ++gz) {
+    double acc[12] = {};  // v (3), then B[c][r] at 3 + 3c + r
+    for (int nn = 0; nn < 27; ++nn) {
+                const int gx = nn / 9, gy = (nn / 3) % 3, gz = nn % 3;
                 const double wt = w[0][gx] * w[1][gy] * w[2][gz];
                 const double c[3] = {ci[0] + gx - 1.0, ci[1] + gy - 1.0, ci[2] + gz - 1.0};
                 double d[3];
@@ -629,14 +656,15 @@ __global__ void __launch_bounds__(kThreads)
                 for (int r = 0; r < 3; ++r) {
                     const double wv = gv[r] * wt;
 #pragma unroll
-                    for (int q = 0; q < 3; ++q) B[q][r] += wv * d[q];
-                    v[r] += wv;
+                    for (int q = 0; q < 3; ++q) acc[3 + 3 * q + r] += wv * d[q];
+                    acc[r] += wv;
                 }
-            }
+    }
+    const double v[3] = {acc[0], acc[1], acc[2]};
 #pragma unroll
     for (int q = 0; q < 3; ++q)
 #pragma unroll
-        for (int r = 0; r < 3; ++r) Q[6 + 3 * q + r] = B[q][r] * 4.0;
+        for (int r = 0; r < 3; ++r) Q[6 + 3 * q + r] = acc[3 + 3 * q + r] * 4.0;
     double xo[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -669,10 +697,11 @@ void adjoint_substep(const Tape& tp, const Particles& Aout, const Particles& Ane
                      double* pgrad, cudaStream_t st) {
     if (n <= 0) return;
     cudaMemsetAsync(gadj, 0, sizeof(float4) * (size_t)ncells, st);
-    k_adj_g2p<Tape><<<blocks(n), kThreads, 0, st>>>(tp, Aout, Anew, gadj, scenes, pscene, n);
+    const int pb = blocks((long long)n * kLanes);
+    k_adj_g2p<Tape><<<pb, kThreads, 0, st>>>(tp, Aout, Anew, gadj, scenes, pscene, n);
     k_adj_update<Tape><<<blocks(ncells), kThreads, 0, st>>>(tp, gadj, scenes, nscenes, ncells);
-    k_adj_p2g2<Tape><<<blocks(n), kThreads, 0, st>>>(tp, Anew, gadj, scenes, pscene, n, pgrad);
-    k_adj_p2g1<Tape><<<blocks(n), kThreads, 0, st>>>(tp, Anew, gadj, scenes, pscene, n);
+    k_adj_p2g2<Tape><<<pb, kThreads, 0, st>>>(tp, Anew, gadj, scenes, pscene, n, pgrad);
+    k_adj_p2g1<Tape><<<pb, kThreads, 0, st>>>(tp, Anew, gadj, scenes, pscene, n);
 }
 
 void launch_adjoint_substep(const Particles& S, const int4* G, const Particles& Aout,

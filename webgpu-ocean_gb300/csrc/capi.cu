@@ -460,6 +460,122 @@ int mpm_set_graph(mpm_sim* s, int enable) {
     return MPM_OK;
 }
 
+int mpm_set_task_size(mpm_sim* s, int cap) {
+    if (int rc = check_sim(s)) return rc;
+    if (sorted_set_task_cap(s->sorted, cap) != 0) return fail(MPM_E_INVALID, sorted_error());
+    return MPM_OK;
+}
+
+int mpm_get_task_size(const mpm_sim* s) { return s ? sorted_task_cap(s->sorted) : MPM_E_INVALID; }
+
+}  // extern "C"
+
+namespace {
+// Times `substeps` sorted-engine substeps for each candidate task size from
+// the same saved state and keeps the fastest.  The state after the call is
+// the state before it (particles, posvel, counters, grid).
+template <class StepFn>
+int tune_task_cap(SortedEngine* e, ParticleStore& ps, int n, float4* posvel,
+                  unsigned long long* counters, int substeps, cudaStream_t st, StepFn step,
+                  int* chosen, double* ms_out) {
+    static const int kCands[] = {64, 128, 256, 512, 1024};
+    Particles save{};
+    float4* pv = nullptr;
+    unsigned long long cnt[2] = {0, 0};
+    cudaEvent_t a = nullptr, b = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(save.p0); cudaFree(save.p1); cudaFree(save.p2); cudaFree(save.p3);
+        cudaFree(pv);
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    };
+    cudaError_t err = cudaSuccess;
+    float4** sp[4] = {&save.p0, &save.p1, &save.p2, &save.p3};
+    for (int q = 0; q < 4 && err == cudaSuccess; ++q) err = cudaMalloc(sp[q], sizeof(float4) * (size_t)(n ? n : 1));
+    if (err == cudaSuccess) err = cudaMalloc(&pv, sizeof(float4) * 2 * (size_t)(n ? n : 1));
+    if (err == cudaSuccess) err = cudaEventCreate(&a);
+    if (err == cudaSuccess) err = cudaEventCreate(&b);
+    if (err == cudaSuccess) err = cudaMemcpy(cnt, counters, sizeof(cnt), cudaMemcpyDeviceToHost);
+    // canonical snapshot of the state
+    if (err == cudaSuccess) {
+        const int c = ps.cur;
+        if (ps.canonical) {
+            const float4* src[4] = {ps.P[c].p0, ps.P[c].p1, ps.P[c].p2, ps.P[c].p3};
+            for (int q = 0; q < 4 && err == cudaSuccess; ++q)
+                err = cudaMemcpyAsync(*sp[q], src[q], sizeof(float4) * (size_t)n, cudaMemcpyDeviceToDevice, st);
+        } else {
+            launch_canonicalize(ps.P[c], ps.id[c], save, nullptr, n, st);
+            err = cudaGetLastError();
+        }
+    }
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(pv, posvel, sizeof(float4) * 2 * (size_t)n, cudaMemcpyDeviceToDevice, st);
+    auto restore = [&]() -> cudaError_t {
+        ps.cur = 0;
+        ps.canonical = true;
+        const float4* src[4] = {save.p0, save.p1, save.p2, save.p3};
+        float4* dst[4] = {ps.P[0].p0, ps.P[0].p1, ps.P[0].p2, ps.P[0].p3};
+        for (int q = 0; q < 4; ++q) {
+            cudaError_t e2 = cudaMemcpyAsync(dst[q], src[q], sizeof(float4) * (size_t)n, cudaMemcpyDeviceToDevice, st);
+            if (e2 != cudaSuccess) return e2;
+        }
+        launch_iota(ps.id[0], n, st);
+        sorted_invalidate(e);
+        return cudaGetLastError();
+    };
+    int best = 0;
+    double best_ms = 0.0;
+    for (int cap : kCands) {
+        if (err != cudaSuccess) break;
+        if (sorted_set_task_cap(e, cap) != 0) continue;
+        if ((err = restore()) != cudaSuccess) break;
+        if (step(1) != 0) { err = cudaErrorLaunchFailure; break; }  // primes
+        cudaEventRecord(a, st);
+        if (step(substeps) != 0) { err = cudaErrorLaunchFailure; break; }
+        cudaEventRecord(b, st);
+        if ((err = cudaEventSynchronize(b)) != cudaSuccess) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (!best || ms < best_ms) { best = cap; best_ms = ms; }
+    }
+    if (err == cudaSuccess) err = restore();
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(posvel, pv, sizeof(float4) * 2 * (size_t)n, cudaMemcpyDeviceToDevice, st);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(counters, cnt, sizeof(cnt), cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    cleanup();
+    if (err != cudaSuccess) return cuda_fail(err, "autotune");
+    if (best) sorted_set_task_cap(e, best);
+    if (chosen) *chosen = best;
+    if (ms_out) *ms_out = best_ms;
+    return MPM_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int mpm_autotune(mpm_sim* s, int substeps, int* chosen_task_size) {
+    if (int rc = check_sim(s)) return rc;
+    if (!s->loaded) return fail(MPM_E_STATE, "no scene loaded (call reset first)");
+    if (substeps < 1) return fail(MPM_E_INVALID, "substeps must be positive");
+    if (!s->sorted_ok || s->n == 0) {
+        if (chosen_task_size) *chosen_task_size = mpm_get_task_size(s);
+        return MPM_OK;
+    }
+    DeviceGuard g(s->device);
+    if (int rc = sync_ref_grid(s, nullptr)) return rc;
+    MPM_CUDA(cudaDeviceSynchronize());
+    const SimConsts k = s->consts();
+    auto step = [&](int ns) {
+        return sorted_step(s->sorted, &s->ps, s->posvel, s->counters, k, ns, s->internal, &s->prof,
+                           s->graph);
+    };
+    const int rc = tune_task_cap(s->sorted, s->ps, s->n, s->posvel, s->counters, substeps,
+                                 s->internal, step, chosen_task_size, nullptr);
+    s->ref_current = true;  // the grid from before the call
+    return rc;
+}
+
 int mpm_num_particles(const mpm_sim* s) { return s ? s->n : 0; }
 int64_t mpm_grid_count(const mpm_sim* s) { return s ? s->grid_count : 0; }
 float mpm_render_diameter(const mpm_sim* s) { return s ? s->render_diameter : 0.f; }
@@ -854,6 +970,27 @@ int mpm_batch_set_scene(mpm_batch* b, int scene, const mpm_scene_desc* desc) {
     b->desc[(size_t)scene] = *desc;
     b->consts[(size_t)scene] = k;
     return MPM_OK;
+}
+
+int mpm_batch_set_task_size(mpm_batch* b, int cap) {
+    if (int rc = check_batch(b)) return rc;
+    if (sorted_set_task_cap(b->sorted, cap) != 0) return fail(MPM_E_INVALID, sorted_error());
+    return MPM_OK;
+}
+
+int mpm_batch_autotune(mpm_batch* b, int substeps, int* chosen_task_size) {
+    if (int rc = check_batch(b)) return rc;
+    if (substeps < 1) return fail(MPM_E_INVALID, "substeps must be positive");
+    DeviceGuard g(b->device);
+    MPM_CUDA(cudaDeviceSynchronize());
+    auto step = [&](int ns) {
+        return sorted_step(b->sorted, &b->ps, b->posvel, b->counters, b->consts[0], ns, nullptr,
+                           &b->prof, b->graph);
+    };
+    const int rc = tune_task_cap(b->sorted, b->ps, b->n, b->posvel, b->counters, substeps, nullptr,
+                                 step, chosen_task_size, nullptr);
+    b->stepped = false;
+    return rc;
 }
 
 int mpm_batch_set_graph(mpm_batch* b, int enable) {

@@ -35,6 +35,7 @@
 //    and reads that scene's geometry and constants from a table (BATCH
 //    instantiations).  The single-scene instantiations take them as kernel
 //    parameters.
+#include <algorithm>
 #include <climits>
 #include <cstdio>
 #include <cstring>
@@ -68,8 +69,13 @@ constexpr int kA = 6;            // p2g_2 / g2p arena edge: brick + 1-cell halo
 constexpr int kSYA = 12, kSXA = 80, kNA = kA * kSXA;
 constexpr int kB = 8;            // next-p2g_1 arena edge: brick + 2-cell halo
 constexpr int kSYB = 12, kSXB = 112, kNB = kB * kSXB;
-constexpr int kMaxSort = 1024;   // bricks with more particles keep the bin order
+constexpr int kMaxSort = 1024;   // tasks with more particles keep the bin order
 constexpr int kScanThreads = 1024;
+// A bin holding more than `task_cap` particles is split into tasks of at
+// most task_cap particles (same brick, separate arena flushes), so that small
+// scenes, whose bricks are few and full, still spread over every SM.
+constexpr int kMinTaskCap = 64;
+constexpr int kMaxTaskCap = 1 << 30;
 
 // Minimum resident CTAs per SM requested from the register allocator.
 #ifndef MPM_G2P_MIN_BLOCKS
@@ -135,6 +141,7 @@ struct Dev {
     const uint32_t* brick_scene;  // global brick -> scene
     const uint32_t* bin_scene;    // global bin -> scene
     int nscenes;
+    int task_cap;                 // most particles per task
 };
 
 // The scene of a task: the table entry in a batch, else the kernel's own.
@@ -905,10 +912,15 @@ __device__ __forceinline__ void block_scan2(uint32_t& a, uint32_t& b, uint32_t* 
     b = eb;
 }
 
+__device__ __forceinline__ uint32_t tasks_of(uint32_t c, uint32_t cap) {
+    return (c + cap - 1u) / cap;
+}
+
 __global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, int nbins) {
     __shared__ uint32_t s_a[32], s_b[32];
     const int base = blockIdx.x * kScanThreads;
-    // counts of all bins before this CTA's range (particles, non-empty bins)
+    const uint32_t cap = (uint32_t)d.task_cap;
+    // counts of all bins before this CTA's range (particles, tasks)
     uint32_t pre_p = 0, pre_t = 0;
     {
         const uint4* c4 = reinterpret_cast<const uint4*>(d.bin_count);
@@ -916,7 +928,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, int nbins) {
         for (int i = threadIdx.x; i < n4; i += kScanThreads) {
             const uint4 q = __ldcg(c4 + i);
             pre_p += q.x + q.y + q.z + q.w;
-            pre_t += (q.x != 0u) + (q.y != 0u) + (q.z != 0u) + (q.w != 0u);
+            pre_t += tasks_of(q.x, cap) + tasks_of(q.y, cap) + tasks_of(q.z, cap) +
+                     tasks_of(q.w, cap);
         }
         uint32_t tp, tt;
         block_scan2(pre_p, pre_t, s_a, s_b, tp, tt);
@@ -926,15 +939,14 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, int nbins) {
     __syncthreads();  // s_a/s_b reused below
     const int bin = base + (int)threadIdx.x;
     const uint32_t c = bin < nbins ? __ldcg(d.bin_count + bin) : 0u;
-    uint32_t ep = c, et = c ? 1u : 0u, tot_p, tot_t;
+    const uint32_t nt = tasks_of(c, cap);
+    uint32_t ep = c, et = nt, tot_p, tot_t;
     block_scan2(ep, et, s_a, s_b, tot_p, tot_t);
     if (bin < nbins) {
         const uint32_t start = pre_p + ep;
         d.bin_start[bin] = start;
         if (c) {
             Task tk;
-            tk.first = (int)start;
-            tk.count = (int)c;
             if (d.bin_scene) {
                 const int sc = (int)__ldg(d.bin_scene + bin);
                 const int local = bin - d.scenes[sc].binbase;
@@ -944,7 +956,11 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, int nbins) {
                 tk.brick = bin == nbins - 1 ? -1 : bin;
                 tk.scene = 0;
             }
-            d.tasks[pre_t + et] = tk;
+            for (uint32_t q = 0; q < nt; ++q) {
+                tk.first = (int)(start + q * cap);
+                tk.count = (int)min(cap, c - q * cap);
+                d.tasks[pre_t + et + q] = tk;
+            }
         }
     }
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
@@ -1020,6 +1036,8 @@ struct SortedEngine {
     bool primed = false;
     bool has_grid = false;
     int blocks_p2g2 = 0, blocks_g2p = 0, blocks_update = 0;
+    int task_cap = kMaxSort;     // most particles per task (see kMinTaskCap)
+    bool task_cap_auto = true;   // task_cap follows the particle count
     int ncells_linear = 0;       // batch: cells of all scenes' reference-layout grids
     std::vector<GraphEntry> graphs;
 };
@@ -1107,7 +1125,7 @@ bool make_geo(const SimConsts& k, Geo& g) {
 // `bins` bins (kept when large enough).
 int ensure_grid_state(SortedEngine* e, long long bricks, long long bins) {
     const size_t cells = (size_t)bricks * 64;
-    const long long max_tasks = bins + 1;
+    const long long max_tasks = bins + (long long)e->max_particles / kMinTaskCap + 2;
     drop_graphs(e);
     if (cells <= e->grid_cells_alloc && bricks <= e->bricks_alloc && max_tasks <= e->max_tasks)
         return 0;
@@ -1127,6 +1145,20 @@ int ensure_grid_state(SortedEngine* e, long long bricks, long long bins) {
     return 0;
 }
 
+// Default task size: enough tasks for every resident CTA of the task
+// kernels, bins left whole when they already are.
+int auto_task_cap(const SortedEngine* e, long long n) {
+    const long long per = e->blocks_g2p > 0 ? n / e->blocks_g2p : kMaxSort;
+    return (int)std::min<long long>(kMaxSort, std::max<long long>(kMinTaskCap, per));
+}
+
+void apply_task_cap(SortedEngine* e, long long n) {
+    const int cap = e->task_cap_auto ? auto_task_cap(e, n) : e->task_cap;
+    if (cap != e->d.task_cap) drop_graphs(e);
+    e->task_cap = cap;
+    e->d.task_cap = cap;
+}
+
 }  // namespace
 
 int sorted_create(SortedEngine** out, int max_particles) {
@@ -1134,6 +1166,7 @@ int sorted_create(SortedEngine** out, int max_particles) {
     SortedEngine* e = new SortedEngine();
     e->max_particles = max_particles;
     e->d.nscenes = 1;
+    e->d.task_cap = kMaxSort;
     const size_t np = (size_t)(max_particles > 0 ? max_particles : 1);
     cudaError_t r = cudaMalloc(&e->d.bin_of, 4 * np);
     if (r == cudaSuccess) r = cudaMalloc(&e->d.rank_of, 4 * np);
@@ -1187,6 +1220,7 @@ int sorted_configure(SortedEngine* e, const SimConsts& k) {
     e->one.k = k;
     e->nbricks = g.nbricks;
     e->nbins = g.nbricks + 1;
+    apply_task_cap(e, k.n);
     e->configured = true;
     return 0;
 }
@@ -1243,9 +1277,28 @@ int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes) {
     e->nbricks = (int)bricks;
     e->nbins = (int)bins;
     e->ncells_linear = (int)lcells;
+    apply_task_cap(e, parts);
     e->configured = true;
     return 0;
 }
+
+int sorted_set_task_cap(SortedEngine* e, int cap) {
+    if (cap != 0 && (cap < kMinTaskCap || cap > kMaxTaskCap)) {
+        g_err = "task size outside [64, 2^30] (0: automatic)";
+        return -1;
+    }
+    e->task_cap_auto = cap == 0;
+    if (cap) e->task_cap = cap;
+    long long n = e->one.k.n;
+    if (e->batch) {
+        n = 0;
+        for (const Scene& sc : e->scenes) n += sc.k.n;
+    }
+    apply_task_cap(e, n);
+    return 0;
+}
+
+int sorted_task_cap(const SortedEngine* e) { return e->d.task_cap; }
 
 int sorted_set_scene_consts(SortedEngine* e, int scene, const SimConsts& k, cudaStream_t st) {
     if (!e->configured || !e->batch || scene < 0 || scene >= (int)e->scenes.size()) {
@@ -1432,6 +1485,7 @@ int sorted_step(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned lon
     // A single scene's constants are kernel parameters: graphs captured with
     // other constants are stale.
     if (graph && memcmp(&e->one.k, &k, sizeof(SimConsts)) != 0) drop_graphs(e);
+    if (k.n != e->one.k.n) apply_task_cap(e, k.n);
     e->one.k = k;
     return step_impl<false>(e, ps, posvel, oob, e->one, n, substeps, graph, st, prof);
 }

@@ -26,6 +26,12 @@ int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes);
 // its geometry and particle count must stay.  Stream-ordered.
 int sorted_set_scene_consts(SortedEngine* e, int scene, const SimConsts& k, cudaStream_t st);
 
+// Most particles per task (a bin with more is split); 0 restores the
+// automatic choice (enough tasks for every resident CTA, at most 1024).
+// Results do not depend on it.
+int sorted_set_task_cap(SortedEngine* e, int cap);
+int sorted_task_cap(const SortedEngine* e);
+
 // Forgets the carried-over state (the next step re-bins and redoes p2g_1).
 void sorted_invalidate(SortedEngine* e);
 

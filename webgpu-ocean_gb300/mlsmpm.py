@@ -211,6 +211,21 @@ class MLSMPMSimulator:
         """Run execute()'s substeps as one CUDA graph (sorted engine)."""
         _check(self._lib.mpm_set_graph(self._handle, int(bool(enable))), "setGraph")
 
+    @property
+    def taskSize(self) -> int:
+        """Most particles per sorted-engine task (0 to set: automatic)."""
+        return _check(self._lib.mpm_get_task_size(self._handle), "taskSize")
+
+    @taskSize.setter
+    def taskSize(self, cap: int) -> None:
+        _check(self._lib.mpm_set_task_size(self._handle, int(cap)), "taskSize")
+
+    def autotune(self, substeps: int = 8) -> int:
+        """Picks the fastest task size for the current scene; state unchanged."""
+        out = ctypes.c_int(0)
+        _check(self._lib.mpm_autotune(self._handle, int(substeps), ctypes.byref(out)), "autotune")
+        return int(out.value)
+
     def checkHealth(self) -> dict:
         h = L.Health()
         code = self._lib.mpm_check_health(self._handle, ctypes.byref(h))
@@ -417,6 +432,15 @@ class MLSMPMBatch:
 
     def setGraph(self, enable: bool) -> None:
         _check(self._lib.mpm_batch_set_graph(self._handle, int(bool(enable))), "setGraph")
+
+    def setTaskSize(self, cap: int) -> None:
+        _check(self._lib.mpm_batch_set_task_size(self._handle, int(cap)), "setTaskSize")
+
+    def autotune(self, substeps: int = 4) -> int:
+        out = ctypes.c_int(0)
+        _check(self._lib.mpm_batch_autotune(self._handle, int(substeps), ctypes.byref(out)),
+               "autotune")
+        return int(out.value)
 
     def downloadParticles(self) -> np.ndarray:
         out = np.zeros((self.numParticles, 20), dtype=np.float32)
