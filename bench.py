@@ -311,6 +311,80 @@ def measure_batched(pkg, torch, stream, repeats: int = 3) -> dict:
     }
 
 
+ADJ_WORKLOAD = ("32,768 particles (32^3 jittered lattice, spacing 0.5, origin 8) in a 48^3 grid, "
+                "velocities N(0, 0.1), 200 substeps, checkpoint every 20, centroid loss to "
+                "(30, 10, 30), gradients w.r.t. initial state, stiffness and viscosity")
+
+
+def measure_adjoint(pkg, torch, repeats: int = 3) -> dict:
+    """Forward (with checkpoints) and backward times of the differentiable
+    configuration, for both tapes, against the plain solver's forward."""
+    import numpy as np
+    recs = pkg.scene_lattice(32, 8.0, 0.5, 0.05, 3)
+    rng = np.random.default_rng(1)
+    recs[:, 4:7] = rng.normal(0.0, 0.1, (len(recs), 3)).astype(np.float32)
+    box, T = [48.0, 48.0, 48.0], 200
+    out = {"workload": ADJ_WORKLOAD, "substeps": T}
+    sim = pkg.MLSMPMSimulator(None, None, 1.2, maxParticles=len(recs), maxGrid=(48, 48, 48))
+    sim.upload(recs, box)
+    sim.setGraph(True)
+    sim.autotune(8)
+    sim.execute(substeps=T)
+    sim.synchronize()
+    best = None
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        sim.execute(substeps=T)
+        sim.synchronize()
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    out["plain_forward_ms"] = 1e3 * best
+    sim.close()
+    for tape in ("fixed", "fp64"):
+        adj = pkg.MLSMPMAdjoint([pkg.scene_desc(len(recs), box)], T, 20, tape=tape)
+        fwd = bwd = None
+        for _ in range(repeats):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            adj.forward(recs, T)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            _, seed = pkg.centroid_loss(adj.state(T), [30.0, 10.0, 30.0])
+            t2 = time.perf_counter()
+            adj.backward({T: seed})
+            torch.cuda.synchronize()
+            t3 = time.perf_counter()
+            fwd = t1 - t0 if fwd is None else min(fwd, t1 - t0)
+            bwd = t3 - t2 if bwd is None else min(bwd, t3 - t2)
+        adj.close()
+        out[tape] = {"forward_ms": 1e3 * fwd, "backward_ms": 1e3 * bwd,
+                     "fwd_plus_adj_over_own_forward": (fwd + bwd) / fwd,
+                     "fwd_plus_adj_over_plain_forward": (fwd + bwd) / best}
+    out["timing"] = ("host wall clock around synchronised calls, best of "
+                     f"{repeats}; plain forward = MLSMPMSimulator.execute(substeps=200), "
+                     "CUDA graph, autotuned task size")
+    return out
+
+
+def measure_inverse(pkg) -> dict:
+    """The batched inverse problem: 64 scenes, 16k-32k particles, 48^3
+    grids, hidden stiffness / viscosity, 100-substep rollouts, 50 Adam
+    iterations of batched forward + adjoint."""
+    import numpy as np
+    r = pkg.inverse.run_inverse_problem(64, seed=BATCH_SEED, substeps=100, iters=50)
+    rel = r["rel_err"]
+    h = r["history"]
+    return {"scenes": r["scenes"], "particles": r["particles"], "substeps": 100,
+            "iterations": 50, "tape": "fixed", "checkpoint_every": 20,
+            "observed_substeps": [20, 40, 60, 80, 100],
+            "seconds": r["seconds"], "ms_per_iteration": 1e3 * r["seconds"] / 50,
+            "stiffness_rel_err_median": float(np.median(rel[:, 0])),
+            "stiffness_rel_err_max": float(rel[:, 0].max()),
+            "viscosity_rel_err_median": float(np.median(rel[:, 1])),
+            "viscosity_rel_err_max": float(rel[:, 1].max()),
+            "loss_first": float(h[0]["loss"].mean()), "loss_last": float(h[-1]["loss"].mean())}
+
+
 def run_ours(args) -> None:
     import numpy as np
     import torch
@@ -438,6 +512,8 @@ def run_ours(args) -> None:
     sim.close()
 
     batched = None if args.skip_batched else measure_batched(pkg, torch, stream)
+    adjoint = None if args.skip_adjoint else measure_adjoint(pkg, torch)
+    inverse = None if args.skip_adjoint else measure_inverse(pkg)
 
     # --- bit-exactness self-check: sorted engine vs dispatch engine -------
     outs = []
@@ -486,6 +562,8 @@ def run_ours(args) -> None:
         "wall_s_timed_region": wall,
         "kernels": kernels,
         "batched": batched,
+        "adjoint": adjoint,
+        "inverse_problem": inverse,
         "parity": {"grid_bit_exact_vs_dispatch_engine": grid_exact,
                    "particles_bit_exact_vs_dispatch_engine": parts_exact, "steps": 3},
     }
@@ -503,6 +581,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-batched", action="store_true",
                     help="leave out the batched-scenes measurement")
+    ap.add_argument("--skip-adjoint", action="store_true",
+                    help="leave out the adjoint and inverse-problem measurements")
     ap.add_argument("--quick", action="store_true",
                     help="time the device-resident steps only (for profiler captures)")
     args = ap.parse_args()

@@ -11,6 +11,8 @@ from .mlsmpm import (MLSMPMAdjoint, MLSMPMBatch, MLSMPMSimulator, MPMError, Grid
                      batch_scenes, centroid_loss, default_params, probe_conversions, probe_packed,
                      scene_dambreak, scene_desc, scene_lattice)
 
-__all__ = ["MLSMPMSimulator", "MLSMPMBatch", "MLSMPMAdjoint", "centroid_loss", "MPMError", "GridCapacityError", "default_params",
-           "scene_dambreak", "scene_lattice", "scene_desc", "batch_scenes", "probe_conversions",
+from . import inverse
+
+__all__ = ["MLSMPMSimulator", "MLSMPMBatch", "MLSMPMAdjoint", "centroid_loss", "inverse",
+           "MPMError", "GridCapacityError", "default_params", "scene_dambreak", "scene_lattice", "scene_desc", "batch_scenes", "probe_conversions",
            "probe_packed", "build", "_lib"]

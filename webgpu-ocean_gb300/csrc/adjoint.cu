@@ -552,13 +552,18 @@ __global__ void __launch_bounds__(kThreads)
     double T[3][3];  // stage 2: [row][col]
     if (stage == 2) {
         double rho = 0.0;
-        for (int nn = 0; nn < 27; ++nn) {
-            const int gx = nn / 9, gy = (nn / 3) % 3, gz = nn % 3;
-            const double wt = w[0][gx] * w[1][gy] * w[2][gz];
-            const int idx = flat64(ci[0] + gx - 1.0, ci[1] + gy - 1.0, ci[2] + gz - 1.0, k.Y, k.Z);
-            if ((unsigned)idx >= (unsigned)k.grid_count) continue;
-            rho += grid[4 * (size_t)idx + 3] * wt;
-        }
+#pragma unroll
+        for (int gx = 0; gx < 3; ++gx)
+#pragma unroll
+            for (int gy = 0; gy < 3; ++gy)
+#pragma unroll
+                for (int gz = 0; gz < 3; ++gz) {
+                    const double wt = w[0][gx] * w[1][gy] * w[2][gz];
+                    const int idx = flat64(ci[0] + gx - 1.0, ci[1] + gy - 1.0, ci[2] + gz - 1.0,
+                                           k.Y, k.Z);
+                    if ((unsigned)idx >= (unsigned)k.grid_count) continue;
+                    rho += grid[4 * (size_t)idx + 3] * wt;
+                }
         const double V = 1.0 / rho;
         const double rr = rho / (double)k.rest_density;
         const double pterm = (double)k.stiffness * (rr * rr * rr * rr * rr - 1.0);
@@ -570,8 +575,12 @@ __global__ void __launch_bounds__(kThreads)
                 T[a][b] = -V * 4.0 * sig * (double)k.dt;
             }
     }
-    for (int nn = 0; nn < 27; ++nn) {
-                const int gx = nn / 9, gy = (nn / 3) % 3, gz = nn % 3;
+#pragma unroll
+    for (int gx = 0; gx < 3; ++gx)
+#pragma unroll
+        for (int gy = 0; gy < 3; ++gy)
+#pragma unroll
+            for (int gz = 0; gz < 3; ++gz) {
                 const double wt = w[0][gx] * w[1][gy] * w[2][gz];
                 const double c[3] = {ci[0] + gx - 1.0, ci[1] + gy - 1.0, ci[2] + gz - 1.0};
                 double d[3];
@@ -639,8 +648,12 @@ __global__ void __launch_bounds__(kThreads)
     double ci[3], w[3][3];
     weights64(x, ci, w);
     double acc[12] = {};  // v (3), then B[c][r] at 3 + 3c + r
-    for (int nn = 0; nn < 27; ++nn) {
-                const int gx = nn / 9, gy = (nn / 3) % 3, gz = nn % 3;
+#pragma unroll
+    for (int gx = 0; gx < 3; ++gx)
+#pragma unroll
+        for (int gy = 0; gy < 3; ++gy)
+#pragma unroll
+            for (int gz = 0; gz < 3; ++gz) {
                 const double wt = w[0][gx] * w[1][gy] * w[2][gz];
                 const double c[3] = {ci[0] + gx - 1.0, ci[1] + gy - 1.0, ci[2] + gz - 1.0};
                 double d[3];

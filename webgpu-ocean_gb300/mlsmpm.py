@@ -334,14 +334,15 @@ def scene_desc(num_particles: int, init_box, real_box=None, *, stiffness: float 
 
 def batch_scenes(num_scenes: int = 256, seed: int = 0, n_range=(4000, 64000), sides=(32, 48, 64),
                  spacing: float = 0.5, jitter: float = 0.05, stiffness_range=(2.0, 4.0),
-                 gravity_magnitude: float = 0.3):
+                 gravity_magnitude: float = 0.3, gravity=None):
     """Independent dam-break-like scenes of uneven sizes (numpy PCG64(seed)).
 
     Per scene: n uniform in n_range; a cubic grid whose side is drawn from
     `sides`; the first n points (x-major) of a jittered cubic lattice with
     ceil(cbrt(n)) points per axis, spacing `spacing`, placed at a uniform
     origin with the block inside the walls [3, side - 4]; gravity a uniform
-    random direction times `gravity_magnitude`; stiffness uniform in
+    random direction times `gravity_magnitude` (or the fixed vector
+    `gravity` when given); stiffness uniform in
     stiffness_range; the other constants are the reference's.
     Returns (list of SceneDesc, (sum n, 20) float32 records).
     """
@@ -360,7 +361,7 @@ def batch_scenes(num_scenes: int = 256, seed: int = 0, n_range=(4000, 64000), si
         lat = np.stack([idx // (a * a), (idx // a) % a, idx % a], axis=1).astype(np.float64)
         pos = origin + spacing * lat + jitter * (2.0 * rng.random((n, 3)) - 1.0)
         g = rng.normal(size=3)
-        g = gravity_magnitude * g / np.linalg.norm(g)
+        g = gravity_magnitude * g / np.linalg.norm(g) if gravity is None else np.asarray(gravity)
         k = float(rng.uniform(*stiffness_range))
         r = np.zeros((n, 20), dtype=np.float32)
         r[:, 0:3] = pos.astype(np.float32)
