@@ -192,10 +192,10 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-# DRAM bytes (read + write) per launch of the dominant kernel, mean of its two
-# variants, from one ncu capture of `bench.py --quick` on this workload
+# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
+# capture of `bench.py --quick` on this workload: its posvel-writing variant
 # (profiles/k_g2p_p2g1_1M_128.md).
-MEASURED_TRAFFIC_PER_LAUNCH = {"sorted_g2p_p2g_1": 100.7e6}
+MEASURED_TRAFFIC_PER_LAUNCH = {"sorted_g2p_p2g_1": 95.3e6}
 
 
 def algorithmic_bytes(kernel: str, n: int, cells: int) -> float | None:
@@ -383,6 +383,20 @@ def measure_inverse(pkg) -> dict:
             "viscosity_rel_err_median": float(np.median(rel[:, 1])),
             "viscosity_rel_err_max": float(rel[:, 1].max()),
             "loss_first": float(h[0]["loss"].mean()), "loss_last": float(h[-1]["loss"].mean())}
+
+
+def run_only(which: str) -> None:
+    import torch
+    import __graft_entry__ as entry
+    entry.build()
+    pkg = entry.load_package()
+    if which == "batched":
+        out = measure_batched(pkg, torch, torch.cuda.Stream())
+    elif which == "adjoint":
+        out = measure_adjoint(pkg, torch)
+    else:
+        out = measure_inverse(pkg)
+    print(json.dumps({"only": which, which: out}), flush=True)
 
 
 def run_ours(args) -> None:
@@ -583,6 +597,8 @@ def main():
                     help="leave out the batched-scenes measurement")
     ap.add_argument("--skip-adjoint", action="store_true",
                     help="leave out the adjoint and inverse-problem measurements")
+    ap.add_argument("--only", choices=["batched", "adjoint", "inverse"],
+                    help="run one side measurement alone and print its JSON (profiling)")
     ap.add_argument("--quick", action="store_true",
                     help="time the device-resident steps only (for profiler captures)")
     args = ap.parse_args()
@@ -590,6 +606,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.only:
+        run_only(args.only)
     else:
         run_ours(args)
 
