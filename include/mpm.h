@@ -299,6 +299,46 @@ int mpm_adjoint_state(mpm_adjoint* adj, int substep, float* out_aos80);
 int mpm_backward(mpm_adjoint* adj, const float* seeds_aos80, const int* seed_substeps,
                  int num_seeds, float* grad_init_aos80, double* grad_params, void* stream);
 
+/* Headless screen-space renderer (render/fluidRender.ts, fluid path):
+ * depth splat, 4 x bilateral filter, thickness splat, gaussian filter and
+ * shading, from the posvel records the simulator writes, into an image in
+ * device memory.  No window, swap chain or graphics API: the output is a
+ * device buffer (RGBA float or 8-bit). */
+typedef struct mpm_renderer mpm_renderer;
+
+/* RenderUniforms (common.ts:1-9, 272 bytes): 4x4 matrices by columns. */
+typedef struct mpm_render_uniforms {
+    float texel_size[2];      /* 1 / width, 1 / height */
+    float sphere_size;        /* billboard size (the simulator's render diameter) */
+    float pad;
+    float inv_projection_matrix[16];
+    float projection_matrix[16];
+    float view_matrix[16];
+    float inv_view_matrix[16];
+} mpm_render_uniforms;
+
+enum {
+    MPM_RENDER_COLOR = 0,     /* width*height float4, rows top to bottom */
+    MPM_RENDER_COLOR8 = 1,    /* width*height RGBA8 */
+    MPM_RENDER_DEPTH = 2,     /* filtered depth map, float */
+    MPM_RENDER_THICKNESS = 3  /* filtered thickness map, float (r16float values) */
+};
+
+/* FluidRenderer constructor (fluidRender.ts:34-46): image size, particle
+ * radius and vertical field of view (radians) set the filter constants.  The
+ * environment map starts as a built-in sky gradient. */
+int mpm_renderer_create(int width, int height, float radius, float fov, mpm_renderer** out);
+int mpm_renderer_destroy(mpm_renderer* renderer);
+/* Cube map faces +x, -x, +y, -y, +z, -z, each face_size^2 RGBA floats. */
+int mpm_renderer_set_envmap(mpm_renderer* renderer, int face_size, const float* rgba);
+/* FluidRenderer.execute (fluidRender.ts:292-488, sphereRenderFl false):
+ * posvel_device = 32-byte records (mpm_posvel_device_ptr), asynchronous. */
+int mpm_renderer_execute(mpm_renderer* renderer, const void* posvel_device, int num_particles,
+                         const mpm_render_uniforms* uniforms, void* stream);
+/* Copies one of the MPM_RENDER_* images to host memory (synchronizes). */
+int mpm_renderer_download(mpm_renderer* renderer, int what, void* out);
+void* mpm_renderer_color_device_ptr(mpm_renderer* renderer);
+
 /*
  * No counterpart in the reference.  The watchdog scan of mpm_check_health
  * over a caller-owned device buffer, allocating nothing: for callers that

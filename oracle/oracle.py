@@ -1,5 +1,6 @@
-"""ctypes front end of the C oracle (oracle/mpm_oracle.c, and the FP64
-continuous restatement oracle/mpm_oracle64.c used for finite differences).
+"""ctypes front end of the C oracle (oracle/mpm_oracle.c, the FP64
+continuous restatement oracle/mpm_oracle64.c used for finite differences,
+and the renderer restatement oracle/render_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
 bench.py (cpu_baseline leg and `--impl reference`) as the checker or the
@@ -20,7 +21,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "build")
 LIB_PATH = os.path.join(BUILD_DIR, "libmpm_oracle.so")
-SOURCES = [os.path.join(HERE, "mpm_oracle.c"), os.path.join(HERE, "mpm_oracle64.c")]
+SOURCES = [os.path.join(HERE, "mpm_oracle.c"), os.path.join(HERE, "mpm_oracle64.c"),
+           os.path.join(HERE, "render_oracle.c")]
 
 # -ffp-contract=off: every float op rounds separately, as the WGSL restatement
 # requires; no -ffast-math (keeps IEEE division, NaN and denormal semantics).
@@ -235,3 +237,51 @@ def run64(state: np.ndarray, params: Params64, substeps: int) -> np.ndarray:
     if L.orc64_run(st, len(st), ctypes.byref(params), int(substeps)) < 0:
         raise MemoryError("orc64_run")
     return st
+
+
+# ---------------------------------------------------------------------------
+# Screen-space renderer (render_oracle.c)
+# ---------------------------------------------------------------------------
+
+def _render_lib():
+    L = lib()
+    if not getattr(L, "_ro_ready", False):
+        f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+        u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+        L.ro_render.argtypes = [f32p, ctypes.c_int64, f32p, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_float, ctypes.c_float, ctypes.c_float, f32p, ctypes.c_int,
+                                f32p, u8p, f32p, f32p]
+        L.ro_render.restype = ctypes.c_int
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.ro_filter_constants.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, fp, fp, fp]
+        for name in ("ro_exp", "ro_log", "ro_half_round"):
+            getattr(L, name).argtypes = [ctypes.c_float]
+            getattr(L, name).restype = ctypes.c_float
+        L.ro_pow.argtypes = [ctypes.c_float, ctypes.c_float]
+        L.ro_pow.restype = ctypes.c_float
+        L._ro_ready = True
+    return L
+
+
+def render(posvel: np.ndarray, uniforms_f32: np.ndarray, width: int, height: int, radius: float,
+           fov: float, env: np.ndarray) -> dict:
+    """The whole fluid path on the CPU.  uniforms_f32: the 272-byte
+    RenderUniforms as 68 float32; env: (6, S, S, 4) float32."""
+    L = _render_lib()
+    pv = np.ascontiguousarray(posvel, dtype=np.float32).reshape(-1, 8)
+    u = np.ascontiguousarray(uniforms_f32, dtype=np.float32).reshape(68)
+    e = np.ascontiguousarray(env, dtype=np.float32)
+    dt, mf, ppc = ctypes.c_float(), ctypes.c_float(), ctypes.c_float()
+    L.ro_filter_constants(height, radius, fov, ctypes.byref(dt), ctypes.byref(mf), ctypes.byref(ppc))
+    out = {"color": np.zeros((height, width, 4), np.float32),
+           "color8": np.zeros((height, width, 4), np.uint8),
+           "depth": np.zeros((height, width), np.float32),
+           "thickness": np.zeros((height, width), np.float32)}
+    if L.ro_render(pv, len(pv), u, width, height, dt, mf, ppc, e, e.shape[1], out["color"],
+                   out["color8"], out["depth"], out["thickness"]) != 0:
+        raise MemoryError("ro_render")
+    return out
+
+
+def render_scalar(name: str, *args) -> float:
+    return float(getattr(_render_lib(), "ro_" + name)(*args))

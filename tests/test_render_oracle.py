@@ -1,0 +1,42 @@
+"""CPU checks of the renderer restatement's scalar helpers (the same code
+runs on the GPU): exp / log / pow against numpy in double precision, and the
+half-precision rounding of r16float writes against numpy's float16."""
+from __future__ import annotations
+
+import numpy as np
+
+
+def test_exp_log_pow_accuracy(oracle_mod):
+    rng = np.random.default_rng(0)
+    xs = np.concatenate([rng.uniform(-100, 88, 4000), rng.uniform(-1, 1, 2000), [0.0, -0.0, 1e-30]])
+    for x in xs.astype(np.float32):
+        got = oracle_mod.render_scalar("exp", float(x))
+        want = np.exp(np.float64(x))
+        if want < 1.2e-38:  # subnormal results: absolute error of one subnormal step
+            assert abs(got - want) <= 2e-45
+        else:
+            assert abs(got - want) <= 3e-7 * want, (x, got, want)
+    for x in np.concatenate([rng.uniform(1e-30, 1e30, 2000), rng.uniform(0.5, 2.0, 2000),
+                             [1.0, 2.0, 1e-40, 3.4e38]]).astype(np.float32):
+        got = oracle_mod.render_scalar("log", float(x))
+        want = np.log(np.float64(x))
+        assert abs(got - want) <= 3e-7 * max(1.0, abs(want)), (x, got, want)
+    for x, y in [(0.5, 250.0), (0.999, 250.0), (0.3, 5.0), (0.0, 5.0), (1.0, 250.0)]:
+        got = oracle_mod.render_scalar("pow", x, y)
+        want = np.float64(np.float32(x)) ** y
+        assert abs(got - want) <= 2e-6 * max(want, 1e-30) + 1e-38, (x, y, got, want)
+    assert np.isnan(oracle_mod.render_scalar("pow", -0.5, 5.0))
+    assert oracle_mod.render_scalar("exp", 200.0) == np.inf
+    assert oracle_mod.render_scalar("exp", -200.0) == 0.0
+
+
+def test_half_rounding_matches_ieee(oracle_mod):
+    rng = np.random.default_rng(1)
+    vals = np.concatenate([
+        rng.uniform(0, 1, 3000), rng.uniform(0, 70000, 1000), rng.uniform(0, 1e-4, 1000),
+        rng.standard_normal(1000) * 1e-6,
+        [0.0, 65504.0, 65519.0, 65520.0, 6.1035156e-05, 5.96e-08, 2.98e-08, 1.0 + 2**-11]]).astype(np.float32)
+    for v in vals:
+        got = np.float32(oracle_mod.render_scalar("half_round", float(v)))
+        want = np.float32(np.float16(v))
+        assert got == want or (np.isinf(got) and np.isinf(want)), (v, got, want)

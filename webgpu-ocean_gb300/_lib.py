@@ -29,6 +29,11 @@ MPM_ENGINE_DISPATCH = 1
 MPM_TAPE_FIXED_POINT = 0
 MPM_TAPE_FP64 = 1
 
+MPM_RENDER_COLOR = 0
+MPM_RENDER_COLOR8 = 1
+MPM_RENDER_DEPTH = 2
+MPM_RENDER_THICKNESS = 3
+
 KERNELS = {
     "clearGrid": 0,
     "p2g_1": 1,
@@ -62,6 +67,20 @@ class SceneDesc(ctypes.Structure):
         ("dt", ctypes.c_float),
         ("fixed_point_multiplier", ctypes.c_float),
         ("gravity", ctypes.c_float * 3),
+    ]
+
+
+class RenderUniforms(ctypes.Structure):
+    """mpm_render_uniforms: RenderUniforms of common.ts:1-9 (272 bytes),
+    4x4 matrices by columns."""
+    _fields_ = [
+        ("texel_size", ctypes.c_float * 2),
+        ("sphere_size", ctypes.c_float),
+        ("pad", ctypes.c_float),
+        ("inv_projection_matrix", ctypes.c_float * 16),
+        ("projection_matrix", ctypes.c_float * 16),
+        ("view_matrix", ctypes.c_float * 16),
+        ("inv_view_matrix", ctypes.c_float * 16),
     ]
 
 
@@ -155,6 +174,12 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "mpm_forward_ckpt": (i32, [vp, fp, i32, vp]),
         "mpm_adjoint_state": (i32, [vp, i32, fp]),
         "mpm_backward": (i32, [vp, fp, ip, i32, fp, dp, vp]),
+        "mpm_renderer_create": (i32, [i32, i32, f32, f32, ctypes.POINTER(vp)]),
+        "mpm_renderer_destroy": (i32, [vp]),
+        "mpm_renderer_set_envmap": (i32, [vp, i32, fp]),
+        "mpm_renderer_execute": (i32, [vp, vp, i32, ctypes.POINTER(RenderUniforms), vp]),
+        "mpm_renderer_download": (i32, [vp, i32, vp]),
+        "mpm_renderer_color_device_ptr": (vp, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

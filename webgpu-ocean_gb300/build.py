@@ -25,8 +25,9 @@ REPO = os.path.dirname(HERE)
 INCLUDE = os.path.join(REPO, "include")
 
 SOURCES = ["capi.cu", "kernels_dispatch.cu", "kernels_sorted.cu", "profiler.cu", "noalloc.cu",
-           "adjoint.cu"]
-HEADERS = ["mpm_math.cuh", "mpm_math_x2.cuh", "mpm_internal.h", "sorted_engine.h", "adjoint.h"]
+           "adjoint.cu", "render.cu"]
+HEADERS = ["mpm_math.cuh", "mpm_math_x2.cuh", "mpm_internal.h", "sorted_engine.h", "adjoint.h",
+           "render_math.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xptxas=--fmad=false",
