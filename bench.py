@@ -385,6 +385,52 @@ def measure_inverse(pkg) -> dict:
             "loss_first": float(h[0]["loss"].mean()), "loss_last": float(h[-1]["loss"].mean())}
 
 
+def measure_render(pkg, torch, frames: int = 10) -> dict:
+    """Headless renderer (depth/thickness splats, 8 bilateral + 2 gaussian
+    passes, shading): ms per frame for the reference's default scene
+    (70,000 particles in 40x30x60, 60 frames in, camera distance 70) at
+    896x504 (a 1280x720 canvas at main.ts's 0.7 pixel ratio), and for the
+    1M-particle lattice at 1344x756."""
+    import math
+    out = {}
+    fov = 45 * math.pi / 180
+    cases = [("default_scene_70k_896x504", 70000, [40.0, 30.0, 60.0], 896, 504, 70.0, 60),
+             ("lattice_1M_1344x756", None, BOX, 1344, 756, 160.0, 5)]
+    for name, n_req, box, W, H, dist, warm in cases:
+        if n_req is None:
+            parts = make_scene(pkg)
+            sim = pkg.MLSMPMSimulator(None, None, 1.2, maxParticles=len(parts),
+                                      maxGrid=(128, 128, 128))
+            sim.upload(parts, box)
+            target = [29.0, 20.0, 29.0]
+        else:
+            sim = pkg.MLSMPMSimulator(None, None, 1.2, maxParticles=200000)
+            sim.reset(n_req, box)
+            target = [box[0] / 2, box[1] / 4, box[2] / 2]
+        for _ in range(warm):
+            sim.execute()
+        r = pkg.FluidRenderer(W, H)
+        u = pkg.camera_uniforms(W, H, dist, target, fov, 1.2)
+        stream = torch.cuda.current_stream()
+        for _ in range(3):
+            r.execute(sim, sim.numParticles, u, stream)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(frames):
+            r.execute(sim, sim.numParticles, u, stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / frames
+        depth = r.download("depth")
+        out[name] = {"particles": sim.numParticles, "width": W, "height": H,
+                     "ms_per_frame": ms, "frames_per_s": 1e3 / ms,
+                     "fluid_pixel_fraction": float((depth > 0).mean())}
+        r.close()
+        sim.close()
+    out["timing"] = f"CUDA events around {frames} frames after 3 warm-up frames"
+    return out
+
+
 def run_only(which: str) -> None:
     import torch
     import __graft_entry__ as entry
@@ -394,6 +440,8 @@ def run_only(which: str) -> None:
         out = measure_batched(pkg, torch, torch.cuda.Stream())
     elif which == "adjoint":
         out = measure_adjoint(pkg, torch)
+    elif which == "render":
+        out = measure_render(pkg, torch)
     else:
         out = measure_inverse(pkg)
     print(json.dumps({"only": which, which: out}), flush=True)
@@ -528,6 +576,7 @@ def run_ours(args) -> None:
     batched = None if args.skip_batched else measure_batched(pkg, torch, stream)
     adjoint = None if args.skip_adjoint else measure_adjoint(pkg, torch)
     inverse = None if args.skip_adjoint else measure_inverse(pkg)
+    render = None if args.skip_batched else measure_render(pkg, torch)
 
     # --- bit-exactness self-check: sorted engine vs dispatch engine -------
     outs = []
@@ -578,6 +627,7 @@ def run_ours(args) -> None:
         "batched": batched,
         "adjoint": adjoint,
         "inverse_problem": inverse,
+        "render": render,
         "parity": {"grid_bit_exact_vs_dispatch_engine": grid_exact,
                    "particles_bit_exact_vs_dispatch_engine": parts_exact, "steps": 3},
     }
@@ -597,7 +647,7 @@ def main():
                     help="leave out the batched-scenes measurement")
     ap.add_argument("--skip-adjoint", action="store_true",
                     help="leave out the adjoint and inverse-problem measurements")
-    ap.add_argument("--only", choices=["batched", "adjoint", "inverse"],
+    ap.add_argument("--only", choices=["batched", "adjoint", "inverse", "render"],
                     help="run one side measurement alone and print its JSON (profiling)")
     ap.add_argument("--quick", action="store_true",
                     help="time the device-resident steps only (for profiler captures)")

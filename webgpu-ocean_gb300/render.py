@@ -135,3 +135,20 @@ def write_ppm(path: str, rgba8: np.ndarray) -> None:
     with open(path, "wb") as f:
         f.write(b"P6\n%d %d\n255\n" % (w, h))
         f.write(np.ascontiguousarray(rgba8[:, :, :3]).tobytes())
+
+
+def write_png(path: str, rgba8: np.ndarray) -> None:
+    """PNG (8-bit RGBA, no filtering) of an (H, W, 4) uint8 image."""
+    import struct
+    import zlib
+    h, w = rgba8.shape[:2]
+    raw = b"".join(b"\x00" + np.ascontiguousarray(rgba8[y]).tobytes() for y in range(h))
+
+    def chunk(tag: bytes, data: bytes) -> bytes:
+        return (struct.pack(">I", len(data)) + tag + data +
+                struct.pack(">I", zlib.crc32(tag + data) & 0xffffffff))
+    with open(path, "wb") as f:
+        f.write(b"\x89PNG\r\n\x1a\n")
+        f.write(chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)))
+        f.write(chunk(b"IDAT", zlib.compress(raw, 6)))
+        f.write(chunk(b"IEND", b""))
