@@ -339,6 +339,36 @@ int mpm_renderer_execute(mpm_renderer* renderer, const void* posvel_device, int 
 int mpm_renderer_download(mpm_renderer* renderer, int what, void* out);
 void* mpm_renderer_color_device_ptr(mpm_renderer* renderer);
 
+/* The reference's second simulator, SPHSimulator (sph/sph.ts), behind the
+ * same four methods.  Particle records are the reference's 64 bytes:
+ * position vec3f @0, v vec3f @16, force vec3f @32, density f32 @44,
+ * nearDensity f32 @48 (sph.ts:13,205-211).  Box sizes are HALF sizes, as
+ * SPHSimulator.reset/changeBoxSize take them. */
+typedef struct mpm_sph mpm_sph;
+
+/* constructor(particleBuffer, posvelBuffer, renderDiameter, device), sph.ts:46 */
+int mpm_sph_create(int max_particles, float render_diameter, void* posvel_device,
+                   size_t posvel_bytes, mpm_sph** out);
+int mpm_sph_destroy(mpm_sph* sph);
+/* reset(numParticles, initHalfBoxSize), sph.ts:300-316 (initDambreak with
+ * Math.random -> SplitMix64(seed)) */
+int mpm_sph_reset_dambreak(mpm_sph* sph, int num_particles, const double init_half_box[3],
+                           uint64_t seed);
+int mpm_sph_upload(mpm_sph* sph, const float* rec64, int n, const float real_half_box[3]);
+/* execute(commandEncoder), sph.ts:318-356: `substeps` (2 per frame) */
+int mpm_sph_step(mpm_sph* sph, int substeps, void* stream);
+/* changeBoxSize(realBoxSize), sph.ts:383-388 (half sizes) */
+int mpm_sph_set_real_box(mpm_sph* sph, const float real_half_box[3]);
+int mpm_sph_num_particles(const mpm_sph* sph);
+int64_t mpm_sph_grid_count(const mpm_sph* sph);
+void* mpm_sph_posvel_device_ptr(mpm_sph* sph);
+/* All particle records / posvel records (synchronize). */
+int mpm_sph_download_particles(mpm_sph* sph, float* out_rec64);
+int mpm_sph_download_posvel(mpm_sph* sph, float* out_posvel);
+/* initDambreak alone, into host memory; returns the record count. */
+int mpm_sph_scene_dambreak(float* out_rec64, int num_particles, const double init_half_box[3],
+                           uint64_t seed);
+
 /*
  * No counterpart in the reference.  The watchdog scan of mpm_check_health
  * over a caller-owned device buffer, allocating nothing: for callers that

@@ -1,6 +1,7 @@
 """ctypes front end of the C oracle (oracle/mpm_oracle.c, the FP64
 continuous restatement oracle/mpm_oracle64.c used for finite differences,
-and the renderer restatement oracle/render_oracle.c).
+the renderer restatement oracle/render_oracle.c and the SPH restatement
+oracle/sph_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
 bench.py (cpu_baseline leg and `--impl reference`) as the checker or the
@@ -22,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "build")
 LIB_PATH = os.path.join(BUILD_DIR, "libmpm_oracle.so")
 SOURCES = [os.path.join(HERE, "mpm_oracle.c"), os.path.join(HERE, "mpm_oracle64.c"),
-           os.path.join(HERE, "render_oracle.c")]
+           os.path.join(HERE, "render_oracle.c"), os.path.join(HERE, "sph_oracle.c")]
 
 # -ffp-contract=off: every float op rounds separately, as the WGSL restatement
 # requires; no -ffast-math (keeps IEEE division, NaN and denormal semantics).
@@ -285,3 +286,31 @@ def render(posvel: np.ndarray, uniforms_f32: np.ndarray, width: int, height: int
 
 def render_scalar(name: str, *args) -> float:
     return float(getattr(_render_lib(), "ro_" + name)(*args))
+
+
+# ---------------------------------------------------------------------------
+# SPH (sph_oracle.c)
+# ---------------------------------------------------------------------------
+
+def sph_execute(records: np.ndarray, real_half, substeps: int = 2):
+    """Runs `substeps` SPH substeps on (n, 16) float32 records; returns
+    (records, posvel (n, 8))."""
+    L = lib()
+    if not getattr(L, "_so_ready", False):
+        f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+        L.so_execute.argtypes = [f32p, ctypes.c_int64, ctypes.POINTER(ctypes.c_float), ctypes.c_int,
+                                 f32p]
+        L.so_execute.restype = ctypes.c_int
+        L.so_grid_count.restype = ctypes.c_int
+        L._so_ready = True
+    rec = np.ascontiguousarray(records, dtype=np.float32).reshape(-1, 16).copy()
+    pv = np.zeros((max(len(rec), 1), 8), np.float32)
+    half = (ctypes.c_float * 3)(*[float(np.float32(h)) for h in real_half])
+    if L.so_execute(rec, len(rec), half, int(substeps), pv) != 0:
+        raise MemoryError("so_execute")
+    return rec, pv[:len(rec)]
+
+
+def sph_grid_count() -> int:
+    sph_execute(np.zeros((0, 16), np.float32), [1, 1, 1], 0)
+    return int(lib().so_grid_count())

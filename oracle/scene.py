@@ -82,3 +82,30 @@ def lattice(n_per_axis: int, origin: float, spacing: float, jitter: float, seed:
     out = np.zeros((n, PARTICLE_FLOATS), dtype=np.float32)
     out[:, 0:3] = pos.astype(np.float32)
     return out
+
+
+def sph_dambreak(init_half_box, num_particles: int, seed: int) -> np.ndarray:
+    """SPHSimulator.initDambreak (sph/sph.ts:357-381) with Math.random ->
+    SplitMix64(seed): 64-byte records (n, 16) float32."""
+    rng = SplitMix64(seed)
+    hx, hy, hz = (float(h) for h in init_half_box)
+    step = 0.5 * 0.07
+    rows = []
+    y = -hy * 0.95
+    while len(rows) < num_particles:
+        before = len(rows)
+        x = -0.95 * hx
+        while x < 0.95 * hx and len(rows) < num_particles:
+            z = -0.95 * hz
+            while z < 0 * hz and len(rows) < num_particles:
+                j = 0.001 * rng.random()
+                rows.append((x + j, y + j, z + j))
+                z += step
+            x += step
+        if len(rows) == before:
+            break
+        y += step
+    out = np.zeros((len(rows), 16), np.float32)
+    if rows:
+        out[:, 0:3] = np.array(rows, dtype=np.float64).astype(np.float32)
+    return out

@@ -11,9 +11,10 @@ from .mlsmpm import (MLSMPMAdjoint, MLSMPMBatch, MLSMPMSimulator, MPMError, Grid
                      batch_scenes, centroid_loss, default_params, probe_conversions, probe_packed,
                      scene_dambreak, scene_desc, scene_lattice)
 
-from . import inverse, render
+from . import inverse, render, sph
+from .sph import SPHSimulator, sph_scene_dambreak
 from .render import FluidRenderer, camera_uniforms
 
-__all__ = ["FluidRenderer", "camera_uniforms", "render", "MLSMPMSimulator", "MLSMPMBatch", "MLSMPMAdjoint", "centroid_loss", "inverse",
+__all__ = ["SPHSimulator", "sph_scene_dambreak", "sph", "FluidRenderer", "camera_uniforms", "render", "MLSMPMSimulator", "MLSMPMBatch", "MLSMPMAdjoint", "centroid_loss", "inverse",
            "MPMError", "GridCapacityError", "default_params", "scene_dambreak", "scene_lattice", "scene_desc", "batch_scenes", "probe_conversions",
            "probe_packed", "build", "_lib"]

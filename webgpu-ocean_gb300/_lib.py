@@ -180,6 +180,18 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "mpm_renderer_execute": (i32, [vp, vp, i32, ctypes.POINTER(RenderUniforms), vp]),
         "mpm_renderer_download": (i32, [vp, i32, vp]),
         "mpm_renderer_color_device_ptr": (vp, [vp]),
+        "mpm_sph_create": (i32, [i32, f32, vp, ctypes.c_size_t, ctypes.POINTER(vp)]),
+        "mpm_sph_destroy": (i32, [vp]),
+        "mpm_sph_reset_dambreak": (i32, [vp, i32, dp, ctypes.c_uint64]),
+        "mpm_sph_upload": (i32, [vp, fp, i32, fp]),
+        "mpm_sph_step": (i32, [vp, i32, vp]),
+        "mpm_sph_set_real_box": (i32, [vp, fp]),
+        "mpm_sph_num_particles": (i32, [vp]),
+        "mpm_sph_grid_count": (i64, [vp]),
+        "mpm_sph_posvel_device_ptr": (vp, [vp]),
+        "mpm_sph_download_particles": (i32, [vp, fp]),
+        "mpm_sph_download_posvel": (i32, [vp, fp]),
+        "mpm_sph_scene_dambreak": (i32, [fp, i32, dp, ctypes.c_uint64]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -25,7 +25,7 @@ REPO = os.path.dirname(HERE)
 INCLUDE = os.path.join(REPO, "include")
 
 SOURCES = ["capi.cu", "kernels_dispatch.cu", "kernels_sorted.cu", "profiler.cu", "noalloc.cu",
-           "adjoint.cu", "render.cu"]
+           "adjoint.cu", "render.cu", "sph.cu"]
 HEADERS = ["mpm_math.cuh", "mpm_math_x2.cuh", "mpm_internal.h", "sorted_engine.h", "adjoint.h",
            "render_math.cuh"]
 
