@@ -431,6 +431,32 @@ def measure_render(pkg, torch, frames: int = 10) -> dict:
     return out
 
 
+def measure_sph(pkg, torch, frames: int = 50) -> dict:
+    """SPH solver: particle-substeps/s at the reference's largest UI setting
+    (40,000 particles, half box 1.4 x 2.0 x 1.4, main.ts:130-131) and at
+    400,000 particles (half box 1.9 x 2.0 x 1.9), after 20 frames."""
+    out = {}
+    for name, n, half in (("ui_max_40k", 40000, [1.4, 2.0, 1.4]),
+                          ("400k", 400000, [1.9, 2.0, 1.9])):
+        sim = pkg.SPHSimulator(None, None, 0.08, maxParticles=n)
+        sim.reset(n, half)
+        stream = torch.cuda.current_stream()
+        for _ in range(20):
+            sim.execute(stream)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(frames):
+            sim.execute(stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / frames
+        out[name] = {"particles": sim.numParticles, "ms_per_frame": ms,
+                     "particle_substeps_per_s": sim.numParticles * 2 / (ms / 1e3)}
+        sim.close()
+    out["timing"] = f"CUDA events around {frames} frames (2 substeps each) after 20"
+    return out
+
+
 def run_only(which: str) -> None:
     import torch
     import __graft_entry__ as entry
@@ -442,6 +468,8 @@ def run_only(which: str) -> None:
         out = measure_adjoint(pkg, torch)
     elif which == "render":
         out = measure_render(pkg, torch)
+    elif which == "sph":
+        out = measure_sph(pkg, torch)
     else:
         out = measure_inverse(pkg)
     print(json.dumps({"only": which, which: out}), flush=True)
@@ -577,6 +605,7 @@ def run_ours(args) -> None:
     adjoint = None if args.skip_adjoint else measure_adjoint(pkg, torch)
     inverse = None if args.skip_adjoint else measure_inverse(pkg)
     render = None if args.skip_batched else measure_render(pkg, torch)
+    sph = None if args.skip_batched else measure_sph(pkg, torch)
 
     # --- bit-exactness self-check: sorted engine vs dispatch engine -------
     outs = []
@@ -628,6 +657,7 @@ def run_ours(args) -> None:
         "adjoint": adjoint,
         "inverse_problem": inverse,
         "render": render,
+        "sph": sph,
         "parity": {"grid_bit_exact_vs_dispatch_engine": grid_exact,
                    "particles_bit_exact_vs_dispatch_engine": parts_exact, "steps": 3},
     }
@@ -647,7 +677,7 @@ def main():
                     help="leave out the batched-scenes measurement")
     ap.add_argument("--skip-adjoint", action="store_true",
                     help="leave out the adjoint and inverse-problem measurements")
-    ap.add_argument("--only", choices=["batched", "adjoint", "inverse", "render"],
+    ap.add_argument("--only", choices=["batched", "adjoint", "inverse", "render", "sph"],
                     help="run one side measurement alone and print its JSON (profiling)")
     ap.add_argument("--quick", action="store_true",
                     help="time the device-resident steps only (for profiler captures)")
