@@ -81,8 +81,10 @@ constexpr int kMaxTaskCap = 1 << 30;
 #ifndef MPM_G2P_MIN_BLOCKS
 #define MPM_G2P_MIN_BLOCKS (1024 / MPM_TASK_THREADS)
 #endif
+// k_p2g2 at 4 CTAs/SM (64 registers, some spilled to L1) measured ~5 %
+// faster than at 3 on the 1M dam-break, early and late in the run.
 #ifndef MPM_P2G2_MIN_BLOCKS
-#define MPM_P2G2_MIN_BLOCKS (768 / MPM_TASK_THREADS)
+#define MPM_P2G2_MIN_BLOCKS (1024 / MPM_TASK_THREADS)
 #endif
 // 1: arena stage bodies use packed f32x2 products (mpm_math_x2.cuh).
 #ifndef MPM_PACKED_MATH
