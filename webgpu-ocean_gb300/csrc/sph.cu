@@ -7,7 +7,7 @@
 // Per substep (two per execute(), sph.ts:325-355):
 //   k_sph_bin       cell of every particle (the grid's fixed [-2, 2]^3
 //                   domain plus a sentinel), per-cell counts
-//   k_sph_scan      exclusive prefix sum of the counts
+//   k_sph_blocksum, k_sph_scan   exclusive prefix sum of the counts
 //   k_sph_scatter   particle order by cell; each cell's run sorted by
 //                   particle index (k_sph_cellsort)
 //   k_sph_gather    sorted copies of positions and velocities
@@ -97,24 +97,20 @@ __global__ void k_sph_bin(float4* __restrict__ P, float4* __restrict__ V, float4
     if (!in) F[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
-// Exclusive scan of count[0 .. m) into start[0 .. m]; one CTA.
+// Exclusive scan of count[0 .. m) into start[0 .. m] in two passes: per-CTA
+// sums of kScan counts, then each CTA scans its own counts after adding the
+// sums of the CTAs before it (at most a few hundred).
 constexpr int kScan = 1024;
-__global__ void __launch_bounds__(kScan) k_sph_scan(const unsigned* __restrict__ count,
-                                                    unsigned* __restrict__ start, int m) {
-    __shared__ unsigned s_w[32];
-    const int per = (m + kScan - 1) / kScan;
-    const int b = threadIdx.x * per, en = min(b + per, m);
-    unsigned sum = 0;
-    for (int k = b; k < en; ++k) sum += count[k];
-    // block exclusive scan of the per-thread sums
+
+__device__ __forceinline__ unsigned block_exclusive(unsigned x, unsigned* s_w, unsigned& total) {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    unsigned x = sum;
+    unsigned v = x;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-        if ((int)lane >= o) x += y;
+        const unsigned y = __shfl_up_sync(0xffffffffu, v, o);
+        if ((int)lane >= o) v += y;
     }
-    if (lane == 31) s_w[warp] = x;
+    if (lane == 31) s_w[warp] = v;
     __syncthreads();
     if (warp == 0) {
         unsigned w = s_w[lane];
@@ -126,12 +122,38 @@ __global__ void __launch_bounds__(kScan) k_sph_scan(const unsigned* __restrict__
         s_w[lane] = w;
     }
     __syncthreads();
-    unsigned run = x - sum + (warp ? s_w[warp - 1] : 0u);
-    for (int k = b; k < en; ++k) {
-        start[k] = run;
-        run += count[k];
-    }
-    if (threadIdx.x == kScan - 1) start[m] = s_w[31];
+    total = s_w[31];
+    return v - x + (warp ? s_w[warp - 1] : 0u);
+}
+
+__global__ void __launch_bounds__(kScan) k_sph_blocksum(const unsigned* __restrict__ count, int m,
+                                                        unsigned* __restrict__ sums) {
+    __shared__ unsigned s_w[32];
+    const int k = blockIdx.x * kScan + threadIdx.x;
+    unsigned total;
+    block_exclusive(k < m ? count[k] : 0u, s_w, total);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScan) k_sph_scan(const unsigned* __restrict__ count,
+                                                    const unsigned* __restrict__ sums, int m,
+                                                    unsigned* __restrict__ start) {
+    __shared__ unsigned s_w[32];
+    __shared__ unsigned s_pre;
+    // sums of the CTAs before this one
+    unsigned pre = 0;
+    for (int b = threadIdx.x; b < (int)blockIdx.x; b += kScan) pre += sums[b];
+    unsigned tp;
+    block_exclusive(pre, s_w, tp);
+    if (threadIdx.x == 0) s_pre = tp;
+    __syncthreads();
+    const unsigned base = s_pre;
+    const int k = blockIdx.x * kScan + threadIdx.x;
+    const unsigned c = k < m ? count[k] : 0u;
+    unsigned tot;
+    const unsigned ex = block_exclusive(c, s_w, tot);
+    if (k < m) start[k] = base + ex;
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) start[m] = base + tot;
 }
 
 __global__ void k_sph_scatter(const int* __restrict__ cell_of, const unsigned* __restrict__ rank,
@@ -373,6 +395,7 @@ struct mpm_sph {
     bool posvel_owned = false;
     int* cell_of = nullptr;
     unsigned *count = nullptr, *start = nullptr, *rank = nullptr, *order = nullptr;
+    unsigned* sums = nullptr;  // per-CTA count sums of the scan
 };
 
 namespace {
@@ -381,7 +404,7 @@ void free_sph(mpm_sph* s) {
     cudaFree(s->P); cudaFree(s->V); cudaFree(s->F); cudaFree(s->SP); cudaFree(s->SV);
     if (s->posvel_owned) cudaFree(s->posvel);
     cudaFree(s->cell_of); cudaFree(s->count); cudaFree(s->start); cudaFree(s->rank);
-    cudaFree(s->order);
+    cudaFree(s->order); cudaFree(s->sums);
     delete s;
 }
 
@@ -458,6 +481,7 @@ int mpm_sph_create(int max_particles, float render_diameter, void* posvel_device
     if (err == cudaSuccess) err = cudaMalloc(&s->order, 4 * np);
     if (err == cudaSuccess) err = cudaMalloc(&s->count, 4 * ((size_t)s->e.total + 1));
     if (err == cudaSuccess) err = cudaMalloc(&s->start, 4 * ((size_t)s->e.total + 1));
+    if (err == cudaSuccess) err = cudaMalloc(&s->sums, 4 * ((size_t)s->e.total / kScan + 2));
     if (err != cudaSuccess) {
         const int rc = cuda_fail(err, "mpm_sph_create");
         free_sph(s);
@@ -551,7 +575,9 @@ int mpm_sph_step(mpm_sph* s, int substeps, void* stream) {
     for (int k = 0; k < substeps; ++k) {
         cudaMemsetAsync(s->count, 0, 4 * ((size_t)e.total + 1), st);
         k_sph_bin<<<pb, 256, 0, st>>>(s->P, s->V, s->F, n, e, s->cell_of, s->count, s->rank);
-        k_sph_scan<<<1, kScan, 0, st>>>(s->count, s->start, e.total);
+        const int sb = (e.total + kScan - 1) / kScan;
+        k_sph_blocksum<<<sb, kScan, 0, st>>>(s->count, e.total, s->sums);
+        k_sph_scan<<<sb, kScan, 0, st>>>(s->count, s->sums, e.total, s->start);
         k_sph_scatter<<<pb, 256, 0, st>>>(s->cell_of, s->rank, s->start, n, s->order);
         k_sph_cellsort<<<cb, 256, 0, st>>>(s->start, e.total, s->order);
         // sorted slots: start[total] of them (read on the device); launched
