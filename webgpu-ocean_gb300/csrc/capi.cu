@@ -177,7 +177,7 @@ struct mpm_sim {
     unsigned long long* counters = nullptr;  // [0] out-of-range, [1] non-finite scratch
 
     float gravity[3] = {0.0f, -0.3f, 0.0f};  // updateGrid.wgsl:34
-    bool graph = false;
+    bool graph = true;
     int engine = MPM_ENGINE_DISPATCH;
     SortedEngine* sorted = nullptr;
     cudaStream_t internal = nullptr;

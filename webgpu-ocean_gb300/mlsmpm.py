@@ -208,7 +208,8 @@ class MLSMPMSimulator:
         _check(self._lib.mpm_set_gravity(self._handle, g), "setGravity")
 
     def setGraph(self, enable: bool) -> None:
-        """Run execute()'s substeps as one CUDA graph (sorted engine)."""
+        """Run execute()'s substeps as one CUDA graph (sorted engine; on by
+        default)."""
         _check(self._lib.mpm_set_graph(self._handle, int(bool(enable))), "setGraph")
 
     @property
