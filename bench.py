@@ -360,6 +360,39 @@ def measure_adjoint(pkg, torch, repeats: int = 3) -> dict:
         out[tape] = {"forward_ms": 1e3 * fwd, "backward_ms": 1e3 * bwd,
                      "fwd_plus_adj_over_own_forward": (fwd + bwd) / fwd,
                      "fwd_plus_adj_over_plain_forward": (fwd + bwd) / best}
+    # the inverse problem's scale: 64 scenes, 1.5M particles, 100 substeps
+    descs, recs64, _ = pkg.inverse.inverse_scenes(64, seed=BATCH_SEED)
+    b = pkg.MLSMPMBatch(descs, recs64)
+    b.step(100)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.step(100)
+    torch.cuda.synchronize()
+    plain64 = time.perf_counter() - t0
+    b.close()
+    adj = pkg.MLSMPMAdjoint(descs, 100, 20, tape="fixed")
+    seed = np.zeros((len(recs64), 20), np.float32)
+    seed[:, 0:3] = 1e-6
+    fwd = bwd = None
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        adj.forward(recs64, 100)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        adj.backward({100: seed})
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        fwd = t1 - t0 if fwd is None else min(fwd, t1 - t0)
+        bwd = t2 - t1 if bwd is None else min(bwd, t2 - t1)
+    adj.close()
+    out["batch_64_scenes"] = {
+        "particles": int(len(recs64)), "substeps": 100, "tape": "fixed",
+        "plain_batched_forward_ms": 1e3 * plain64,
+        "forward_ms": 1e3 * fwd, "backward_ms": 1e3 * bwd,
+        "fwd_plus_adj_over_own_forward": (fwd + bwd) / fwd,
+        "fwd_plus_adj_over_plain_forward": (fwd + bwd) / plain64,
+        "note": "forward_ms includes uploading the initial state from host memory"}
     out["timing"] = ("host wall clock around synchronised calls, best of "
                      f"{repeats}; plain forward = MLSMPMSimulator.execute(substeps=200), "
                      "CUDA graph, autotuned task size")
