@@ -340,8 +340,9 @@ def measure_adjoint(pkg, torch, repeats: int = 3) -> dict:
         best = dt if best is None else min(best, dt)
     out["plain_forward_ms"] = 1e3 * best
     sim.close()
-    for tape in ("fixed", "fp64"):
-        adj = pkg.MLSMPMAdjoint([pkg.scene_desc(len(recs), box)], T, 20, tape=tape)
+    for name, tape, every in (("fixed", "fixed", 20), ("fp64", "fp64", 20),
+                              ("fixed_full_tape", "fixed", 1)):
+        adj = pkg.MLSMPMAdjoint([pkg.scene_desc(len(recs), box)], T, every, tape=tape)
         fwd = bwd = None
         for _ in range(repeats):
             torch.cuda.synchronize()
@@ -357,7 +358,7 @@ def measure_adjoint(pkg, torch, repeats: int = 3) -> dict:
             fwd = t1 - t0 if fwd is None else min(fwd, t1 - t0)
             bwd = t3 - t2 if bwd is None else min(bwd, t3 - t2)
         adj.close()
-        out[tape] = {"forward_ms": 1e3 * fwd, "backward_ms": 1e3 * bwd,
+        out[name] = {"checkpoint_every": every, "forward_ms": 1e3 * fwd, "backward_ms": 1e3 * bwd,
                      "fwd_plus_adj_over_own_forward": (fwd + bwd) / fwd,
                      "fwd_plus_adj_over_plain_forward": (fwd + bwd) / best}
     # the inverse problem's scale: 64 scenes, 1.5M particles, 100 substeps

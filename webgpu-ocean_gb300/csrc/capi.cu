@@ -1087,6 +1087,7 @@ struct mpm_adjoint {
     std::vector<Particles> ckpt;     // states after 0, every, 2*every, ..., T substeps
     std::vector<Particles> seg;      // states inside a segment (seg[0] unused)
     int4* gtape = nullptr;           // every x ncells: updated grids of a segment
+                                     // (max_substeps x ncells for a full tape)
     // FP64 tape
     std::vector<double*> ckpt64;
     std::vector<double*> seg64;
@@ -1240,6 +1241,11 @@ void free_tapes(mpm_adjoint* a) {
     a->gtape64 = nullptr;
 }
 
+// checkpoint_every == 1 keeps every substep's state and updated grid (a full
+// tape): the backward then recomputes nothing.
+bool full_tape(const mpm_adjoint* a) { return a->every == 1; }
+int tape_grids(const mpm_adjoint* a) { return full_tape(a) ? a->max_substeps : a->every; }
+
 // Allocates the buffers of the selected tape (and frees the other's).
 cudaError_t alloc_tape(mpm_adjoint* a) {
     free_tapes(a);
@@ -1252,7 +1258,7 @@ cudaError_t alloc_tape(mpm_adjoint* a) {
         a->seg.resize((size_t)a->every);
         for (int i = 1; i < a->every && e == cudaSuccess; ++i)
             e = alloc_particles(a->seg[(size_t)i], np);
-        if (e == cudaSuccess) e = cudaMalloc(&a->gtape, sizeof(int4) * (size_t)a->every * nc);
+        if (e == cudaSuccess) e = cudaMalloc(&a->gtape, sizeof(int4) * (size_t)tape_grids(a) * nc);
     } else {
         a->ckpt64.assign((size_t)a->nck, nullptr);
         for (int i = 0; i < a->nck && e == cudaSuccess; ++i)
@@ -1262,7 +1268,8 @@ cudaError_t alloc_tape(mpm_adjoint* a) {
             e = cudaMalloc(&a->seg64[(size_t)i], sizeof(double) * kRec64 * np);
         for (int i = 0; i < 2 && e == cudaSuccess; ++i)
             e = cudaMalloc(&a->scratch64[i], sizeof(double) * kRec64 * np);
-        if (e == cudaSuccess) e = cudaMalloc(&a->gtape64, sizeof(double4) * (size_t)a->every * nc);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&a->gtape64, sizeof(double4) * (size_t)tape_grids(a) * nc);
     }
     return e;
 }
@@ -1405,7 +1412,8 @@ int mpm_forward_ckpt(mpm_adjoint* a, const float* init, int substeps, void* stre
         for (int t = 0; t < substeps; ++t) {
             const int slot = ckpt_slot(a, t + 1, substeps);
             double* dst = slot >= 0 ? a->ckpt64[(size_t)slot] : a->scratch64[t & 1];
-            launch_substep64(cur, a->gtape64, dst, a->scenes_d, S, a->pscene_d, n, a->ncells, st);
+            double4* G = a->gtape64 + (full_tape(a) ? (size_t)t * (size_t)a->ncells : 0);
+            launch_substep64(cur, G, dst, a->scenes_d, S, a->pscene_d, n, a->ncells, st);
             cur = dst;
         }
     } else {
@@ -1418,6 +1426,10 @@ int mpm_forward_ckpt(mpm_adjoint* a, const float* init, int substeps, void* stre
                             &b->prof, b->graph) != 0)
                 return fail(MPM_E_CUDA, std::string("forward: ") + sorted_error());
             b->stepped = true;
+            if (full_tape(a) &&
+                sorted_export_all(b->sorted, a->gtape + (size_t)t * (size_t)a->ncells, st,
+                                  &b->prof) != 0)
+                return fail(MPM_E_CUDA, std::string("forward: ") + sorted_error());
             t += ns;
             batch_canonical_to(b, a->ckpt[(size_t)ckpt_slot(a, t, substeps)], st);
         }
@@ -1482,7 +1494,10 @@ int mpm_backward(mpm_adjoint* a, const float* seeds, const int* seed_steps, int 
         const int t0 = j * a->every;
         const int t1 = t0 + a->every < a->T ? t0 + a->every : a->T;
         // recompute the segment: states and updated grids of every substep
-        if (f64) {
+        // (a full tape kept them all)
+        const size_t g0 = full_tape(a) ? (size_t)t0 : 0;  // tape grid of substep t0
+        if (full_tape(a)) {
+        } else if (f64) {
             const double* curS = a->ckpt64[(size_t)j];
             for (int t = t0; t < t1; ++t) {
                 double* dst = t + 1 < t1 ? a->seg64[(size_t)(t + 1 - t0)] : a->scratch64[0];
@@ -1510,12 +1525,12 @@ int mpm_backward(mpm_adjoint* a, const float* seeds, const int* seed_steps, int 
         for (int t = t1 - 1; t >= t0; --t) {
             if (f64) {
                 const double* Sx = t == t0 ? a->ckpt64[(size_t)j] : a->seg64[(size_t)(t - t0)];
-                launch_adjoint_substep64(Sx, a->gtape64 + (size_t)(t - t0) * nc, a->adj[cur],
+                launch_adjoint_substep64(Sx, a->gtape64 + (g0 + (size_t)(t - t0)) * nc, a->adj[cur],
                                          a->adj[cur ^ 1], a->gadj, a->scenes_d, S, a->pscene_d, n,
                                          a->ncells, a->pgrad_d, st);
             } else {
                 const Particles& Sx = t == t0 ? a->ckpt[(size_t)j] : a->seg[(size_t)(t - t0)];
-                launch_adjoint_substep(Sx, a->gtape + (size_t)(t - t0) * nc, a->adj[cur],
+                launch_adjoint_substep(Sx, a->gtape + (g0 + (size_t)(t - t0)) * nc, a->adj[cur],
                                        a->adj[cur ^ 1], a->gadj, a->scenes_d, S, a->pscene_d, n,
                                        a->ncells, a->pgrad_d, st);
             }
