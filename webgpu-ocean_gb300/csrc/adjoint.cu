@@ -10,14 +10,19 @@
 // order on the substep's input state S_t and its updated grid G_t (both
 // recorded by a forward recompute from a checkpoint):
 //
-//   k_adj_g2p     particle-parallel; the g2p gather becomes a float scatter
-//                 of the grid-velocity adjoint (3 atomics per stencil cell)
+//   k_adj_g2p     particle-parallel; the g2p gather becomes a scatter of
+//                 the grid-velocity adjoint (one float4 reduction per
+//                 stencil cell)
 //   k_adj_update  cell-parallel, elementwise: velocity adjoint -> momentum
 //                 and mass adjoints
 //   k_adj_p2g2    particle-parallel gather of the momentum adjoint through
 //                 the stress term; the density gather becomes a scatter of
 //                 the density adjoint onto the mass adjoint
 //   k_adj_p2g1    particle-parallel gather of the mass and momentum adjoints
+//
+// Large batches run the particle kernels in the order of a per-substep
+// spatial sort (k_adj_bin / k_adj_place / k_adj_perm), one thread per
+// particle; small ones in particle order, three threads per particle.
 //
 // Two tapes: the fixed-point solver's own (S_t as f32 records, G_t as the
 // i32 grid) or an FP64 integration of the continuous model on the GPU
@@ -63,30 +68,36 @@ __device__ __forceinline__ void make_sten(const float x[3], Sten& s) {
     }
 }
 
-// Stencil cell (gx, gy, gz): its weight, weight gradient, dist and flat index
-// (false when outside [0, grid_count)).
+// Stencil cell (gx, gy, gz) of a particle: its weight, weight gradient and
+// dist.
 struct Node {
     float w;
     float gw[3];
     float dist[3];
-    int idx;
 };
 
-__device__ __forceinline__ bool node(const Sten& s, const float x[3], int gx, int gy, int gz,
-                                     const SimConsts& k, Node& nd) {
+__device__ __forceinline__ float node_weight(const Sten& s, int gx, int gy, int gz) {
+    return (s.w[0][gx] * s.w[1][gy]) * s.w[2][gz];
+}
+
+__device__ __forceinline__ void node_geom(const Sten& s, const float x[3], int gx, int gy, int gz,
+                                          Node& nd) {
     const float wx = s.w[0][gx], wy = s.w[1][gy], wz = s.w[2][gz];
     nd.w = (wx * wy) * wz;
     nd.gw[0] = (s.dw[0][gx] * wy) * wz;
     nd.gw[1] = (wx * s.dw[1][gy]) * wz;
     nd.gw[2] = (wx * wy) * s.dw[2][gz];
-    const float cx = s.cf[0] + (float)gx - 1.0f;
-    const float cy = s.cf[1] + (float)gy - 1.0f;
-    const float cz = s.cf[2] + (float)gz - 1.0f;
-    nd.dist[0] = (cx + 0.5f) - x[0];
-    nd.dist[1] = (cy + 0.5f) - x[1];
-    nd.dist[2] = (cz + 0.5f) - x[2];
-    nd.idx = flat_index(cx, cy, cz, k.Y, k.Z);
-    return (unsigned)nd.idx < (unsigned)k.grid_count;
+    nd.dist[0] = ((s.cf[0] + (float)gx - 1.0f) + 0.5f) - x[0];
+    nd.dist[1] = ((s.cf[1] + (float)gy - 1.0f) + 0.5f) - x[1];
+    nd.dist[2] = ((s.cf[2] + (float)gz - 1.0f) + 0.5f) - x[2];
+}
+
+// Flat index of the stencil cell in the scene's grid, -1 where the forward
+// dropped it (outside [0, grid_count)).
+__device__ __forceinline__ int node_index(const Sten& s, int gx, int gy, int gz, const SimConsts& k) {
+    const int idx = flat_index(s.cf[0] + (float)gx - 1.0f, s.cf[1] + (float)gy - 1.0f,
+                               s.cf[2] + (float)gz - 1.0f, k.Y, k.Z);
+    return (unsigned)idx < (unsigned)k.grid_count ? idx : -1;
 }
 
 struct Rec {
@@ -188,102 +199,253 @@ __device__ __forceinline__ void add_param_grads(double* pg, int scene, bool acti
     }
 }
 
-// Lanes per particle in the particle-parallel adjoint kernels: lane q of a
-// group of kLanes consecutive lanes takes stencil cells q, q + kLanes, ...
-// of the 27, and the group sums its partial results with shuffles.  Small
-// scenes then still fill the GPU.
-constexpr int kLanes = 4;
-
-template <class R, int N>
-__device__ __forceinline__ void group_sum(R (&v)[N]) {
-#pragma unroll
-    for (int o = 1; o < kLanes; o <<= 1)
-#pragma unroll
-        for (int j = 0; j < N; ++j) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
+// ---------------------------------------------------------------------------
+// Spatial sort of one substep's particles.  The particle-parallel kernels
+// below walk the particles in the order of the brick (4^3 cells) of their
+// base cell floor(x), so that the threads of a warp gather and scatter
+// neighbouring cells: their loads hit L1 and their reductions land on a few
+// L2 lines.  Particles whose stencil leaves the grid interior go to one
+// extra bin at the end.
+// ---------------------------------------------------------------------------
+template <class Tape>
+__global__ void __launch_bounds__(kThreads)
+    k_adj_bin(Tape tp, const AdjScene* __restrict__ scenes, const int* __restrict__ pscene, int n,
+              AdjSort so) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const AdjScene& sc = scenes[pscene[i]];
+    const SimConsts& k = sc.k;
+    float x[3];
+    tp.pos(i, x);
+    int bin = so.nbins - 1;
+    if (x[0] >= 1.0f && x[1] >= 1.0f && x[2] >= 1.0f && x[0] < 1.0e9f && x[1] < 1.0e9f &&
+        x[2] < 1.0e9f) {
+        const int cx = (int)floorf(x[0]), cy = (int)floorf(x[1]), cz = (int)floorf(x[2]);
+        const long long top = ((long long)(cx + 1) * k.Y + (cy + 1)) * k.Z + (cz + 1);
+        if (cy + 1 < k.Y && cz + 1 < k.Z && top < k.grid_count)
+            bin = sc.bbase + ((cx >> 2) * sc.BY + (cy >> 2)) * sc.BZ + (cz >> 2);
+    }
+    so.key_rank[i] = make_int2(bin, atomicAdd(so.bin_count + bin, 1));
 }
+
+// One thread per bin: the bin's first slot in the sorted order (bins are
+// placed in whatever order the warp-wide allocations from the counter come;
+// only their contiguity matters).
+__global__ void __launch_bounds__(kThreads) k_adj_place(AdjSort so) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = b < so.nbins ? so.bin_count[b] : 0;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int cs = c;  // inclusive warp scan
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(full, cs, o);
+        if (lane >= o) cs += u;
+    }
+    int base = 0;
+    if (lane == 31 && cs > 0) base = atomicAdd(so.placed, cs);
+    base = __shfl_sync(full, base, 31);
+    if (c > 0) so.bin_first[b] = base + cs - c;
+}
+
+__global__ void __launch_bounds__(kThreads) k_adj_perm(AdjSort so, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int2 kr = so.key_rank[i];
+    so.perm[so.bin_first[kr.x] + kr.y] = i;
+}
+
+// ---------------------------------------------------------------------------
+// Particle-parallel adjoint kernels.  L lanes per particle: L = 1 runs the
+// whole 27-cell stencil in one thread; L = 3 gives lane q the nine cells of
+// x-slab gx = q (groups of three lanes, ten particles per warp, lanes 30-31
+// idle), for batches too small to fill the GPU one thread per particle.  A
+// group sums its partial results in lane order, so every lane holds the same
+// totals.  Each particle makes one gather pass over its stencil and at most
+// one scatter pass; terms that depend on a gathered total enter after the
+// gather by linearity.
+// ---------------------------------------------------------------------------
+template <int L>
+struct Lanes {
+    int q;        // this lane's slab (L = 3) or 0
+    int j;        // particle slot in the sorted order
+    bool active;  // a real particle (idle lanes repeat the last one)
+};
+
+template <int L>
+__device__ __forceinline__ Lanes<L> lanes_of(int n) {
+    Lanes<L> g;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (L == 1) {
+        g.q = 0;
+        g.j = t;
+        g.active = t < n;
+    } else {
+        const int lane = threadIdx.x & 31;
+        g.q = lane % 3;
+        g.j = (t >> 5) * 10 + lane / 3;
+        g.active = lane < 30 && g.j < n;
+    }
+    if (!g.active) g.j = n - 1;
+    return g;
+}
+
+template <int L>
+inline int lane_blocks(long long n) {
+    const long long per = L == 1 ? kThreads : (kThreads / 32) * 10;
+    return (int)((n + per - 1) / per);
+}
+
+// Sum over the lanes of a group, in lane order.
+template <int L, int N>
+__device__ __forceinline__ void lane_sum(float (&v)[N]) {
+    if (L == 1) return;
+    const int base = (threadIdx.x & 31) / 3 * 3;
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        const float a = __shfl_sync(0xffffffffu, v[j], base);
+        const float b = __shfl_sync(0xffffffffu, v[j], base + 1);
+        const float c = __shfl_sync(0xffffffffu, v[j], base + 2);
+        v[j] = (a + b) + c;
+    }
+}
+
+// The x-axis factors of slab gx of a particle's stencil.
+struct Slab {
+    int gx;
+    float w, dw;
+};
+
+__device__ __forceinline__ Slab slab(const Sten& st, int gx) {
+    Slab s;
+    s.gx = gx;
+    s.w = gx == 0 ? st.w[0][0] : (gx == 1 ? st.w[0][1] : st.w[0][2]);
+    s.dw = gx == 0 ? st.dw[0][0] : (gx == 1 ? st.dw[0][1] : st.dw[0][2]);
+    return s;
+}
+
+__device__ __forceinline__ void slab_node(const Sten& s, const float x[3], const Slab& sx, int gy,
+                                          int gz, Node& nd) {
+    const float wx = sx.w, wy = s.w[1][gy], wz = s.w[2][gz];
+    nd.w = (wx * wy) * wz;
+    nd.gw[0] = (sx.dw * wy) * wz;
+    nd.gw[1] = (wx * s.dw[1][gy]) * wz;
+    nd.gw[2] = (wx * wy) * s.dw[2][gz];
+    nd.dist[0] = ((s.cf[0] + (float)sx.gx - 1.0f) + 0.5f) - x[0];
+    nd.dist[1] = ((s.cf[1] + (float)gy - 1.0f) + 0.5f) - x[1];
+    nd.dist[2] = ((s.cf[2] + (float)gz - 1.0f) + 0.5f) - x[2];
+}
+
+// The slabs lane q visits: all three (L = 1) or its own.
+template <int L>
+__device__ __forceinline__ int slab_count() { return L == 1 ? 3 : 1; }
+
+template <int L>
+__device__ __forceinline__ int slab_gx(int s, int q) { return L == 1 ? s : q; }
 
 // ---------------------------------------------------------------------------
 // g2p backward (g2p.wgsl:26-92).  Aout: adjoint of S_{t+1}; writes the g2p
 // part of the position adjoint of S_t into Anew (velocity and C adjoints
-// zeroed) and scatters the grid-velocity adjoint into gadj.xyz.
+// zeroed) and scatters the grid-velocity adjoint into gadj.xyz.  With
+// u_n = Cbar v_n (rows of the C adjoint against the cell velocity) and
+// q_n = vgbar + 4 Cbar^T d_n, the position adjoint
+//   sum_n grad w_n (v_n . q_n) - 4 w_n u_n  =  G vgbar + H,
+// G = sum_n grad w_n v_n^T, H = sum_n 4 grad w_n (d_n . u_n) - 4 w_n u_n.
 // ---------------------------------------------------------------------------
-template <class Tape>
+template <class Tape, int L>
 __global__ void __launch_bounds__(kThreads)
     k_adj_g2p(Tape tp, Particles Aout, Particles Anew, float4* __restrict__ gadj,
-              const AdjScene* __restrict__ scenes, const int* __restrict__ pscene, int n) {
-    const int gi = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = gi & (kLanes - 1);
-    const bool active = gi / kLanes < n;
-    const int i = active ? gi / kLanes : n - 1;
+              const AdjScene* __restrict__ scenes, const int* __restrict__ pscene,
+              const int* __restrict__ perm, int n) {
+    const Lanes<L> ln = lanes_of<L>(n);
+    const int i = perm ? perm[ln.j] : ln.j;
     const AdjScene& sc = scenes[pscene[i]];
     const SimConsts& k = sc.k;
-    const int lb = sc.lbase;
-    float4* ga = gadj + lb;
+    float4* ga = gadj + sc.lbase;
     float x[3];
     tp.pos(i, x);
     Sten st;
     make_sten(x, st);
-
-    float vg[3] = {0.0f, 0.0f, 0.0f};
-    for (int nn = lane; nn < 27; nn += kLanes) {
-        Node nd;
-        if (!node(st, x, nn / 9, (nn / 3) % 3, nn % 3, k, nd)) continue;
-        float vi[3];
-        tp.vel(lb + nd.idx, k.fm, vi);
-        vg[0] += nd.w * vi[0];
-        vg[1] += nd.w * vi[1];
-        vg[2] += nd.w * vi[2];
-    }
-    group_sum(vg);
-
     const Rec ao = load_rec(Aout, i);
+
+    float acc[15] = {};  // vg (3), G row-major (9), H (3)
+#pragma unroll
+    for (int s = 0; s < slab_count<L>(); ++s) {
+        const Slab sx = slab(st, slab_gx<L>(s, ln.q));
+#pragma unroll
+        for (int gy = 0; gy < 3; ++gy)
+#pragma unroll
+            for (int gz = 0; gz < 3; ++gz) {
+                const int c = node_index(st, sx.gx, gy, gz, k);
+                if (c < 0) continue;
+                float vi[3];
+                tp.vel(sc.lbase + c, k.fm, vi);
+                Node nd;
+                slab_node(st, x, sx, gy, gz, nd);
+                float u[3];
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                    u[j] = ao.C[j][0] * vi[0] + ao.C[j][1] * vi[1] + ao.C[j][2] * vi[2];
+                const float du = 4.0f * (nd.dist[0] * u[0] + nd.dist[1] * u[1] + nd.dist[2] * u[2]);
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    acc[a] += nd.w * vi[a];
+                    acc[12 + a] += nd.gw[a] * du - 4.0f * nd.w * u[a];
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) acc[3 + 3 * a + r] += nd.gw[a] * vi[r];
+                }
+            }
+    }
+    lane_sum<L>(acc);
+
     float xbar[3], vgbar[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const float xt = x[a] + vg[a] * k.dt;
+        const float vg = acc[a];
+        const float xt = x[a] + vg * k.dt;
         const float hiw = k.real_box[a] - 2.0f;
         const bool inside = xt >= 1.0f && xt <= hiw;
         const float xc = fminf(fmaxf(xt, 1.0f), hiw);
-        const float xn = xc + (vg[a] * k.dt) * 3.0f;
+        const float xn = xc + (vg * k.dt) * 3.0f;
         const float nw = (xn < 3.0f ? 1.0f : 0.0f) + (xn > k.real_box[a] - 4.0f ? 1.0f : 0.0f);
         const float xcbar = ao.x[a] - 0.3f * nw * ao.v[a];
         const float xtbar = inside ? xcbar : 0.0f;
         vgbar[a] = ao.v[a] * (1.0f - 0.9f * k.dt * nw) + k.dt * xtbar;
-        xbar[a] = lane == 0 ? xtbar : 0.0f;
+        xbar[a] = xtbar;
     }
+    if (!ln.active) return;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        xbar[a] += acc[3 + 3 * a] * vgbar[0] + acc[4 + 3 * a] * vgbar[1] + acc[5 + 3 * a] * vgbar[2] +
+                   acc[12 + a];
 
-    for (int nn = lane; nn < 27; nn += kLanes) {
-        Node nd;
-        if (!node(st, x, nn / 9, (nn / 3) % 3, nn % 3, k, nd)) continue;
-        float vi[3];
-        tp.vel(lb + nd.idx, k.fm, vi);
-        float q[3];
 #pragma unroll
-        for (int r = 0; r < 3; ++r)
-            q[r] = vgbar[r] + 4.0f * (ao.C[0][r] * nd.dist[0] + ao.C[1][r] * nd.dist[1] +
-                                      ao.C[2][r] * nd.dist[2]);
-        if (active) {
-            float* cell = reinterpret_cast<float*>(ga + nd.idx);
-            atomicAdd(cell + 0, nd.w * q[0]);
-            atomicAdd(cell + 1, nd.w * q[1]);
-            atomicAdd(cell + 2, nd.w * q[2]);
-        }
-        const float s = vi[0] * q[0] + vi[1] * q[1] + vi[2] * q[2];
+    for (int s = 0; s < slab_count<L>(); ++s) {
+        const Slab sx = slab(st, slab_gx<L>(s, ln.q));
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
-            xbar[a] += nd.gw[a] * s - 4.0f * nd.w *
-                                          (ao.C[a][0] * vi[0] + ao.C[a][1] * vi[1] +
-                                           ao.C[a][2] * vi[2]);
+        for (int gy = 0; gy < 3; ++gy)
+#pragma unroll
+            for (int gz = 0; gz < 3; ++gz) {
+                const int c = node_index(st, sx.gx, gy, gz, k);
+                if (c < 0) continue;
+                Node nd;
+                slab_node(st, x, sx, gy, gz, nd);
+                float q[3];
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+                    q[r] = nd.w * (vgbar[r] + 4.0f * (ao.C[0][r] * nd.dist[0] + ao.C[1][r] * nd.dist[1] +
+                                                      ao.C[2][r] * nd.dist[2]));
+                atomicAdd(ga + c, make_float4(q[0], q[1], q[2], 0.0f));
+            }
     }
-    group_sum(xbar);
-
-    if (active && lane == 0) {
+    if (ln.q == 0) {
         Rec an{};
 #pragma unroll
         for (int a = 0; a < 3; ++a) an.x[a] = xbar[a];
         store_rec(Anew, i, an);
     }
 }
+
 
 // ---------------------------------------------------------------------------
 // updateGrid backward (updateGrid.wgsl:23-46), per cell of all scenes:
@@ -329,20 +491,25 @@ __global__ void __launch_bounds__(kThreads)
     gadj[j] = make_float4(mvbar[0], mvbar[1], mvbar[2], mbar);
 }
 
+
 // ---------------------------------------------------------------------------
 // p2g_2 backward (p2g_2.wgsl:30-94).  Accumulates into Anew (position and C
 // adjoints), the scene's stiffness / viscosity adjoints, and scatters the
-// density adjoint onto gadj.w.
+// density adjoint onto gadj.w.  The stress matrix T = beta sig,
+// beta = -4 V dt, sig = -p I + mu S (S the symmetric strain), depends on the
+// density being gathered, so T enters after the gather by linearity:
+//   sum_n grad w_n (g_n . T d_n) - w_n T^T g_n
+//     = beta (-p P1 + mu P2 + p Q - mu S Q)
+// with P1 = sum_n grad w_n (g_n . d_n), P2 = sum_n grad w_n (g_n . S d_n) and
+// Q = sum_n w_n g_n.
 // ---------------------------------------------------------------------------
-template <class Tape>
+template <class Tape, int L>
 __global__ void __launch_bounds__(kThreads)
     k_adj_p2g2(Tape tp, Particles Anew, float4* __restrict__ gadj,
-               const AdjScene* __restrict__ scenes, const int* __restrict__ pscene, int n,
-               double* __restrict__ pgrad) {
-    const int gi = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = gi & (kLanes - 1);
-    const bool active = gi / kLanes < n;
-    const int i = active ? gi / kLanes : n - 1;
+               const AdjScene* __restrict__ scenes, const int* __restrict__ pscene,
+               const int* __restrict__ perm, int n, double* __restrict__ pgrad) {
+    const Lanes<L> ln = lanes_of<L>(n);
+    const int i = perm ? perm[ln.j] : ln.j;
     const int scene = pscene[i];
     const AdjScene& sc = scenes[scene];
     const SimConsts& k = sc.k;
@@ -351,53 +518,69 @@ __global__ void __launch_bounds__(kThreads)
     const Rec p = tp.rec(i);
     Sten st;
     make_sten(p.x, st);
-    float rho[1] = {0.0f};
-    for (int nn = lane; nn < 27; nn += kLanes) {
-        Node nd;
-        if (!node(st, p.x, nn / 9, (nn / 3) % 3, nn % 3, k, nd)) continue;
-        rho[0] += tp.mass(lb + nd.idx, k.fm) * nd.w;
-    }
-    group_sum(rho);
-    const float V = 1.0f / rho[0];
-    const float r = rho[0] / k.rest_density;
-    const float r4 = (r * r) * (r * r);
-    const float pterm = k.stiffness * (r4 * r - 1.0f);
-    const float pres = fmaxf(pterm, 0.0f);
-    float T[3][3], sig[3][3], strain[3][3];  // [row][col]
+    float strain[3][3];  // [row][col], symmetric
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int b = 0; b < 3; ++b) {
-            strain[a][b] = p.C[b][a] + p.C[a][b];
-            sig[a][b] = (a == b ? -pres : 0.0f) + k.dynamic_viscosity * strain[a][b];
-            T[a][b] = -4.0f * V * k.dt * sig[a][b];
-        }
-    float acc[12] = {};  // Tb (row-major 9), then the position adjoint (3)
-    for (int nn = lane; nn < 27; nn += kLanes) {
-        Node nd;
-        if (!node(st, p.x, nn / 9, (nn / 3) % 3, nn % 3, k, nd)) continue;
-        const float4 g4 = ga[nd.idx];
-        const float g[3] = {g4.x, g4.y, g4.z};
-        float s = 0.0f;
+        for (int b = 0; b < 3; ++b) strain[a][b] = p.C[b][a] + p.C[a][b];
+
+    // rho (1), m grad w (3), sum w g d^T row-major (9), P1 (3), P2 (3), Q (3)
+    float acc[22] = {};
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const float td = T[a][0] * nd.dist[0] + T[a][1] * nd.dist[1] + T[a][2] * nd.dist[2];
-            s += g[a] * td;
+    for (int s = 0; s < slab_count<L>(); ++s) {
+        const Slab sx = slab(st, slab_gx<L>(s, ln.q));
 #pragma unroll
-            for (int b = 0; b < 3; ++b) acc[3 * a + b] += nd.w * g[a] * nd.dist[b];
-        }
+        for (int gy = 0; gy < 3; ++gy)
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
-            acc[9 + c] += nd.gw[c] * s - nd.w * (T[0][c] * g[0] + T[1][c] * g[1] + T[2][c] * g[2]);
+            for (int gz = 0; gz < 3; ++gz) {
+                const int c = node_index(st, sx.gx, gy, gz, k);
+                if (c < 0) continue;
+                const float4 g4 = ga[c];
+                const float g[3] = {g4.x, g4.y, g4.z};
+                const float m = tp.mass(lb + c, k.fm);
+                Node nd;
+                slab_node(st, p.x, sx, gy, gz, nd);
+                acc[0] += m * nd.w;
+                const float gd = g[0] * nd.dist[0] + g[1] * nd.dist[1] + g[2] * nd.dist[2];
+                float gsd = 0.0f;
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+                    gsd += g[a] * (strain[a][0] * nd.dist[0] + strain[a][1] * nd.dist[1] +
+                                   strain[a][2] * nd.dist[2]);
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    acc[1 + a] += m * nd.gw[a];
+                    acc[13 + a] += nd.gw[a] * gd;
+                    acc[16 + a] += nd.gw[a] * gsd;
+                    acc[19 + a] += nd.w * g[a];
+#pragma unroll
+                    for (int b = 0; b < 3; ++b) acc[4 + 3 * a + b] += nd.w * g[a] * nd.dist[b];
+                }
+            }
     }
-    group_sum(acc);
+    lane_sum<L>(acc);
+    const float rho = acc[0];
+    const float V = 1.0f / rho;
+    const float r = rho / k.rest_density;
+    const float r4 = (r * r) * (r * r);
+    const float pterm = k.stiffness * (r4 * r - 1.0f);
+    const float pres = fmaxf(pterm, 0.0f);
+    const float mu = k.dynamic_viscosity;
+    const float beta = -4.0f * V * k.dt;
+    float xb[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float sq = strain[a][0] * acc[19] + strain[a][1] * acc[20] + strain[a][2] * acc[21];
+        xb[a] = beta * (-pres * acc[13 + a] + mu * acc[16 + a] + pres * acc[19 + a] - mu * sq);
+    }
     float sb[3][3], Vbar = 0.0f;
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
-            sb[a][b] = -4.0f * V * k.dt * acc[3 * a + b];
-            Vbar += -4.0f * k.dt * sig[a][b] * acc[3 * a + b];
+            const float sig = (a == b ? -pres : 0.0f) + mu * strain[a][b];
+            sb[a][b] = beta * acc[4 + 3 * a + b];
+            Vbar += -4.0f * k.dt * sig * acc[4 + 3 * a + b];
         }
     float gk = 0.0f, gmu = 0.0f;
     float Cb[3][3];
@@ -405,31 +588,36 @@ __global__ void __launch_bounds__(kThreads)
     for (int a = 0; a < 3; ++a)
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
-            Cb[b][a] = k.dynamic_viscosity * (sb[a][b] + sb[b][a]);  // M(a, b) = C[b][a]
+            Cb[b][a] = mu * (sb[a][b] + sb[b][a]);  // M(a, b) = C[b][a]
             gmu += strain[a][b] * sb[a][b];
         }
     const float pbar = -(sb[0][0] + sb[1][1] + sb[2][2]);
-    float rhobar = -Vbar / (rho[0] * rho[0]);
+    float rhobar = -Vbar / (rho * rho);
     if (pterm > 0.0f) {
         gk = pbar * (r4 * r - 1.0f);
         rhobar += pbar * k.stiffness * 5.0f * r4 / k.rest_density;
     }
-    float xb[3] = {0.0f, 0.0f, 0.0f};
-    for (int nn = lane; nn < 27; nn += kLanes) {
-        Node nd;
-        if (!node(st, p.x, nn / 9, (nn / 3) % 3, nn % 3, k, nd)) continue;
-        if (active) atomicAdd(reinterpret_cast<float*>(ga + nd.idx) + 3, rhobar * nd.w);
-        const float m = tp.mass(lb + nd.idx, k.fm);
+    if (ln.active) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) xb[c] += rhobar * m * nd.gw[c];
+        for (int s = 0; s < slab_count<L>(); ++s) {
+            const Slab sx = slab(st, slab_gx<L>(s, ln.q));
+#pragma unroll
+            for (int gy = 0; gy < 3; ++gy)
+#pragma unroll
+                for (int gz = 0; gz < 3; ++gz) {
+                    const int c = node_index(st, sx.gx, gy, gz, k);
+                    if (c < 0) continue;
+                    const float w = (sx.w * st.w[1][gy]) * st.w[2][gz];
+                    atomicAdd(reinterpret_cast<float*>(ga + c) + 3, rhobar * w);
+                }
+        }
     }
-    group_sum(xb);
-    const bool leader = active && lane == 0;
+    const bool leader = ln.active && ln.q == 0;
     if (leader) {
         Rec an = load_rec(Anew, i);
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            an.x[a] += acc[9 + a] + xb[a];
+            an.x[a] += xb[a] + rhobar * acc[1 + a];
 #pragma unroll
             for (int b = 0; b < 3; ++b) an.C[a][b] += Cb[a][b];
         }
@@ -442,14 +630,13 @@ __global__ void __launch_bounds__(kThreads)
 // p2g_1 backward (p2g_1.wgsl:24-65): gathers the mass and momentum adjoints;
 // sets the velocity adjoint and adds to the position and C adjoints.
 // ---------------------------------------------------------------------------
-template <class Tape>
+template <class Tape, int L>
 __global__ void __launch_bounds__(kThreads)
     k_adj_p2g1(Tape tp, Particles Anew, const float4* __restrict__ gadj,
-               const AdjScene* __restrict__ scenes, const int* __restrict__ pscene, int n) {
-    const int gi = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = gi & (kLanes - 1);
-    const bool active = gi / kLanes < n;
-    const int i = active ? gi / kLanes : n - 1;
+               const AdjScene* __restrict__ scenes, const int* __restrict__ pscene,
+               const int* __restrict__ perm, int n) {
+    const Lanes<L> ln = lanes_of<L>(n);
+    const int i = perm ? perm[ln.j] : ln.j;
     const AdjScene& sc = scenes[pscene[i]];
     const SimConsts& k = sc.k;
     const float4* ga = gadj + sc.lbase;
@@ -457,28 +644,37 @@ __global__ void __launch_bounds__(kThreads)
     Sten st;
     make_sten(p.x, st);
     float acc[15] = {};  // v adjoint (3), C adjoint C[b][a] at 3 + 3b + a (9), x adjoint (3)
-    for (int nn = lane; nn < 27; nn += kLanes) {
-        Node nd;
-        if (!node(st, p.x, nn / 9, (nn / 3) % 3, nn % 3, k, nd)) continue;
-        const float4 g4 = __ldg(ga + nd.idx);
-        const float g[3] = {g4.x, g4.y, g4.z};
-        float s = g4.w;
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const float q = p.v[a] + (p.C[0][a] * nd.dist[0] + p.C[1][a] * nd.dist[1] +
-                                      p.C[2][a] * nd.dist[2]);
-            s += g[a] * q;
-            acc[a] += nd.w * g[a];
+    for (int s = 0; s < slab_count<L>(); ++s) {
+        const Slab sx = slab(st, slab_gx<L>(s, ln.q));
 #pragma unroll
-            for (int b = 0; b < 3; ++b) acc[3 + 3 * b + a] += nd.w * g[a] * nd.dist[b];
-        }
+        for (int gy = 0; gy < 3; ++gy)
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
-            acc[12 + c] += nd.gw[c] * s -
-                           nd.w * (p.C[c][0] * g[0] + p.C[c][1] * g[1] + p.C[c][2] * g[2]);
+            for (int gz = 0; gz < 3; ++gz) {
+                const int c = node_index(st, sx.gx, gy, gz, k);
+                if (c < 0) continue;
+                const float4 g4 = __ldg(ga + c);
+                Node nd;
+                slab_node(st, p.x, sx, gy, gz, nd);
+                const float g[3] = {g4.x, g4.y, g4.z};
+                float s2 = g4.w;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const float q = p.v[a] + (p.C[0][a] * nd.dist[0] + p.C[1][a] * nd.dist[1] +
+                                              p.C[2][a] * nd.dist[2]);
+                    s2 += g[a] * q;
+                    acc[a] += nd.w * g[a];
+#pragma unroll
+                    for (int b = 0; b < 3; ++b) acc[3 + 3 * b + a] += nd.w * g[a] * nd.dist[b];
+                }
+#pragma unroll
+                for (int c2 = 0; c2 < 3; ++c2)
+                    acc[12 + c2] += nd.gw[c2] * s2 -
+                                    nd.w * (p.C[c2][0] * g[0] + p.C[c2][1] * g[1] + p.C[c2][2] * g[2]);
+            }
     }
-    group_sum(acc);
-    if (!(active && lane == 0)) return;
+    lane_sum<L>(acc);
+    if (!(ln.active && ln.q == 0)) return;
     Rec an = load_rec(Anew, i);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -702,35 +898,62 @@ __global__ void __launch_bounds__(kThreads)
 
 inline int blocks(long long n) { return (int)((n + kThreads - 1) / kThreads); }
 
-}  // namespace
+
+template <class Tape, int L>
+void adjoint_kernels(const Tape& tp, const Particles& Aout, const Particles& Anew, float4* gadj,
+                     const AdjScene* scenes, int nscenes, const int* pscene, int n, int ncells,
+                     double* pgrad, const int* perm, cudaStream_t st) {
+    const int pb = lane_blocks<L>(n);
+    k_adj_g2p<Tape, L><<<pb, kThreads, 0, st>>>(tp, Aout, Anew, gadj, scenes, pscene, perm, n);
+    k_adj_update<Tape><<<blocks(ncells), kThreads, 0, st>>>(tp, gadj, scenes, nscenes, ncells);
+    k_adj_p2g2<Tape, L><<<pb, kThreads, 0, st>>>(tp, Anew, gadj, scenes, pscene, perm, n, pgrad);
+    k_adj_p2g1<Tape, L><<<pb, kThreads, 0, st>>>(tp, Anew, gadj, scenes, pscene, perm, n);
+}
 
 template <class Tape>
 void adjoint_substep(const Tape& tp, const Particles& Aout, const Particles& Anew, float4* gadj,
                      const AdjScene* scenes, int nscenes, const int* pscene, int n, int ncells,
-                     double* pgrad, cudaStream_t st) {
+                     double* pgrad, const AdjSort& so, cudaStream_t st) {
     if (n <= 0) return;
     cudaMemsetAsync(gadj, 0, sizeof(float4) * (size_t)ncells, st);
-    const int pb = blocks((long long)n * kLanes);
-    k_adj_g2p<Tape><<<pb, kThreads, 0, st>>>(tp, Aout, Anew, gadj, scenes, pscene, n);
-    k_adj_update<Tape><<<blocks(ncells), kThreads, 0, st>>>(tp, gadj, scenes, nscenes, ncells);
-    k_adj_p2g2<Tape><<<pb, kThreads, 0, st>>>(tp, Anew, gadj, scenes, pscene, n, pgrad);
-    k_adj_p2g1<Tape><<<pb, kThreads, 0, st>>>(tp, Anew, gadj, scenes, pscene, n);
+    if (so.lanes == 3) {  // small batch: the sort's launches would cost more than it saves
+        adjoint_kernels<Tape, 3>(tp, Aout, Anew, gadj, scenes, nscenes, pscene, n, ncells, pgrad,
+                                 nullptr, st);
+        return;
+    }
+    cudaMemsetAsync(so.bin_count, 0, sizeof(int) * (size_t)so.nbins, st);
+    cudaMemsetAsync(so.placed, 0, sizeof(int), st);
+    k_adj_bin<Tape><<<blocks(n), kThreads, 0, st>>>(tp, scenes, pscene, n, so);
+    k_adj_place<<<blocks(so.nbins), kThreads, 0, st>>>(so);
+    k_adj_perm<<<blocks(n), kThreads, 0, st>>>(so, n);
+    adjoint_kernels<Tape, 1>(tp, Aout, Anew, gadj, scenes, nscenes, pscene, n, ncells, pgrad,
+                             so.perm, st);
+}
+
+}  // namespace
+
+void adj_bricks(const SimConsts& k, int& BX, int& BY, int& BZ) {
+    const long long yz = (long long)k.Y * k.Z;
+    const long long xi = yz > 0 ? ((long long)k.grid_count + yz - 1) / yz : 0;
+    BX = (int)((xi + 3) / 4);
+    BY = (k.Y + 3) / 4;
+    BZ = (k.Z + 3) / 4;
 }
 
 void launch_adjoint_substep(const Particles& S, const int4* G, const Particles& Aout,
                             const Particles& Anew, float4* gadj, const AdjScene* scenes,
                             int nscenes, const int* pscene, int n, int ncells, double* pgrad,
-                            cudaStream_t st) {
+                            const AdjSort& so, cudaStream_t st) {
     adjoint_substep(TapeFixed{S, G}, Aout, Anew, gadj, scenes, nscenes, pscene, n, ncells, pgrad,
-                    st);
+                    so, st);
 }
 
 void launch_adjoint_substep64(const double* S, const double4* G, const Particles& Aout,
                               const Particles& Anew, float4* gadj, const AdjScene* scenes,
                               int nscenes, const int* pscene, int n, int ncells, double* pgrad,
-                              cudaStream_t st) {
+                              const AdjSort& so, cudaStream_t st) {
     adjoint_substep(Tape64{S, G}, Aout, Anew, gadj, scenes, nscenes, pscene, n, ncells, pgrad,
-                    st);
+                    so, st);
 }
 
 void launch_substep64(const double* S, double4* G, double* Sout, const AdjScene* scenes,

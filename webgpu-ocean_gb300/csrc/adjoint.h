@@ -10,12 +10,32 @@ namespace mpm {
 // (C[c][r] at 6 + 3c + r), padding [15].
 constexpr int kRec64 = 16;
 
-// One scene of an adjoint batch: its constants and the first cell of its
-// grid in the linear (reference-layout) concatenation of all scenes' grids.
+// One scene of an adjoint batch: its constants, the first cell of its grid in
+// the linear (reference-layout) concatenation of all scenes' grids, and its
+// bricks (4^3 base cells, BX x BY x BZ of them) in the adjoint's spatial
+// sort, numbered from bbase.
 struct AdjScene {
     SimConsts k;
     int lbase;
-    int pad[3];
+    int bbase;
+    int BY, BZ;
+};
+
+// Bricks per axis of a scene's grid (x extent ceil(grid_count / (Y Z))).
+void adj_bricks(const SimConsts& k, int& BX, int& BY, int& BZ);
+
+// Scratch of the adjoint's per-substep spatial sort: particles are ordered
+// by the brick of their base cell (bin nbins - 1: stencils that leave the
+// grid interior), and the particle kernels run in that order with `lanes`
+// (1 or 3) threads per particle.
+struct AdjSort {
+    int2* key_rank = nullptr;   // n: (bin, rank in bin)
+    int* perm = nullptr;        // n: particle ids in sorted order
+    int* bin_count = nullptr;   // nbins
+    int* bin_first = nullptr;   // nbins
+    int* placed = nullptr;      // 1: particles placed so far
+    int nbins = 0;
+    int lanes = 1;
 };
 
 // One substep backward.  S: the substep's input state (particle order of the
@@ -26,14 +46,14 @@ struct AdjScene {
 void launch_adjoint_substep(const Particles& S, const int4* G, const Particles& Aout,
                             const Particles& Anew, float4* gadj, const AdjScene* scenes,
                             int nscenes, const int* pscene, int n, int ncells, double* pgrad,
-                            cudaStream_t st);
+                            const AdjSort& so, cudaStream_t st);
 
 // The same on the FP64 tape (S: kRec64 doubles per particle; G: double4
 // cells {v or momentum, mass}).
 void launch_adjoint_substep64(const double* S, const double4* G, const Particles& Aout,
                               const Particles& Anew, float4* gadj, const AdjScene* scenes,
                               int nscenes, const int* pscene, int n, int ncells, double* pgrad,
-                              cudaStream_t st);
+                              const AdjSort& so, cudaStream_t st);
 
 // One FP64 substep of the continuous model: S -> Sout, leaving the updated
 // grid in G (ncells double4, all scenes).

@@ -1099,8 +1099,10 @@ struct mpm_adjoint {
     AdjScene* scenes_d = nullptr;
     int* pscene_d = nullptr;
     double* pgrad_d = nullptr;
+    AdjSort sort;                    // per-substep spatial sort of the adjoint kernels
     int ncells = 0;
     std::vector<int> lbase;
+    std::vector<int> bbase;          // first brick of each scene in the sort
 };
 
 namespace {
@@ -1282,6 +1284,11 @@ void free_adjoint(mpm_adjoint* a) {
     cudaFree(a->scenes_d);
     cudaFree(a->pscene_d);
     cudaFree(a->pgrad_d);
+    cudaFree(a->sort.key_rank);
+    cudaFree(a->sort.perm);
+    cudaFree(a->sort.bin_count);
+    cudaFree(a->sort.bin_first);
+    cudaFree(a->sort.placed);
     if (a->b) mpm_batch_destroy(a->b);
     delete a;
 }
@@ -1290,11 +1297,26 @@ int upload_adj_scenes(mpm_adjoint* a) {
     const int S = (int)a->b->consts.size();
     std::vector<AdjScene> hs((size_t)S);
     for (int s = 0; s < S; ++s) {
-        hs[(size_t)s].k = a->b->consts[(size_t)s];
-        hs[(size_t)s].lbase = a->lbase[(size_t)s];
+        AdjScene& h = hs[(size_t)s];
+        h.k = a->b->consts[(size_t)s];
+        h.lbase = a->lbase[(size_t)s];
+        h.bbase = a->bbase[(size_t)s];
+        int BX = 0;
+        adj_bricks(h.k, BX, h.BY, h.BZ);
     }
     MPM_CUDA(cudaMemcpy(a->scenes_d, hs.data(), sizeof(AdjScene) * (size_t)S, cudaMemcpyHostToDevice));
     return MPM_OK;
+}
+
+// Threads per particle in the adjoint kernels: three (one per stencil
+// x-slab) while one thread per particle would leave most of the GPU idle
+// (fewer particles than 512 per SM), else one.
+int adj_lanes(long long n) {
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1)
+        nsm = 1;
+    return n < 512LL * nsm ? 3 : 1;
 }
 
 // Checkpoint slot of the state after `step` substeps of a T-substep forward
@@ -1317,13 +1339,19 @@ int mpm_adjoint_create(const mpm_scene_desc* scenes, int num_scenes, int max_sub
         return fail(MPM_E_INVALID, "max_substeps and checkpoint_every must be positive");
     if (!scenes || num_scenes < 1) return fail(MPM_E_INVALID, "a batch needs at least one scene");
     long long n = 0, cells = 0;
-    std::vector<int> lbase((size_t)num_scenes);
+    long long bricks = 0;
+    std::vector<int> lbase((size_t)num_scenes), bbase((size_t)num_scenes);
     std::vector<int> pscene;
     for (int s = 0; s < num_scenes; ++s) {
         SimConsts k;
         if (int rc = scene_consts(scenes[s], k)) return rc;
         lbase[(size_t)s] = (int)cells;
+        bbase[(size_t)s] = (int)bricks;
         cells += k.grid_count;
+        int BX = 0, BY = 0, BZ = 0;
+        adj_bricks(k, BX, BY, BZ);
+        bricks += (long long)BX * BY * BZ;
+        if (bricks > 0x3fffffffLL) return fail(MPM_E_CAPACITY, "batch too large");
         n += scenes[s].num_particles;
         if (cells > 0x7fffffffLL || n > 0x3fffffffLL) return fail(MPM_E_CAPACITY, "batch too large");
         pscene.insert(pscene.end(), (size_t)scenes[s].num_particles, s);
@@ -1343,9 +1371,18 @@ int mpm_adjoint_create(const mpm_scene_desc* scenes, int num_scenes, int max_sub
     a->nck = (max_substeps + a->every - 1) / a->every + 1;
     a->ncells = (int)cells;
     a->lbase = lbase;
+    a->bbase = bbase;
     DeviceGuard g(b->device);
     const size_t np = (size_t)(n > 0 ? n : 1);
+    AdjSort& so = a->sort;
+    so.nbins = (int)bricks + 1;
+    so.lanes = adj_lanes(n);
     cudaError_t e = alloc_tape(a);
+    if (e == cudaSuccess) e = cudaMalloc(&so.key_rank, sizeof(int2) * np);
+    if (e == cudaSuccess) e = cudaMalloc(&so.perm, sizeof(int) * np);
+    if (e == cudaSuccess) e = cudaMalloc(&so.bin_count, sizeof(int) * (size_t)so.nbins);
+    if (e == cudaSuccess) e = cudaMalloc(&so.bin_first, sizeof(int) * (size_t)so.nbins);
+    if (e == cudaSuccess) e = cudaMalloc(&so.placed, sizeof(int));
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = alloc_particles(a->adj[i], np);
     if (e == cudaSuccess) e = cudaMalloc(&a->gadj, sizeof(float4) * (size_t)cells);
     if (e == cudaSuccess) e = cudaMalloc(&a->scenes_d, sizeof(AdjScene) * (size_t)num_scenes);
@@ -1527,12 +1564,12 @@ int mpm_backward(mpm_adjoint* a, const float* seeds, const int* seed_steps, int 
                 const double* Sx = t == t0 ? a->ckpt64[(size_t)j] : a->seg64[(size_t)(t - t0)];
                 launch_adjoint_substep64(Sx, a->gtape64 + (g0 + (size_t)(t - t0)) * nc, a->adj[cur],
                                          a->adj[cur ^ 1], a->gadj, a->scenes_d, S, a->pscene_d, n,
-                                         a->ncells, a->pgrad_d, st);
+                                         a->ncells, a->pgrad_d, a->sort, st);
             } else {
                 const Particles& Sx = t == t0 ? a->ckpt[(size_t)j] : a->seg[(size_t)(t - t0)];
                 launch_adjoint_substep(Sx, a->gtape + (g0 + (size_t)(t - t0)) * nc, a->adj[cur],
                                        a->adj[cur ^ 1], a->gadj, a->scenes_d, S, a->pscene_d, n,
-                                       a->ncells, a->pgrad_d, st);
+                                       a->ncells, a->pgrad_d, a->sort, st);
             }
             cur ^= 1;
             add_seeds(t, a->adj[cur]);
