@@ -325,15 +325,19 @@ def measure_adjoint(pkg, torch, repeats: int = 3) -> dict:
     recs[:, 4:7] = rng.normal(0.0, 0.1, (len(recs), 3)).astype(np.float32)
     box, T = [48.0, 48.0, 48.0], 200
     out = {"workload": ADJ_WORKLOAD, "substeps": T}
+    # the plain solver over the same substeps from the same initial state
+    # (upload included, as in the checkpointed forward), graph captured first
     sim = pkg.MLSMPMSimulator(None, None, 1.2, maxParticles=len(recs), maxGrid=(48, 48, 48))
     sim.upload(recs, box)
     sim.setGraph(True)
     sim.autotune(8)
+    sim.upload(recs, box)
     sim.execute(substeps=T)
     sim.synchronize()
     best = None
     for _ in range(repeats):
         t0 = time.perf_counter()
+        sim.upload(recs, box)
         sim.execute(substeps=T)
         sim.synchronize()
         dt = time.perf_counter() - t0
@@ -365,11 +369,15 @@ def measure_adjoint(pkg, torch, repeats: int = 3) -> dict:
     descs, recs64, _ = pkg.inverse.inverse_scenes(64, seed=BATCH_SEED)
     b = pkg.MLSMPMBatch(descs, recs64)
     b.step(100)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    b.step(100)
-    torch.cuda.synchronize()
-    plain64 = time.perf_counter() - t0
+    plain64 = None
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.upload(recs64)
+        b.step(100)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        plain64 = dt if plain64 is None else min(plain64, dt)
     b.close()
     adj = pkg.MLSMPMAdjoint(descs, 100, 20, tape="fixed")
     seed = np.zeros((len(recs64), 20), np.float32)
@@ -393,10 +401,11 @@ def measure_adjoint(pkg, torch, repeats: int = 3) -> dict:
         "forward_ms": 1e3 * fwd, "backward_ms": 1e3 * bwd,
         "fwd_plus_adj_over_own_forward": (fwd + bwd) / fwd,
         "fwd_plus_adj_over_plain_forward": (fwd + bwd) / plain64,
-        "note": "forward_ms includes uploading the initial state from host memory"}
+        "note": "forward_ms and plain_batched_forward_ms include uploading the initial state from host memory"}
     out["timing"] = ("host wall clock around synchronised calls, best of "
-                     f"{repeats}; plain forward = MLSMPMSimulator.execute(substeps=200), "
-                     "CUDA graph, autotuned task size")
+                     f"{repeats}; plain forward = upload of the same initial state + "
+                     "MLSMPMSimulator.execute(substeps=200) (CUDA graph, autotuned task size), "
+                     "batch: upload + MLSMPMBatch.step(100)")
     return out
 
 

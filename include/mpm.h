@@ -244,6 +244,10 @@ int mpm_batch_num_scenes(const mpm_batch* batch);
 int64_t mpm_batch_num_particles(const mpm_batch* batch);
 /* `substeps` substeps of every scene; asynchronous on `stream`. */
 int mpm_batch_step(mpm_batch* batch, int substeps, void* stream);
+/* Replaces every scene's particles (same counts and order as at creation)
+ * and restarts the scenes from them, as a fresh mpm_batch_create would;
+ * captured graphs are kept (synchronizes). */
+int mpm_batch_upload(mpm_batch* batch, const float* aos80);
 /* Replaces scene s's constants (box sizes and num_particles must stay). */
 int mpm_batch_set_scene(mpm_batch* batch, int scene, const mpm_scene_desc* desc);
 int mpm_batch_set_graph(mpm_batch* batch, int enable); /* default 1 */

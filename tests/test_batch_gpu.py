@@ -177,3 +177,46 @@ def test_batch_task_size_and_autotune(cuda, pkg, oracle_mod):
     batch.step(4)
     assert_bits_equal(batch.downloadParticles(), results[0], "after autotune")
     batch.close()
+
+
+def test_batch_upload_restarts_and_reuses_graphs(cuda, pkg):
+    """upload() restarts every scene from new records exactly as a fresh batch
+    would, with the CUDA graph captured before the upload replayed."""
+    from oracle import scene as scene_mod
+    descs, recs = mixed_scenes(pkg, scene_mod)
+    fresh = pkg.MLSMPMBatch(descs, recs)
+    fresh.step(5)
+    want = fresh.downloadParticles()
+    fresh.close()
+    batch = pkg.MLSMPMBatch(descs, recs)
+    other = recs.copy()
+    other[:, 4:7] += np.float32(0.05)
+    batch.upload(other)
+    batch.step(5)
+    moved = batch.downloadParticles()
+    launches = batch.launchCount()
+    batch.upload(recs)
+    batch.step(5)
+    assert_bits_equal(batch.downloadParticles(), want, "after upload")
+    assert not np.array_equal(moved, want)
+    assert batch.launchCount() > launches
+    with pytest.raises(ValueError):
+        batch.upload(recs[:-1])
+    batch.close()
+
+
+def test_simulator_reupload_replays_its_graph(cuda, pkg):
+    """Re-uploading the same scene keeps the simulator's captured graph and
+    gives the same trajectory as the first run."""
+    from oracle import scene as scene_mod
+    recs = scene_mod.lattice(16, 6.0, 0.5, 0.05, 5)
+    sim = pkg.MLSMPMSimulator(None, None, 1.2, maxParticles=len(recs), maxGrid=(32, 32, 32))
+    sim.setGraph(True)
+    outs = []
+    for _ in range(3):
+        sim.upload(recs, [32.0, 32.0, 32.0])
+        sim.execute(substeps=7)
+        outs.append(sim.downloadParticles())
+    assert_bits_equal(outs[1], outs[0], "second upload")
+    assert_bits_equal(outs[2], outs[0], "third upload")
+    sim.close()

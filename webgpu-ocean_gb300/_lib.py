@@ -160,6 +160,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "mpm_batch_num_scenes": (i32, [vp]),
         "mpm_batch_num_particles": (i64, [vp]),
         "mpm_batch_step": (i32, [vp, i32, vp]),
+        "mpm_batch_upload": (i32, [vp, fp]),
         "mpm_batch_set_scene": (i32, [vp, i32, ctypes.POINTER(SceneDesc)]),
         "mpm_batch_set_graph": (i32, [vp, i32]),
         "mpm_batch_download_particles": (i32, [vp, fp]),

@@ -686,6 +686,43 @@ __global__ void __launch_bounds__(kThreads)
     store_rec(Anew, i, an);
 }
 
+// 80-byte reference records (x, v, C columns padded to four floats) <->
+// FP64 tape records.
+__global__ void k_records_to_rec64(const float* __restrict__ rec, double* __restrict__ S, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* P = rec + 20 * (size_t)i;
+    double* q = S + (size_t)kRec64 * i;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        q[a] = P[a];
+        q[3 + a] = P[4 + a];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) q[6 + 3 * c + r] = P[8 + 4 * c + r];
+    q[15] = 0.0;
+}
+
+__global__ void k_rec64_to_records(const double* __restrict__ S, float* __restrict__ rec, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* q = S + (size_t)kRec64 * i;
+    float* P = rec + 20 * (size_t)i;
+#pragma unroll
+    for (int j = 0; j < 20; ++j) P[j] = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        P[a] = (float)q[a];
+        P[4 + a] = (float)q[3 + a];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) P[8 + 4 * c + r] = (float)q[6 + 3 * c + r];
+}
+
 // A += B over n records (all four streams).
 __global__ void k_axpy(Particles A, Particles B, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -965,6 +1002,16 @@ void launch_substep64(const double* S, double4* G, double* Sout, const AdjScene*
     }
     k64_update<<<blocks(ncells), kThreads, 0, st>>>(G, scenes, nscenes, ncells);
     if (n > 0) k64_g2p<<<blocks(n), kThreads, 0, st>>>(S, G, Sout, scenes, pscene, n);
+}
+
+void launch_records_to_rec64(const float* rec, double* S, int n, cudaStream_t st) {
+    if (n <= 0) return;
+    k_records_to_rec64<<<blocks(n), kThreads, 0, st>>>(rec, S, n);
+}
+
+void launch_rec64_to_records(const double* S, float* rec, int n, cudaStream_t st) {
+    if (n <= 0) return;
+    k_rec64_to_records<<<blocks(n), kThreads, 0, st>>>(S, rec, n);
 }
 
 void launch_particles_axpy(const Particles& A, const Particles& B, int n, cudaStream_t st) {

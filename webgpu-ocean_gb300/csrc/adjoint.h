@@ -60,6 +60,10 @@ void launch_adjoint_substep64(const double* S, const double4* G, const Particles
 void launch_substep64(const double* S, double4* G, double* Sout, const AdjScene* scenes,
                       int nscenes, const int* pscene, int n, int ncells, cudaStream_t st);
 
+// 80-byte reference records (device) <-> FP64 tape records.
+void launch_records_to_rec64(const float* rec, double* S, int n, cudaStream_t st);
+void launch_rec64_to_records(const double* S, float* rec, int n, cudaStream_t st);
+
 // A += B, record-wise over n particles.
 void launch_particles_axpy(const Particles& A, const Particles& B, int n, cudaStream_t st);
 

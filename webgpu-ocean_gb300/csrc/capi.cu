@@ -109,30 +109,57 @@ int scene_lattice(float* out, int npa, double origin, double spacing, double jit
     return (int)p;
 }
 
-// Reference 80-byte records <-> the library's four float4 streams.
-void aos80_to_soa(const float* in, int n, std::vector<float4> q[4]) {
-    for (int k = 0; k < 4; ++k) q[k].resize((size_t)n);
-    for (int i = 0; i < n; ++i) {
-        const float* P = in + 20 * (size_t)i;
-        // C[c][r] = P[8 + 4c + r]
-        q[0][i] = make_float4(P[0], P[1], P[2], P[8]);
-        q[1][i] = make_float4(P[9], P[10], P[12], P[13]);
-        q[2][i] = make_float4(P[14], P[16], P[17], P[18]);
-        q[3][i] = make_float4(P[4], P[5], P[6], 0.0f);
+// Reference 80-byte records in host memory <-> the library's four float4
+// streams, converted on the device: one copy of the records through a
+// staging buffer of 80 bytes per particle (`stage`, or a stream-ordered
+// allocation when null), then a gather kernel.
+struct Stage {
+    float* p = nullptr;
+    bool owned = false;
+    cudaError_t get(float* given, int n, cudaStream_t st) {
+        if (given) {
+            p = given;
+            return cudaSuccess;
+        }
+        owned = true;
+        return cudaMallocAsync(reinterpret_cast<void**>(&p), (size_t)80 * (size_t)n, st);
     }
+    void release(cudaStream_t st) {
+        if (owned && p) cudaFreeAsync(p, st);
+        p = nullptr;
+        owned = false;
+    }
+};
+
+cudaError_t upload_records(const Particles& dst, const float* host, int n, float* stage,
+                           cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    Stage sg;
+    cudaError_t e = sg.get(stage, n, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(sg.p, host, (size_t)80 * (size_t)n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        launch_records_to_streams(sg.p, dst, n, st);
+        e = cudaGetLastError();
+    }
+    sg.release(st);
+    return e;
 }
 
-void soa_to_aos80(const std::vector<float4> q[4], int n, float* out) {
-    for (int i = 0; i < n; ++i) {
-        float* P = out + 20 * (size_t)i;
-        std::memset(P, 0, 80);
-        const float4 a = q[0][i], b = q[1][i], c = q[2][i], d = q[3][i];
-        P[0] = a.x; P[1] = a.y; P[2] = a.z;
-        P[4] = d.x; P[5] = d.y; P[6] = d.z;
-        P[8] = a.w; P[9] = b.x; P[10] = b.y;
-        P[12] = b.z; P[13] = b.w; P[14] = c.x;
-        P[16] = c.y; P[17] = c.z; P[18] = c.w;
+cudaError_t download_records(const Particles& src, float* host, int n, float* stage,
+                             cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    Stage sg;
+    cudaError_t e = sg.get(stage, n, st);
+    if (e == cudaSuccess) {
+        launch_streams_to_records(src, sg.p, n, st);
+        e = cudaGetLastError();
     }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(host, sg.p, (size_t)80 * (size_t)n, cudaMemcpyDeviceToHost, st);
+    sg.release(st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e;
 }
 
 int f2i_trunc_sat(float x) {
@@ -230,15 +257,9 @@ int load_particles(mpm_sim* s, const float* aos80, int n, const float init_box[3
     DeviceGuard g(s->device);
     if (!g.ok) return fail(MPM_E_CUDA, "cannot select the simulator's device");
     MPM_CUDA(cudaDeviceSynchronize());
-    std::vector<float4> q[4];
-    aos80_to_soa(aos80, n, q);
     s->ps.cur = 0;
     s->ps.canonical = true;
-    const Particles& P = s->ps.P[0];
-    float4* dst[4] = {P.p0, P.p1, P.p2, P.p3};
-    for (int k = 0; k < 4; ++k)
-        if (n) MPM_CUDA(cudaMemcpy(dst[k], q[k].data(), sizeof(float4) * (size_t)n,
-                                   cudaMemcpyHostToDevice));
+    MPM_CUDA(upload_records(s->ps.P[0], aos80, n, nullptr, nullptr));
     launch_iota(s->ps.id[0], n, nullptr);
     MPM_CUDA(cudaGetLastError());
     s->n = n;
@@ -596,15 +617,7 @@ int mpm_download_particles(mpm_sim* s, float* out) {
         MPM_CUDA(cudaDeviceSynchronize());
         Psrc = &s->ps.P[c ^ 1];
     }
-    std::vector<float4> q[4];
-    const float4* src[4] = {Psrc->p0, Psrc->p1, Psrc->p2, Psrc->p3};
-    for (int k = 0; k < 4; ++k) {
-        q[k].resize((size_t)s->n);
-        if (s->n)
-            MPM_CUDA(cudaMemcpy(q[k].data(), src[k], sizeof(float4) * (size_t)s->n,
-                                cudaMemcpyDeviceToHost));
-    }
-    soa_to_aos80(q, s->n, out);
+    MPM_CUDA(download_records(*Psrc, out, s->n, nullptr, nullptr));
     return MPM_OK;
 }
 
@@ -903,14 +916,7 @@ int mpm_batch_create(const mpm_scene_desc* scenes, int num_scenes, const float* 
     if (e == cudaSuccess) e = cudaMalloc(&b->counters, sizeof(unsigned long long) * 2);
     if (e == cudaSuccess) e = cudaMemset(b->counters, 0, sizeof(unsigned long long) * 2);
     if (e == cudaSuccess) e = cudaMemset(b->posvel, 0, sizeof(float4) * 2 * np);
-    if (e == cudaSuccess) {
-        std::vector<float4> q[4];
-        aos80_to_soa(aos80, (int)n, q);
-        const Particles& P = b->ps.P[0];
-        float4* dst[4] = {P.p0, P.p1, P.p2, P.p3};
-        for (int k = 0; k < 4 && e == cudaSuccess; ++k)
-            if (n) e = cudaMemcpy(dst[k], q[k].data(), sizeof(float4) * (size_t)n, cudaMemcpyHostToDevice);
-    }
+    if (e == cudaSuccess) e = upload_records(b->ps.P[0], aos80, (int)n, nullptr, nullptr);
     if (e == cudaSuccess) {
         launch_iota(b->ps.id[0], (int)n, nullptr);
         e = cudaGetLastError();
@@ -956,6 +962,25 @@ int mpm_batch_step(mpm_batch* b, int substeps, void* stream) {
         return fail(MPM_E_CUDA, std::string("batch: ") + sorted_error());
     b->stepped = true;
     MPM_CUDA(cudaGetLastError());
+    return MPM_OK;
+}
+
+int mpm_batch_upload(mpm_batch* b, const float* aos80) {
+    if (int rc = check_batch(b)) return rc;
+    if (!aos80 && b->n) return fail(MPM_E_INVALID, "particle array is null");
+    DeviceGuard g(b->device);
+    if (!g.ok) return fail(MPM_E_CUDA, "cannot select the batch's device");
+    MPM_CUDA(cudaDeviceSynchronize());
+    b->ps.cur = 0;
+    b->ps.canonical = true;
+    MPM_CUDA(upload_records(b->ps.P[0], aos80, b->n, nullptr, nullptr));
+    launch_iota(b->ps.id[0], b->n, nullptr);
+    MPM_CUDA(cudaGetLastError());
+    MPM_CUDA(cudaMemset(b->counters, 0, sizeof(unsigned long long) * 2));
+    if (b->n) MPM_CUDA(cudaMemset(b->posvel, 0, sizeof(float4) * 2 * (size_t)b->n));
+    sorted_invalidate(b->sorted);
+    b->stepped = false;
+    MPM_CUDA(cudaDeviceSynchronize());
     return MPM_OK;
 }
 
@@ -1012,15 +1037,7 @@ int mpm_batch_download_particles(mpm_batch* b, float* out) {
         MPM_CUDA(cudaDeviceSynchronize());
         Psrc = &b->ps.P[c ^ 1];
     }
-    std::vector<float4> q[4];
-    const float4* src[4] = {Psrc->p0, Psrc->p1, Psrc->p2, Psrc->p3};
-    for (int k = 0; k < 4; ++k) {
-        q[k].resize((size_t)b->n);
-        if (b->n)
-            MPM_CUDA(cudaMemcpy(q[k].data(), src[k], sizeof(float4) * (size_t)b->n,
-                                cudaMemcpyDeviceToHost));
-    }
-    soa_to_aos80(q, b->n, out);
+    MPM_CUDA(download_records(*Psrc, out, b->n, nullptr, nullptr));
     return MPM_OK;
 }
 
@@ -1096,6 +1113,7 @@ struct mpm_adjoint {
     // adjoint state
     Particles adj[2]{};
     float4* gadj = nullptr;
+    float* stage = nullptr;          // 80 bytes per particle: host records in and out
     AdjScene* scenes_d = nullptr;
     int* pscene_d = nullptr;
     double* pgrad_d = nullptr;
@@ -1136,69 +1154,26 @@ cudaError_t copy_particles(const Particles& dst, const Particles& src, int n, cu
     return cudaSuccess;
 }
 
-cudaError_t upload_aos80(const Particles& dst, const float* aos80, int n) {
-    std::vector<float4> q[4];
-    aos80_to_soa(aos80, n, q);
-    float4* d[4] = {dst.p0, dst.p1, dst.p2, dst.p3};
-    for (int k = 0; k < 4; ++k) {
-        if (!n) break;
-        const cudaError_t e =
-            cudaMemcpy(d[k], q[k].data(), sizeof(float4) * (size_t)n, cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) return e;
+// The same for the FP64 tape's records (kRec64 doubles).
+cudaError_t upload_records64(double* dst, const float* host, int n, float* stage, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemcpyAsync(stage, host, (size_t)80 * (size_t)n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        launch_records_to_rec64(stage, dst, n, st);
+        e = cudaGetLastError();
     }
-    return cudaSuccess;
+    return e;
 }
 
-cudaError_t download_aos80(const Particles& src, int n, float* aos80) {
-    std::vector<float4> q[4];
-    const float4* s[4] = {src.p0, src.p1, src.p2, src.p3};
-    for (int k = 0; k < 4; ++k) {
-        q[k].resize((size_t)n);
-        if (!n) continue;
-        const cudaError_t e =
-            cudaMemcpy(q[k].data(), s[k], sizeof(float4) * (size_t)n, cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) return e;
-    }
-    soa_to_aos80(q, n, aos80);
-    return cudaSuccess;
-}
-
-// 80-byte records <-> FP64 tape records (kRec64 doubles).
-cudaError_t upload_aos80_64(double* dst, const float* aos80, int n) {
-    std::vector<double> h((size_t)kRec64 * (size_t)(n > 0 ? n : 1), 0.0);
-    for (int i = 0; i < n; ++i) {
-        const float* P = aos80 + 20 * (size_t)i;
-        double* q = h.data() + (size_t)kRec64 * i;
-        for (int a = 0; a < 3; ++a) {
-            q[a] = P[a];
-            q[3 + a] = P[4 + a];
-        }
-        for (int c = 0; c < 3; ++c)
-            for (int r = 0; r < 3; ++r) q[6 + 3 * c + r] = P[8 + 4 * c + r];
-    }
-    if (!n) return cudaSuccess;
-    return cudaMemcpy(dst, h.data(), sizeof(double) * kRec64 * (size_t)n, cudaMemcpyHostToDevice);
-}
-
-cudaError_t download_aos80_64(const double* src, int n, float* aos80) {
-    std::vector<double> h((size_t)kRec64 * (size_t)(n > 0 ? n : 1));
-    if (n) {
-        const cudaError_t e = cudaMemcpy(h.data(), src, sizeof(double) * kRec64 * (size_t)n,
-                                         cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) return e;
-    }
-    for (int i = 0; i < n; ++i) {
-        float* P = aos80 + 20 * (size_t)i;
-        const double* q = h.data() + (size_t)kRec64 * i;
-        std::memset(P, 0, 80);
-        for (int a = 0; a < 3; ++a) {
-            P[a] = (float)q[a];
-            P[4 + a] = (float)q[3 + a];
-        }
-        for (int c = 0; c < 3; ++c)
-            for (int r = 0; r < 3; ++r) P[8 + 4 * c + r] = (float)q[6 + 3 * c + r];
-    }
-    return cudaSuccess;
+cudaError_t download_records64(const double* src, float* host, int n, float* stage,
+                               cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    launch_rec64_to_records(src, stage, n, st);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(host, stage, (size_t)80 * (size_t)n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e;
 }
 
 // Puts a canonical state into the batch's particle store and forgets the
@@ -1281,6 +1256,7 @@ void free_adjoint(mpm_adjoint* a) {
     free_particles(a->adj[0]);
     free_particles(a->adj[1]);
     cudaFree(a->gadj);
+    cudaFree(a->stage);
     cudaFree(a->scenes_d);
     cudaFree(a->pscene_d);
     cudaFree(a->pgrad_d);
@@ -1385,6 +1361,7 @@ int mpm_adjoint_create(const mpm_scene_desc* scenes, int num_scenes, int max_sub
     if (e == cudaSuccess) e = cudaMalloc(&so.placed, sizeof(int));
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = alloc_particles(a->adj[i], np);
     if (e == cudaSuccess) e = cudaMalloc(&a->gadj, sizeof(float4) * (size_t)cells);
+    if (e == cudaSuccess) e = cudaMalloc(&a->stage, (size_t)80 * np);
     if (e == cudaSuccess) e = cudaMalloc(&a->scenes_d, sizeof(AdjScene) * (size_t)num_scenes);
     if (e == cudaSuccess) e = cudaMalloc(&a->pscene_d, sizeof(int) * np);
     if (e == cudaSuccess) e = cudaMalloc(&a->pgrad_d, sizeof(double) * 2 * (size_t)num_scenes);
@@ -1444,7 +1421,7 @@ int mpm_forward_ckpt(mpm_adjoint* a, const float* init, int substeps, void* stre
     a->T = -1;
     MPM_CUDA(cudaStreamSynchronize(st));
     if (a->tape == MPM_TAPE_FP64) {
-        MPM_CUDA(upload_aos80_64(a->ckpt64[0], init, n));
+        MPM_CUDA(upload_records64(a->ckpt64[0], init, n, a->stage, st));
         const double* cur = a->ckpt64[0];
         for (int t = 0; t < substeps; ++t) {
             const int slot = ckpt_slot(a, t + 1, substeps);
@@ -1454,7 +1431,7 @@ int mpm_forward_ckpt(mpm_adjoint* a, const float* init, int substeps, void* stre
             cur = dst;
         }
     } else {
-        MPM_CUDA(upload_aos80(a->ckpt[0], init, n));
+        MPM_CUDA(upload_records(a->ckpt[0], init, n, a->stage, st));
         MPM_CUDA(batch_load_device(b, a->ckpt[0], st));
         int t = 0;
         while (t < substeps) {
@@ -1484,8 +1461,8 @@ int mpm_adjoint_state(mpm_adjoint* a, int substep, float* out) {
     if (j < 0) return fail(MPM_E_INVALID, "substep is not a checkpoint");
     DeviceGuard g(a->b->device);
     MPM_CUDA(cudaDeviceSynchronize());
-    if (a->tape == MPM_TAPE_FP64) MPM_CUDA(download_aos80_64(a->ckpt64[(size_t)j], a->b->n, out));
-    else MPM_CUDA(download_aos80(a->ckpt[(size_t)j], a->b->n, out));
+    if (a->tape == MPM_TAPE_FP64) MPM_CUDA(download_records64(a->ckpt64[(size_t)j], out, a->b->n, a->stage, nullptr));
+    else MPM_CUDA(download_records(a->ckpt[(size_t)j], out, a->b->n, a->stage, nullptr));
     return MPM_OK;
 }
 
@@ -1510,7 +1487,8 @@ int mpm_backward(mpm_adjoint* a, const float* seeds, const int* seed_steps, int 
     };
     for (int i = 0; i < nseeds; ++i) {
         cudaError_t e = alloc_particles(sbuf[(size_t)i], (size_t)(n > 0 ? n : 1));
-        if (e == cudaSuccess) e = upload_aos80(sbuf[(size_t)i], seeds + (size_t)i * 20 * (size_t)n, n);
+        if (e == cudaSuccess)
+            e = upload_records(sbuf[(size_t)i], seeds + (size_t)i * 20 * (size_t)n, n, a->stage, st);
         if (e != cudaSuccess) {
             release();
             return cuda_fail(e, "mpm_backward seeds");
@@ -1579,7 +1557,7 @@ int mpm_backward(mpm_adjoint* a, const float* seeds, const int* seed_steps, int 
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     release();
     if (e != cudaSuccess) return cuda_fail(e, "mpm_backward");
-    if (grad_init) MPM_CUDA(download_aos80(a->adj[cur], n, grad_init));
+    if (grad_init) MPM_CUDA(download_records(a->adj[cur], grad_init, n, a->stage, st));
     if (grad_params)
         MPM_CUDA(cudaMemcpy(grad_params, a->pgrad_d, sizeof(double) * 2 * (size_t)S,
                             cudaMemcpyDeviceToHost));

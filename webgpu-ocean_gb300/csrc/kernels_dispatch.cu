@@ -131,6 +131,31 @@ __global__ void k_iota(uint32_t* __restrict__ id, int n) {
     if (j < n) id[j] = (uint32_t)j;
 }
 
+// 80-byte reference records (20 floats: x, pad, v, pad, C columns padded to
+// four) <-> the four float4 streams.  Record i is five aligned float4.
+__global__ void k_records_to_streams(const float4* __restrict__ rec, Particles P, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4* r = rec + 5 * (size_t)i;
+    const float4 a = r[0], b = r[1], c = r[2], d = r[3], e = r[4];
+    P.p0[i] = make_float4(a.x, a.y, a.z, c.x);
+    P.p1[i] = make_float4(c.y, c.z, d.x, d.y);
+    P.p2[i] = make_float4(d.z, e.x, e.y, e.z);
+    P.p3[i] = make_float4(b.x, b.y, b.z, 0.0f);
+}
+
+__global__ void k_streams_to_records(Particles P, float4* __restrict__ rec, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = P.p0[i], b = P.p1[i], c = P.p2[i], d = P.p3[i];
+    float4* r = rec + 5 * (size_t)i;
+    r[0] = make_float4(a.x, a.y, a.z, 0.0f);
+    r[1] = make_float4(d.x, d.y, d.z, 0.0f);
+    r[2] = make_float4(a.w, b.x, b.y, 0.0f);
+    r[3] = make_float4(b.z, b.w, c.x, 0.0f);
+    r[4] = make_float4(c.y, c.z, c.w, 0.0f);
+}
+
 __global__ void k_count_nonfinite(Particles P, int n, unsigned long long* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned bad = 0;
@@ -229,6 +254,16 @@ void launch_canonicalize(const Particles& src, const uint32_t* id, const Particl
 void launch_iota(uint32_t* id, int n, cudaStream_t st) {
     if (n <= 0) return;
     k_iota<<<blocks_for(n), kThreads, 0, st>>>(id, n);
+}
+
+void launch_records_to_streams(const float* rec, const Particles& P, int n, cudaStream_t st) {
+    if (n <= 0) return;
+    k_records_to_streams<<<blocks_for(n), kThreads, 0, st>>>(reinterpret_cast<const float4*>(rec), P, n);
+}
+
+void launch_streams_to_records(const Particles& P, float* rec, int n, cudaStream_t st) {
+    if (n <= 0) return;
+    k_streams_to_records<<<blocks_for(n), kThreads, 0, st>>>(P, reinterpret_cast<float4*>(rec), n);
 }
 
 void launch_count_nonfinite(const Particles& P, int n, unsigned long long* out, cudaStream_t st) {

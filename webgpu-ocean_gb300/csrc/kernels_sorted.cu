@@ -1128,7 +1128,6 @@ bool make_geo(const SimConsts& k, Geo& g) {
 int ensure_grid_state(SortedEngine* e, long long bricks, long long bins) {
     const size_t cells = (size_t)bricks * 64;
     const long long max_tasks = bins + (long long)e->max_particles / kMinTaskCap + 2;
-    drop_graphs(e);
     if (cells <= e->grid_cells_alloc && bricks <= e->bricks_alloc && max_tasks <= e->max_tasks)
         return 0;
     free_grid_state(e);
@@ -1213,13 +1212,18 @@ int sorted_configure(SortedEngine* e, const SimConsts& k) {
     e->has_grid = false;
     Geo g;
     if (!make_geo(k, g)) return -1;
+    // Captured graphs hold the scene by value: they stay valid across a
+    // reconfiguration with the same constants and geometry (a re-upload of
+    // the same scene) and are dropped otherwise.
+    Scene one{};
+    one.g = g;
+    one.k = k;
+    if (e->batch || std::memcmp(&one, &e->one, sizeof(Scene)) != 0) drop_graphs(e);
     if (ensure_grid_state(e, g.nbricks, (long long)g.nbricks + 1)) return -1;
     free_tables(e);
     e->batch = false;
     e->scenes.clear();
-    e->one = Scene{};
-    e->one.g = g;
-    e->one.k = k;
+    e->one = one;
     e->nbricks = g.nbricks;
     e->nbins = g.nbricks + 1;
     apply_task_cap(e, k.n);
@@ -1256,6 +1260,7 @@ int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes) {
             return -1;
         }
     }
+    drop_graphs(e);
     if (ensure_grid_state(e, bricks, bins)) return -1;
     free_tables(e);
     std::vector<uint32_t> brick_scene((size_t)bricks), bin_scene((size_t)bins);

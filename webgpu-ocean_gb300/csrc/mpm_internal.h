@@ -78,6 +78,9 @@ void launch_copy_position(const Particles& P, float4* posvel, int n, cudaStream_
 void launch_canonicalize(const Particles& src, const uint32_t* id, const Particles& dst,
                          uint32_t* id_dst, int n, cudaStream_t st);
 void launch_iota(uint32_t* id, int n, cudaStream_t st);
+// 80-byte reference records (device, 16-byte aligned) <-> particle streams.
+void launch_records_to_streams(const float* rec, const Particles& P, int n, cudaStream_t st);
+void launch_streams_to_records(const Particles& P, float* rec, int n, cudaStream_t st);
 
 // Diagnostics.
 void launch_count_nonfinite(const Particles& P, int n, unsigned long long* out, cudaStream_t st);

@@ -417,6 +417,17 @@ class MLSMPMBatch:
         _check(self._lib.mpm_batch_step(self._handle, int(substeps),
                                         _stream_handle(commandEncoder)), "step")
 
+    def upload(self, particles: np.ndarray) -> None:
+        """Restarts every scene from new particle records (same counts and
+        order as at construction); keeps the captured CUDA graphs."""
+        recs = np.ascontiguousarray(particles, dtype=np.float32).reshape(-1, 20)
+        if recs.shape[0] != int(self.sceneOffsets[-1]):
+            raise ValueError("particle array does not match the scenes' particle counts")
+        with self._on_device():
+            _check(self._lib.mpm_batch_upload(self._handle,
+                                              recs.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+                   "upload")
+
     def execute(self, commandEncoder=None) -> None:
         """Two substeps of every scene (mls-mpm/mls-mpm.ts:245-268)."""
         self.step(2, commandEncoder)
