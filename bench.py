@@ -500,6 +500,46 @@ def measure_sph(pkg, torch, frames: int = 50) -> dict:
     return out
 
 
+def measure_expanding(pkg, torch, substeps: int = 40) -> dict:
+    """The inverse problem's 64 scenes (1.52M particles) stepped from their
+    initial state without CUDA graphs (one launch per kernel, for launch-level
+    profiles): the blocks expand over the rollout and every substep costs more
+    than the one before."""
+    descs, recs, _ = pkg.inverse.inverse_scenes(64, seed=BATCH_SEED)
+    b = pkg.MLSMPMBatch(descs, recs, graph=False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.step(substeps)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    out = {"particles": int(b.numParticles), "substeps": substeps, "ms": 1e3 * dt,
+           "health_ok": bool(b.checkHealth()["ok"])}
+    b.close()
+    return out
+
+
+def measure_adjoint_batch(pkg, torch, substeps: int = 40, every: int = 10) -> dict:
+    """One checkpointed forward and backward of the inverse problem's 64
+    scenes (1.52M particles) on the fixed-point tape (for kernel profiles)."""
+    import numpy as np
+    descs, recs, _ = pkg.inverse.inverse_scenes(64, seed=BATCH_SEED)
+    adj = pkg.MLSMPMAdjoint(descs, substeps, every, tape="fixed")
+    seed = np.zeros((len(recs), 20), np.float32)
+    seed[:, 0:3] = 1e-6
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    adj.forward(recs, substeps)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    g, _ = adj.backward({substeps: seed})
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    adj.close()
+    return {"particles": int(len(recs)), "substeps": substeps, "checkpoint_every": every,
+            "forward_ms": 1e3 * (t1 - t0), "backward_ms": 1e3 * (t2 - t1),
+            "grad_finite": bool(np.isfinite(g).all())}
+
+
 def run_only(which: str) -> None:
     import torch
     import __graft_entry__ as entry
@@ -513,6 +553,10 @@ def run_only(which: str) -> None:
         out = measure_render(pkg, torch)
     elif which == "sph":
         out = measure_sph(pkg, torch)
+    elif which == "expanding":
+        out = measure_expanding(pkg, torch)
+    elif which == "adjoint_batch":
+        out = measure_adjoint_batch(pkg, torch)
     else:
         out = measure_inverse(pkg)
     print(json.dumps({"only": which, which: out}), flush=True)
@@ -720,7 +764,8 @@ def main():
                     help="leave out the batched-scenes measurement")
     ap.add_argument("--skip-adjoint", action="store_true",
                     help="leave out the adjoint and inverse-problem measurements")
-    ap.add_argument("--only", choices=["batched", "adjoint", "inverse", "render", "sph"],
+    ap.add_argument("--only", choices=["batched", "adjoint", "inverse", "render", "sph",
+                                       "expanding", "adjoint_batch"],
                     help="run one side measurement alone and print its JSON (profiling)")
     ap.add_argument("--quick", action="store_true",
                     help="time the device-resident steps only (for profiler captures)")

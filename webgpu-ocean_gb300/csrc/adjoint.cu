@@ -46,6 +46,17 @@ namespace {
 
 constexpr int kThreads = 256;
 
+// Resident CTAs per SM the particle kernels ask the register allocator for
+// (one thread per particle, unbounded: k_adj_p2g2 ~160 registers, k_adj_g2p
+// ~124; capped at 2 and 3 CTAs of 256 threads they spill 68 and 120 bytes
+// and the 1.5M-particle backward runs ~5 % faster).
+#ifndef MPM_ADJ_P2G2_MIN_BLOCKS
+#define MPM_ADJ_P2G2_MIN_BLOCKS 2
+#endif
+#ifndef MPM_ADJ_G2P_MIN_BLOCKS
+#define MPM_ADJ_G2P_MIN_BLOCKS 3
+#endif
+
 struct Sten {
     float cf[3];     // floor(x)
     float w[3][3];   // w[axis][g]
@@ -353,7 +364,7 @@ __device__ __forceinline__ int slab_gx(int s, int q) { return L == 1 ? s : q; }
 // G = sum_n grad w_n v_n^T, H = sum_n 4 grad w_n (d_n . u_n) - 4 w_n u_n.
 // ---------------------------------------------------------------------------
 template <class Tape, int L>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, MPM_ADJ_G2P_MIN_BLOCKS)
     k_adj_g2p(Tape tp, Particles Aout, Particles Anew, float4* __restrict__ gadj,
               const AdjScene* __restrict__ scenes, const int* __restrict__ pscene,
               const int* __restrict__ perm, int n) {
@@ -504,7 +515,7 @@ __global__ void __launch_bounds__(kThreads)
 // Q = sum_n w_n g_n.
 // ---------------------------------------------------------------------------
 template <class Tape, int L>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, MPM_ADJ_P2G2_MIN_BLOCKS)
     k_adj_p2g2(Tape tp, Particles Anew, float4* __restrict__ gadj,
                const AdjScene* __restrict__ scenes, const int* __restrict__ pscene,
                const int* __restrict__ perm, int n, double* __restrict__ pgrad) {
