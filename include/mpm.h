@@ -126,6 +126,16 @@ int mpm_download_grid(mpm_sim* sim, int32_t* out_cells);
 /* Asynchronous on `stream`: copies n*32 B of posvel into host memory
  * (pinned memory makes it truly asynchronous). */
 int mpm_download_posvel(mpm_sim* sim, float* out_posvel, void* stream);
+/* Pipelined read-back for a frame loop (no counterpart in the reference,
+ * whose renderer reads posvel on the GPU): snapshots posvel on `stream` (a
+ * device-to-device copy) and copies the snapshot into `out_posvel` (pinned
+ * host memory) on the library's own copy stream, so the next mpm_execute on
+ * `stream` overlaps the transfer.  `out_posvel` holds the posvel of the call
+ * once mpm_wait_posvel returns. */
+int mpm_download_posvel_async(mpm_sim* sim, float* out_posvel, void* stream);
+/* Waits for the last mpm_download_posvel_async copy: on the host when
+ * `stream` is NULL, else makes `stream` wait for it. */
+int mpm_wait_posvel(mpm_sim* sim, void* stream);
 
 /* Enqueues one WGSL entry point alone (mls-mpm/mls-mpm.ts:248-265) on the
  * dispatch engine's state.  Running the six in order equals one substep. */

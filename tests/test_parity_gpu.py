@@ -326,3 +326,33 @@ def test_autotune_keeps_the_state(cuda, pkg, oracle_mod):
         ref.execute(2, NTHREADS)
     assert_state_equal(sim, ref, "after autotune")
     sim.close()
+
+
+def test_pipelined_posvel_readback(cuda, pkg):
+    """downloadPosvelAsync copies the posvel of the moment of the call, even
+    while the next execute() runs on the same stream."""
+    import torch
+    from oracle import scene as scene_mod
+    recs = scene_mod.lattice(20, 6.0, 0.5, 0.05, 9)
+    box = [40.0, 40.0, 40.0]
+    ref = pkg.MLSMPMSimulator(None, None, 1.2, maxParticles=len(recs), maxGrid=(40, 40, 40))
+    ref.upload(recs, box)
+    want = []
+    for _ in range(4):
+        ref.execute()
+        want.append(ref.downloadPosvel().copy())
+    ref.close()
+    sim = pkg.MLSMPMSimulator(None, None, 1.2, maxParticles=len(recs), maxGrid=(40, 40, 40))
+    sim.upload(recs, box)
+    stream = torch.cuda.Stream()
+    bufs = [torch.empty((len(recs), 8), dtype=torch.float32, pin_memory=True).numpy()
+            for _ in range(2)]
+    sim.execute(stream)
+    for i in range(4):
+        out = sim.downloadPosvelAsync(stream, out=bufs[i % 2])
+        sim.execute(stream)  # overlaps the copy; must not change `out`
+        sim.waitPosvel()
+        assert np.array_equal(out.view(np.uint32), want[i].view(np.uint32)), f"step {i}"
+    sim.waitPosvel(stream)
+    stream.synchronize()
+    sim.close()

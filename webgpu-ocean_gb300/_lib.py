@@ -132,6 +132,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "mpm_download_particles": (i32, [vp, fp]),
         "mpm_download_grid": (i32, [vp, ip]),
         "mpm_download_posvel": (i32, [vp, fp, vp]),
+        "mpm_download_posvel_async": (i32, [vp, fp, vp]),
+        "mpm_wait_posvel": (i32, [vp, vp]),
         "mpm_dispatch": (i32, [vp, i32, vp]),
         "mpm_set_engine": (i32, [vp, i32]),
         "mpm_get_engine": (i32, [vp]),

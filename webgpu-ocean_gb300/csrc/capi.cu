@@ -209,6 +209,10 @@ struct mpm_sim {
     SortedEngine* sorted = nullptr;
     cudaStream_t internal = nullptr;
     LaunchProfiler prof;
+    // pipelined posvel read-back (mpm_download_posvel_async), made on first use
+    float4* posvel_snap = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t snap_taken = nullptr, snap_copied = nullptr;
 
     SimConsts consts() const {
         SimConsts k{};
@@ -415,6 +419,10 @@ int mpm_destroy(mpm_sim* s) {
     if (s->posvel_owned) cudaFree(s->posvel);
     if (s->sorted) sorted_destroy(s->sorted);
     if (s->internal) cudaStreamDestroy(s->internal);
+    cudaFree(s->posvel_snap);
+    if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+    if (s->snap_taken) cudaEventDestroy(s->snap_taken);
+    if (s->snap_copied) cudaEventDestroy(s->snap_copied);
     s->prof.release();
     delete s;
     return MPM_OK;
@@ -640,6 +648,39 @@ int mpm_download_posvel(mpm_sim* s, float* out, void* stream) {
     if (s->n)
         MPM_CUDA(cudaMemcpyAsync(out, s->posvel, sizeof(float4) * 2 * (size_t)s->n,
                                  cudaMemcpyDeviceToHost, static_cast<cudaStream_t>(stream)));
+    return MPM_OK;
+}
+
+int mpm_download_posvel_async(mpm_sim* s, float* out, void* stream) {
+    if (int rc = check_sim(s)) return rc;
+    if (!out && s->n) return fail(MPM_E_INVALID, "null output");
+    DeviceGuard g(s->device);
+    if (!s->copy_stream) {
+        MPM_CUDA(cudaMalloc(&s->posvel_snap, sizeof(float4) * 2 * (size_t)(s->max_particles > 0 ? s->max_particles : 1)));
+        MPM_CUDA(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+        MPM_CUDA(cudaEventCreateWithFlags(&s->snap_taken, cudaEventDisableTiming));
+        MPM_CUDA(cudaEventCreateWithFlags(&s->snap_copied, cudaEventDisableTiming));
+        MPM_CUDA(cudaEventRecord(s->snap_copied, s->copy_stream));
+    }
+    if (!s->n) return MPM_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t bytes = sizeof(float4) * 2 * (size_t)s->n;
+    // the previous read-back has left the snapshot before it is overwritten
+    MPM_CUDA(cudaStreamWaitEvent(st, s->snap_copied, 0));
+    MPM_CUDA(cudaMemcpyAsync(s->posvel_snap, s->posvel, bytes, cudaMemcpyDeviceToDevice, st));
+    MPM_CUDA(cudaEventRecord(s->snap_taken, st));
+    MPM_CUDA(cudaStreamWaitEvent(s->copy_stream, s->snap_taken, 0));
+    MPM_CUDA(cudaMemcpyAsync(out, s->posvel_snap, bytes, cudaMemcpyDeviceToHost, s->copy_stream));
+    MPM_CUDA(cudaEventRecord(s->snap_copied, s->copy_stream));
+    return MPM_OK;
+}
+
+int mpm_wait_posvel(mpm_sim* s, void* stream) {
+    if (int rc = check_sim(s)) return rc;
+    if (!s->snap_copied) return MPM_OK;
+    DeviceGuard g(s->device);
+    if (stream) MPM_CUDA(cudaStreamWaitEvent(static_cast<cudaStream_t>(stream), s->snap_copied, 0));
+    else MPM_CUDA(cudaEventSynchronize(s->snap_copied));
     return MPM_OK;
 }
 

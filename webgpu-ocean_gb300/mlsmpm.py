@@ -178,6 +178,24 @@ class MLSMPMSimulator:
             self.synchronize()
         return out
 
+    def downloadPosvelAsync(self, commandEncoder=None, out: np.ndarray | None = None) -> np.ndarray:
+        """Pipelined read-back: snapshots posvel on the stream and copies it
+        to `out` (pinned host memory for real overlap) on the library's copy
+        stream; the next execute() overlaps the transfer.  `out` is valid
+        after waitPosvel()."""
+        if out is None:
+            out = np.zeros((self.numParticles, 8), dtype=np.float32)
+        _check(self._lib.mpm_download_posvel_async(
+            self._handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+            _stream_handle(commandEncoder)), "downloadPosvelAsync")
+        return out
+
+    def waitPosvel(self, commandEncoder=None) -> None:
+        """Waits for the last downloadPosvelAsync copy (on the host, or makes
+        the given stream wait)."""
+        _check(self._lib.mpm_wait_posvel(self._handle, _stream_handle(commandEncoder)),
+               "waitPosvel")
+
     def writeParticleBuffer(self) -> None:
         """Copies the particle records (80-byte layout) into particleBuffer."""
         import torch
