@@ -200,6 +200,9 @@ def run_reference(args) -> None:
 # capture of `bench.py --quick` on this workload: its posvel-writing variant
 # (profiles/k_g2p_p2g1_1M_128.md).
 MEASURED_TRAFFIC_PER_LAUNCH = {"sorted_g2p_p2g_1": 95.3e6}
+# ncu smsp__inst_executed.sum of one launch at the early dam-break state
+# (profiles/k_g2p_p2g1_1M_128.md): the instruction-issue roofline.
+MEASURED_WARP_INSTRUCTIONS_PER_LAUNCH = {"sorted_g2p_p2g_1": 76.7e6}
 
 
 def algorithmic_bytes(kernel: str, n: int, cells: int) -> float | None:
@@ -666,6 +669,20 @@ def run_ours(args) -> None:
                 "algorithmic_bytes_per_launch": abytes,
                 "mean_launch_us": avg_s * 1e6, "cells_touched": cells,
                 "kernel_share": top_ms / step_kernel_ms if step_kernel_ms else None}
+    # The kernel is bound by instruction issue and latency, not DRAM: its
+    # warp-instructions per launch over the same mean duration, against 4
+    # issues per SM per cycle at the sampled SM clock.
+    issue = None
+    instr = MEASURED_WARP_INSTRUCTIONS_PER_LAUNCH.get(top_name)
+    if roof is not None and instr and clocks.get("sm_mhz"):
+        nsm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+        peak_issue = 4.0 * nsm * clocks["sm_mhz"] * 1e6
+        got = instr / (roof["mean_launch_us"] * 1e-6)
+        issue = {"kernel": top_name, "achieved": got / 1e12, "peak": peak_issue / 1e12,
+                 "unit": "T warp-instructions/s", "frac": got / peak_issue,
+                 "warp_instructions_per_launch": instr,
+                 "source": "ncu smsp__inst_executed.sum of one early-state launch, "
+                           "profiles/k_g2p_p2g1_1M_128.md; peak = 4 x SMs x median SM clock"}
     kernels = {k: {"launches": v[0], "mean_us": 1e3 * v[2] / v[1] if v[1] else None,
                    "share": v[2] / step_kernel_ms if step_kernel_ms else None}
                for k, v in stats.items()}
@@ -769,6 +786,7 @@ def run_ours(args) -> None:
         "roofline": roof,
         "cpu_baseline": cpu,
         "clocks": clocks,
+        "issue_roofline": issue,
         "gpu_launches": launches,
         "wall_s_timed_region": wall,
         "kernels": kernels,
