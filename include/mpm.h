@@ -374,6 +374,9 @@ int mpm_sph_reset_dambreak(mpm_sph* sph, int num_particles, const double init_ha
 int mpm_sph_upload(mpm_sph* sph, const float* rec64, int n, const float real_half_box[3]);
 /* execute(commandEncoder), sph.ts:318-356: `substeps` (2 per frame) */
 int mpm_sph_step(mpm_sph* sph, int substeps, void* stream);
+/* Frames replay as CUDA graphs (captured once per substep and particle
+ * count); 0 launches every kernel each frame.  Results are the same. */
+int mpm_sph_set_graph(mpm_sph* sph, int enable); /* default 1 */
 /* changeBoxSize(realBoxSize), sph.ts:383-388 (half sizes) */
 int mpm_sph_set_real_box(mpm_sph* sph, const float real_half_box[3]);
 int mpm_sph_num_particles(const mpm_sph* sph);

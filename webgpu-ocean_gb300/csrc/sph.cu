@@ -314,10 +314,11 @@ __global__ void k_sph_force(const float4* __restrict__ SP, const float4* __restr
 
 // integrate.wgsl:37-64 and copyPosition.wgsl:27-37.
 __global__ void k_sph_integrate(float4* __restrict__ P, float4* __restrict__ V,
-                                const float4* __restrict__ F, int n, Env e, float rx, float ry,
-                                float rz, float4* __restrict__ posvel) {
+                                const float4* __restrict__ F, int n, Env e,
+                                const float* __restrict__ box, float4* __restrict__ posvel) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const float rx = box[0], ry = box[1], rz = box[2];
     float4 p = P[i], v = V[i];
     const float dens = p.w;
     if (dens != 0.0f) {
@@ -396,11 +397,28 @@ struct mpm_sph {
     int* cell_of = nullptr;
     unsigned *count = nullptr, *start = nullptr, *rank = nullptr, *order = nullptr;
     unsigned* sums = nullptr;  // per-CTA count sums of the scan
+    // the real box as the kernels read it (a device uniform, so that a
+    // captured frame graph survives changeBoxSize)
+    float* box_d = nullptr;
+    float box_uploaded[3] = {NAN, NAN, NAN};
+    bool graph = true;
+    struct FrameGraph {
+        int substeps, n;
+        cudaGraphExec_t exec;
+    };
+    std::vector<FrameGraph> graphs;
 };
 
 namespace {
 
+void drop_graphs(mpm_sph* s) {
+    for (auto& g : s->graphs) cudaGraphExecDestroy(g.exec);
+    s->graphs.clear();
+}
+
 void free_sph(mpm_sph* s) {
+    drop_graphs(s);
+    cudaFree(s->box_d);
     cudaFree(s->P); cudaFree(s->V); cudaFree(s->F); cudaFree(s->SP); cudaFree(s->SV);
     if (s->posvel_owned) cudaFree(s->posvel);
     cudaFree(s->cell_of); cudaFree(s->count); cudaFree(s->start); cudaFree(s->rank);
@@ -482,6 +500,7 @@ int mpm_sph_create(int max_particles, float render_diameter, void* posvel_device
     if (err == cudaSuccess) err = cudaMalloc(&s->count, 4 * ((size_t)s->e.total + 1));
     if (err == cudaSuccess) err = cudaMalloc(&s->start, 4 * ((size_t)s->e.total + 1));
     if (err == cudaSuccess) err = cudaMalloc(&s->sums, 4 * ((size_t)s->e.total / kScan + 2));
+    if (err == cudaSuccess) err = cudaMalloc(&s->box_d, sizeof(float) * 3);
     if (err != cudaSuccess) {
         const int rc = cuda_fail(err, "mpm_sph_create");
         free_sph(s);
@@ -563,13 +582,12 @@ int mpm_sph_set_real_box(mpm_sph* s, const float real_half[3]) {
     return MPM_OK;
 }
 
-// execute (sph.ts:325-355): `substeps` x (grid clear, build, prefix sum,
-// reorder, density, reorder, force, integrate, copyPosition).
-int mpm_sph_step(mpm_sph* s, int substeps, void* stream) {
-    if (!s || substeps < 0) return fail(MPM_E_INVALID, "bad arguments");
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
+}  // extern "C"
+
+namespace {
+
+void enqueue_substeps(mpm_sph* s, int substeps, cudaStream_t st) {
     const int n = s->n;
-    if (n == 0 || substeps == 0) return MPM_OK;
     const Env& e = s->e;
     const int pb = (n + 255) / 256, cb = (e.total + 255) / 256;
     for (int k = 0; k < substeps; ++k) {
@@ -585,11 +603,68 @@ int mpm_sph_step(mpm_sph* s, int substeps, void* stream) {
         k_sph_gather<<<pb, 256, 0, st>>>(s->P, s->V, s->order, s->start + e.total, s->SP, s->SV);
         k_sph_density<<<pb, 256, 0, st>>>(s->P, s->V, s->SP, s->SV, s->order, s->start, e);
         k_sph_force<<<pb, 256, 0, st>>>(s->SP, s->SV, s->order, s->start, e, s->F);
-        k_sph_integrate<<<pb, 256, 0, st>>>(s->P, s->V, s->F, n, e, s->real_half[0],
-                                            s->real_half[1], s->real_half[2], s->posvel);
+        k_sph_integrate<<<pb, 256, 0, st>>>(s->P, s->V, s->F, n, e, s->box_d, s->posvel);
+    }
+}
+
+// The frame's launches as a CUDA graph, captured once per (substeps,
+// particle count) and replayed.
+cudaError_t launch_graph(mpm_sph* s, int substeps, cudaStream_t st) {
+    mpm_sph::FrameGraph* hit = nullptr;
+    for (auto& g : s->graphs)
+        if (g.substeps == substeps && g.n == s->n) hit = &g;
+    if (!hit) {
+        cudaStream_t cs = nullptr;
+        cudaError_t err = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+        if (err != cudaSuccess) return err;
+        cudaGraph_t graph = nullptr;
+        err = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (err == cudaSuccess) {
+            enqueue_substeps(s, substeps, cs);
+            err = cudaStreamEndCapture(cs, &graph);
+        }
+        cudaGraphExec_t exec = nullptr;
+        if (err == cudaSuccess) err = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        cudaStreamDestroy(cs);
+        if (err != cudaSuccess) return err;
+        s->graphs.push_back({substeps, s->n, exec});
+        hit = &s->graphs.back();
+    }
+    return cudaGraphLaunch(hit->exec, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+// execute (sph.ts:325-355): `substeps` x (grid clear, build, prefix sum,
+// reorder, density, reorder, force, integrate, copyPosition).
+int mpm_sph_step(mpm_sph* s, int substeps, void* stream) {
+    if (!s || substeps < 0) return fail(MPM_E_INVALID, "bad arguments");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (s->n == 0 || substeps == 0) return MPM_OK;
+    if (std::memcmp(s->box_uploaded, s->real_half, sizeof(s->real_half)) != 0) {
+        // pageable source: staged before the call returns
+        const cudaError_t err =
+            cudaMemcpyAsync(s->box_d, s->real_half, sizeof(s->real_half), cudaMemcpyHostToDevice, st);
+        if (err != cudaSuccess) return cuda_fail(err, "mpm_sph_step");
+        std::memcpy(s->box_uploaded, s->real_half, sizeof(s->real_half));
+    }
+    if (s->graph) {
+        const cudaError_t err = launch_graph(s, substeps, st);
+        if (err != cudaSuccess) return cuda_fail(err, "mpm_sph_step graph");
+    } else {
+        enqueue_substeps(s, substeps, st);
     }
     const cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return cuda_fail(err, "mpm_sph_step");
+    return MPM_OK;
+}
+
+int mpm_sph_set_graph(mpm_sph* s, int enable) {
+    if (!s) return fail(MPM_E_INVALID, "bad arguments");
+    s->graph = enable != 0;
     return MPM_OK;
 }
 

@@ -54,6 +54,10 @@ class SPHSimulator:
         _check(self._lib.mpm_sph_step(self._handle, int(substeps), _stream_handle(commandEncoder)),
                "execute")
 
+    def setGraph(self, enable: bool) -> None:
+        """Replay frames as CUDA graphs (default) or launch every kernel."""
+        _check(self._lib.mpm_sph_set_graph(self._handle, int(bool(enable))), "setGraph")
+
     def changeBoxSize(self, realBoxSize) -> None:
         """sph.ts:383-388 (half sizes)."""
         b = (ctypes.c_float * 3)(*[float(x) for x in realBoxSize])
