@@ -226,3 +226,23 @@ def test_inverse_problem_recovers_constants(cuda, pkg):
     assert h[-1]["loss"].mean() < 0.1 * h[0]["loss"].mean()
     assert np.median(r["rel_err"][:, 0]) < 0.05
     assert np.isfinite(r["recovered"]).all()
+
+
+@pytest.mark.parametrize("tape", ["fixed", "fp64"])
+def test_repeated_backward_after_one_forward(cuda, pkg, tape):
+    """A second and third backward after the same forward (the first one used
+    the forward's record of the last segment, later ones recompute it) give
+    the same gradients as the first."""
+    from oracle import scene as scene_mod
+    recs = lattice_with_velocity(scene_mod, 10, 9.0)
+    adj = pkg.MLSMPMAdjoint([pkg.scene_desc(len(recs), [32.0, 32.0, 32.0])], 25, 10, tape=tape)
+    adj.forward(recs, 25)
+    _, seed = pkg.centroid_loss(adj.state(25), TARGET)
+    outs = [adj.backward({25: seed}) for _ in range(3)]
+    adj.close()
+    for g, p in outs[1:]:
+        # float atomics make the summation order differ between runs
+        np.testing.assert_allclose(g, outs[0][0], rtol=1e-4,
+                                   atol=1e-5 * float(np.abs(outs[0][0]).max()))
+        np.testing.assert_allclose(p, outs[0][1], rtol=1e-4)
+    assert np.isfinite(outs[0][0]).all()

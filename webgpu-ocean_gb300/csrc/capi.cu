@@ -1159,6 +1159,14 @@ struct mpm_adjoint {
     int* pscene_d = nullptr;
     double* pgrad_d = nullptr;
     AdjSort sort;                    // per-substep spatial sort of the adjoint kernels
+    std::vector<Particles> seedbuf;  // seeds of mpm_backward, kept between calls
+    // The backward as one CUDA graph, captured for (T, every, tape, seed
+    // substeps) and replayed while they stay the same.
+    cudaGraphExec_t bgraph = nullptr;
+    int bg_T = -1, bg_every = 0, bg_tape = -1, bg_cur = 0;
+    bool last_taped = false;         // the forward recorded its last segment's tape
+    bool bg_last_taped = false;
+    std::vector<int> bg_steps;
     int ncells = 0;
     std::vector<int> lbase;
     std::vector<int> bbase;          // first brick of each scene in the sort
@@ -1292,7 +1300,15 @@ cudaError_t alloc_tape(mpm_adjoint* a) {
     return e;
 }
 
+void drop_backward_graph(mpm_adjoint* a) {
+    if (a->bgraph) cudaGraphExecDestroy(a->bgraph);
+    a->bgraph = nullptr;
+    a->bg_T = -1;
+}
+
 void free_adjoint(mpm_adjoint* a) {
+    drop_backward_graph(a);
+    for (Particles& P : a->seedbuf) free_particles(P);
     free_tapes(a);
     free_particles(a->adj[0]);
     free_particles(a->adj[1]);
@@ -1334,6 +1350,77 @@ int adj_lanes(long long n) {
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1)
         nsm = 1;
     return n < 512LL * nsm ? 3 : 1;
+}
+
+// The whole backward of the last forward, enqueued on `st` (kernels,
+// memsets and device copies only, so it can be captured): for each
+// checkpoint segment from the last, recompute its states and updated grids
+// (unless the full tape kept them), then run its adjoint substeps in reverse,
+// adding the seeds at their substeps.  *cur_out: the adjoint buffer that
+// ends up holding dL/dS_0.
+int enqueue_backward(mpm_adjoint* a, const int* seed_steps, int nseeds, cudaStream_t st,
+                     int* cur_out) {
+    mpm_batch* b = a->b;
+    const int n = b->n, S = (int)b->consts.size();
+    const bool f64 = a->tape == MPM_TAPE_FP64;
+    auto add_seeds = [&](int step, const Particles& A) {
+        for (int i = 0; i < nseeds; ++i)
+            if (seed_steps[i] == step) launch_particles_axpy(A, a->seedbuf[(size_t)i], n, st);
+    };
+    int cur = 0;
+    float4* z[4] = {a->adj[0].p0, a->adj[0].p1, a->adj[0].p2, a->adj[0].p3};
+    for (int q = 0; q < 4; ++q) MPM_CUDA(cudaMemsetAsync(z[q], 0, sizeof(float4) * (size_t)n, st));
+    MPM_CUDA(cudaMemsetAsync(a->pgrad_d, 0, sizeof(double) * 2 * (size_t)S, st));
+    add_seeds(a->T, a->adj[cur]);
+    const int nseg = (a->T + a->every - 1) / a->every;
+    const size_t nc = (size_t)a->ncells;
+    for (int j = nseg - 1; j >= 0; --j) {
+        const int t0 = j * a->every;
+        const int t1 = t0 + a->every < a->T ? t0 + a->every : a->T;
+        // recompute the segment: states and updated grids of every substep
+        // (a full tape kept them all)
+        const size_t g0 = full_tape(a) ? (size_t)t0 : 0;  // tape grid of substep t0
+        if (full_tape(a) || (a->last_taped && j == nseg - 1)) {
+        } else if (f64) {
+            const double* curS = a->ckpt64[(size_t)j];
+            for (int t = t0; t < t1; ++t) {
+                double* dst = t + 1 < t1 ? a->seg64[(size_t)(t + 1 - t0)] : a->scratch64[0];
+                launch_substep64(curS, a->gtape64 + (size_t)(t - t0) * nc, dst, a->scenes_d, S,
+                                 a->pscene_d, n, a->ncells, st);
+                curS = dst;
+            }
+        } else {
+            if (cudaError_t e = batch_load_device(b, a->ckpt[(size_t)j], st); e != cudaSuccess)
+                return cuda_fail(e, "mpm_backward recompute");
+            for (int t = t0; t < t1; ++t) {
+                if (sorted_step(b->sorted, &b->ps, b->posvel, b->counters, b->consts[0], 1, st,
+                                &b->prof, b->graph) != 0 ||
+                    sorted_export_all(b->sorted, a->gtape + (size_t)(t - t0) * nc, st, &b->prof) != 0)
+                    return fail(MPM_E_CUDA, std::string("backward recompute: ") + sorted_error());
+                b->stepped = true;
+                if (t + 1 < t1) batch_canonical_to(b, a->seg[(size_t)(t + 1 - t0)], st);
+            }
+        }
+        // adjoint substeps in reverse
+        for (int t = t1 - 1; t >= t0; --t) {
+            if (f64) {
+                const double* Sx = t == t0 ? a->ckpt64[(size_t)j] : a->seg64[(size_t)(t - t0)];
+                launch_adjoint_substep64(Sx, a->gtape64 + (g0 + (size_t)(t - t0)) * nc, a->adj[cur],
+                                         a->adj[cur ^ 1], a->gadj, a->scenes_d, S, a->pscene_d, n,
+                                         a->ncells, a->pgrad_d, a->sort, st);
+            } else {
+                const Particles& Sx = t == t0 ? a->ckpt[(size_t)j] : a->seg[(size_t)(t - t0)];
+                launch_adjoint_substep(Sx, a->gtape + (g0 + (size_t)(t - t0)) * nc, a->adj[cur],
+                                       a->adj[cur ^ 1], a->gadj, a->scenes_d, S, a->pscene_d, n,
+                                       a->ncells, a->pgrad_d, a->sort, st);
+            }
+            cur ^= 1;
+            add_seeds(t, a->adj[cur]);
+        }
+    }
+    MPM_CUDA(cudaGetLastError());
+    *cur_out = cur;
+    return MPM_OK;
 }
 
 // Checkpoint slot of the state after `step` substeps of a T-substep forward
@@ -1437,6 +1524,7 @@ int mpm_adjoint_set_tape(mpm_adjoint* a, int tape) {
     MPM_CUDA(cudaDeviceSynchronize());
     a->tape = tape;
     a->T = -1;
+    drop_backward_graph(a);  // it holds the old tape's buffers
     MPM_CUDA(alloc_tape(a));
     return MPM_OK;
 }
@@ -1461,13 +1549,24 @@ int mpm_forward_ckpt(mpm_adjoint* a, const float* init, int substeps, void* stre
     const int n = b->n, S = (int)b->consts.size();
     a->T = -1;
     MPM_CUDA(cudaStreamSynchronize(st));
+    // The last checkpoint segment is the first one the backward needs: its
+    // states and updated grids are recorded here, as the backward's
+    // recompute would record them, so that it is not recomputed.
+    const int nseg = (substeps + a->every - 1) / a->every;
+    const int last_t0 = nseg > 0 ? (nseg - 1) * a->every : 0;
+    const bool tape_last = !full_tape(a) && substeps > 0;
+    const size_t nc = (size_t)a->ncells;
     if (a->tape == MPM_TAPE_FP64) {
         MPM_CUDA(upload_records64(a->ckpt64[0], init, n, a->stage, st));
         const double* cur = a->ckpt64[0];
         for (int t = 0; t < substeps; ++t) {
             const int slot = ckpt_slot(a, t + 1, substeps);
             double* dst = slot >= 0 ? a->ckpt64[(size_t)slot] : a->scratch64[t & 1];
-            double4* G = a->gtape64 + (full_tape(a) ? (size_t)t * (size_t)a->ncells : 0);
+            double4* G = a->gtape64 + (full_tape(a) ? (size_t)t * nc : 0);
+            if (tape_last && t >= last_t0) {
+                G = a->gtape64 + (size_t)(t - last_t0) * nc;
+                if (t + 1 < substeps) dst = a->seg64[(size_t)(t + 1 - last_t0)];
+            }
             launch_substep64(cur, G, dst, a->scenes_d, S, a->pscene_d, n, a->ncells, st);
             cur = dst;
         }
@@ -1476,6 +1575,18 @@ int mpm_forward_ckpt(mpm_adjoint* a, const float* init, int substeps, void* stre
         MPM_CUDA(batch_load_device(b, a->ckpt[0], st));
         int t = 0;
         while (t < substeps) {
+            if (tape_last && t >= last_t0) {  // one substep at a time, recording
+                if (sorted_step(b->sorted, &b->ps, b->posvel, b->counters, b->consts[0], 1, st,
+                                &b->prof, b->graph) != 0 ||
+                    sorted_export_all(b->sorted, a->gtape + (size_t)(t - last_t0) * nc, st,
+                                      &b->prof) != 0)
+                    return fail(MPM_E_CUDA, std::string("forward: ") + sorted_error());
+                b->stepped = true;
+                ++t;
+                if (t < substeps) batch_canonical_to(b, a->seg[(size_t)(t - last_t0)], st);
+                else batch_canonical_to(b, a->ckpt[(size_t)ckpt_slot(a, t, substeps)], st);
+                continue;
+            }
             const int ns = substeps - t < a->every ? substeps - t : a->every;
             if (sorted_step(b->sorted, &b->ps, b->posvel, b->counters, b->consts[0], ns, st,
                             &b->prof, b->graph) != 0)
@@ -1491,6 +1602,7 @@ int mpm_forward_ckpt(mpm_adjoint* a, const float* init, int substeps, void* stre
     }
     MPM_CUDA(cudaGetLastError());
     a->T = substeps;
+    a->last_taped = tape_last;
     return MPM_OK;
 }
 
@@ -1520,83 +1632,64 @@ int mpm_backward(mpm_adjoint* a, const float* seeds, const int* seed_steps, int 
     DeviceGuard g(b->device);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int n = b->n, S = (int)b->consts.size();
-    const bool f64 = a->tape == MPM_TAPE_FP64;
     MPM_CUDA(cudaStreamSynchronize(st));
-    std::vector<Particles> sbuf((size_t)nseeds);
-    auto release = [&]() {
-        for (Particles& P : sbuf) free_particles(P);
-    };
-    for (int i = 0; i < nseeds; ++i) {
-        cudaError_t e = alloc_particles(sbuf[(size_t)i], (size_t)(n > 0 ? n : 1));
-        if (e == cudaSuccess)
-            e = upload_records(sbuf[(size_t)i], seeds + (size_t)i * 20 * (size_t)n, n, a->stage, st);
+    // seeds into device streams kept between calls (a captured backward
+    // reads them at fixed addresses)
+    while ((int)a->seedbuf.size() < nseeds) {
+        drop_backward_graph(a);
+        Particles P{};
+        const cudaError_t e = alloc_particles(P, (size_t)(n > 0 ? n : 1));
         if (e != cudaSuccess) {
-            release();
+            free_particles(P);
             return cuda_fail(e, "mpm_backward seeds");
         }
+        a->seedbuf.push_back(P);
     }
-    auto add_seeds = [&](int step, const Particles& A) {
-        for (int i = 0; i < nseeds; ++i)
-            if (seed_steps[i] == step) launch_particles_axpy(A, sbuf[(size_t)i], n, st);
-    };
+    for (int i = 0; i < nseeds; ++i)
+        MPM_CUDA(upload_records(a->seedbuf[(size_t)i], seeds + (size_t)i * 20 * (size_t)n, n,
+                                a->stage, st));
+    const std::vector<int> steps(seed_steps, seed_steps + nseeds);
     int cur = 0;
-    float4* z[4] = {a->adj[0].p0, a->adj[0].p1, a->adj[0].p2, a->adj[0].p3};
-    for (int q = 0; q < 4; ++q) MPM_CUDA(cudaMemsetAsync(z[q], 0, sizeof(float4) * (size_t)n, st));
-    MPM_CUDA(cudaMemsetAsync(a->pgrad_d, 0, sizeof(double) * 2 * (size_t)S, st));
-    add_seeds(a->T, a->adj[cur]);
-    const int nseg = (a->T + a->every - 1) / a->every;
-    const size_t nc = (size_t)a->ncells;
-    for (int j = nseg - 1; j >= 0; --j) {
-        const int t0 = j * a->every;
-        const int t1 = t0 + a->every < a->T ? t0 + a->every : a->T;
-        // recompute the segment: states and updated grids of every substep
-        // (a full tape kept them all)
-        const size_t g0 = full_tape(a) ? (size_t)t0 : 0;  // tape grid of substep t0
-        if (full_tape(a)) {
-        } else if (f64) {
-            const double* curS = a->ckpt64[(size_t)j];
-            for (int t = t0; t < t1; ++t) {
-                double* dst = t + 1 < t1 ? a->seg64[(size_t)(t + 1 - t0)] : a->scratch64[0];
-                launch_substep64(curS, a->gtape64 + (size_t)(t - t0) * nc, dst, a->scenes_d, S,
-                                 a->pscene_d, n, a->ncells, st);
-                curS = dst;
-            }
-        } else {
-            if (cudaError_t e = batch_load_device(b, a->ckpt[(size_t)j], st); e != cudaSuccess) {
-                release();
-                return cuda_fail(e, "mpm_backward recompute");
-            }
-            for (int t = t0; t < t1; ++t) {
-                if (sorted_step(b->sorted, &b->ps, b->posvel, b->counters, b->consts[0], 1, st,
-                                &b->prof, b->graph) != 0 ||
-                    sorted_export_all(b->sorted, a->gtape + (size_t)(t - t0) * nc, st, &b->prof) != 0) {
-                    release();
-                    return fail(MPM_E_CUDA, std::string("backward recompute: ") + sorted_error());
-                }
-                b->stepped = true;
-                if (t + 1 < t1) batch_canonical_to(b, a->seg[(size_t)(t + 1 - t0)], st);
-            }
+    if (b->prof.enabled) {  // per-launch profiling: no graph
+        if (int rc = enqueue_backward(a, seed_steps, nseeds, st, &cur)) return rc;
+    } else if (a->bgraph && a->bg_T == a->T && a->bg_every == a->every && a->bg_tape == a->tape &&
+               a->bg_last_taped == a->last_taped && a->bg_steps == steps) {
+        MPM_CUDA(cudaGraphLaunch(a->bgraph, st));
+        cur = a->bg_cur;
+    } else {
+        drop_backward_graph(a);
+        cudaStream_t cs = nullptr;
+        MPM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        const bool engine_graph = b->graph;
+        b->graph = false;  // the engine's kernels go straight into this graph
+        cudaGraph_t graph = nullptr;
+        int rc = 0;
+        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            rc = enqueue_backward(a, seed_steps, nseeds, cs, &cur);
+            e = cudaStreamEndCapture(cs, &graph);
         }
-        // adjoint substeps in reverse
-        for (int t = t1 - 1; t >= t0; --t) {
-            if (f64) {
-                const double* Sx = t == t0 ? a->ckpt64[(size_t)j] : a->seg64[(size_t)(t - t0)];
-                launch_adjoint_substep64(Sx, a->gtape64 + (g0 + (size_t)(t - t0)) * nc, a->adj[cur],
-                                         a->adj[cur ^ 1], a->gadj, a->scenes_d, S, a->pscene_d, n,
-                                         a->ncells, a->pgrad_d, a->sort, st);
-            } else {
-                const Particles& Sx = t == t0 ? a->ckpt[(size_t)j] : a->seg[(size_t)(t - t0)];
-                launch_adjoint_substep(Sx, a->gtape + (g0 + (size_t)(t - t0)) * nc, a->adj[cur],
-                                       a->adj[cur ^ 1], a->gadj, a->scenes_d, S, a->pscene_d, n,
-                                       a->ncells, a->pgrad_d, a->sort, st);
-            }
-            cur ^= 1;
-            add_seeds(t, a->adj[cur]);
-        }
+        b->graph = engine_graph;
+        cudaGraphExec_t exec = nullptr;
+        if (e == cudaSuccess && rc == 0) e = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        cudaStreamDestroy(cs);
+        if (rc) return rc;
+        if (e != cudaSuccess) return cuda_fail(e, "mpm_backward capture");
+        a->bgraph = exec;
+        a->bg_T = a->T;
+        a->bg_every = a->every;
+        a->bg_tape = a->tape;
+        a->bg_last_taped = a->last_taped;
+        a->bg_steps = steps;
+        a->bg_cur = cur;
+        MPM_CUDA(cudaGraphLaunch(exec, st));
     }
+    // the recompute of the earlier segments reused the buffers that held the
+    // forward's record of the last one: a further backward recomputes it
+    a->last_taped = false;
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    release();
     if (e != cudaSuccess) return cuda_fail(e, "mpm_backward");
     if (grad_init) MPM_CUDA(download_records(a->adj[cur], grad_init, n, a->stage, st));
     if (grad_params)
