@@ -315,6 +315,10 @@ int mpm_adjoint_state(mpm_adjoint* adj, int substep, float* out_aos80);
  * (synchronizes). */
 int mpm_backward(mpm_adjoint* adj, const float* seeds_aos80, const int* seed_substeps,
                  int num_seeds, float* grad_init_aos80, double* grad_params, void* stream);
+/* The same with one pointer per seed block (no contiguous array of all
+ * seeds needed). */
+int mpm_backward_list(mpm_adjoint* adj, const float* const* seeds_aos80, const int* seed_substeps,
+                      int num_seeds, float* grad_init_aos80, double* grad_params, void* stream);
 
 /* Headless screen-space renderer (render/fluidRender.ts, fluid path):
  * depth splat, 4 x bilateral filter, thickness splat, gaussian filter and

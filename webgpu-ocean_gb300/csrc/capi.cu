@@ -1622,10 +1622,22 @@ int mpm_adjoint_state(mpm_adjoint* a, int substep, float* out) {
 int mpm_backward(mpm_adjoint* a, const float* seeds, const int* seed_steps, int nseeds,
                  float* grad_init, double* grad_params, void* stream) {
     if (!a) return fail(MPM_E_INVALID, "null adjoint handle");
+    if (nseeds < 0 || (nseeds > 0 && (!seeds || !seed_steps)))
+        return fail(MPM_E_INVALID, "bad seeds");
+    std::vector<const float*> list((size_t)(nseeds > 0 ? nseeds : 1));
+    for (int i = 0; i < nseeds; ++i) list[(size_t)i] = seeds + (size_t)i * 20 * (size_t)a->b->n;
+    return mpm_backward_list(a, list.data(), seed_steps, nseeds, grad_init, grad_params, stream);
+}
+
+int mpm_backward_list(mpm_adjoint* a, const float* const* seeds, const int* seed_steps, int nseeds,
+                      float* grad_init, double* grad_params, void* stream) {
+    if (!a) return fail(MPM_E_INVALID, "null adjoint handle");
     mpm_batch* b = a->b;
     if (a->T < 0) return fail(MPM_E_STATE, "no forward run");
     if (nseeds < 0 || (nseeds > 0 && (!seeds || !seed_steps)))
         return fail(MPM_E_INVALID, "bad seeds");
+    for (int i = 0; i < nseeds; ++i)
+        if (!seeds[i] && b->n) return fail(MPM_E_INVALID, "null seed block");
     for (int i = 0; i < nseeds; ++i)
         if (seed_steps[i] < 0 || seed_steps[i] > a->T)
             return fail(MPM_E_INVALID, "seed substep outside [0, T]");
@@ -1646,8 +1658,7 @@ int mpm_backward(mpm_adjoint* a, const float* seeds, const int* seed_steps, int 
         a->seedbuf.push_back(P);
     }
     for (int i = 0; i < nseeds; ++i)
-        MPM_CUDA(upload_records(a->seedbuf[(size_t)i], seeds + (size_t)i * 20 * (size_t)n, n,
-                                a->stage, st));
+        MPM_CUDA(upload_records(a->seedbuf[(size_t)i], seeds[i], n, a->stage, st));
     const std::vector<int> steps(seed_steps, seed_steps + nseeds);
     int cur = 0;
     if (b->prof.enabled) {  // per-launch profiling: no graph

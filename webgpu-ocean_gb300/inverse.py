@@ -60,6 +60,7 @@ def fit_parameters(adj: MLSMPMAdjoint, init: np.ndarray, observed: dict, substep
     m = np.zeros_like(theta)
     v = np.zeros_like(theta)
     steps = sorted(observed)
+    per_particle = np.repeat(counts, np.diff(offs))[:, None]  # its scene's particle count
     history = []
     t0 = time.perf_counter()
     for it in range(iters):
@@ -71,11 +72,9 @@ def fit_parameters(adj: MLSMPMAdjoint, init: np.ndarray, observed: dict, substep
         for t in steps:
             x = adj.state(t)
             diff = x[:, 0:3].astype(np.float64) - observed[t]
+            loss += np.add.reduceat(np.einsum("ij,ij->i", diff, diff), offs[:-1]) / counts
             seed = np.zeros_like(x)
-            for s in range(S):
-                lo, hi = offs[s], offs[s + 1]
-                loss[s] += np.mean(np.sum(diff[lo:hi] ** 2, axis=1))
-                seed[lo:hi, 0:3] = (2.0 * diff[lo:hi] / counts[s]).astype(np.float32)
+            seed[:, 0:3] = (2.0 * diff / per_particle).astype(np.float32)
             seeds[t] = seed
         _, pgrad = adj.backward(seeds)
         g = pgrad * params  # d/d log(p) = p * d/dp

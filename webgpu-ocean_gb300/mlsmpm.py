@@ -598,17 +598,16 @@ class MLSMPMAdjoint:
     def backward(self, seeds: dict, commandEncoder=None):
         steps = sorted(seeds)
         n = self.numParticles
-        block = np.zeros((max(len(steps), 1), n, 20), dtype=np.float32)
-        for j, t in enumerate(steps):
-            block[j] = np.asarray(seeds[t], dtype=np.float32).reshape(n, 20)
+        blocks = [np.ascontiguousarray(seeds[t], dtype=np.float32).reshape(n, 20) for t in steps]
+        fp = ctypes.POINTER(ctypes.c_float)
+        ptrs = (fp * max(len(steps), 1))(*[b.ctypes.data_as(fp) for b in blocks])
         st = (ctypes.c_int32 * max(len(steps), 1))(*[int(t) for t in steps])
-        grad = np.zeros((n, 20), dtype=np.float32)
+        grad = np.empty((n, 20), dtype=np.float32)
         pgrad = np.zeros((self.numScenes, 2), dtype=np.float64)
-        _check(self._lib.mpm_backward(self._handle,
-                                      block.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), st,
-                                      len(steps), grad.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
-                                      pgrad.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
-                                      _stream_handle(commandEncoder)), "backward")
+        _check(self._lib.mpm_backward_list(self._handle, ptrs, st, len(steps),
+                                           grad.ctypes.data_as(fp),
+                                           pgrad.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                           _stream_handle(commandEncoder)), "backward")
         return grad, pgrad
 
     def close(self) -> None:
