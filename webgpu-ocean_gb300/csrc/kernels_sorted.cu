@@ -86,6 +86,12 @@ constexpr int kMaxTaskCap = 1 << 30;
 #ifndef MPM_P2G2_MIN_BLOCKS
 #define MPM_P2G2_MIN_BLOCKS (1024 / MPM_TASK_THREADS)
 #endif
+// Tasks with fewer particles than this skip the bank-class lane table (its
+// barriers and position loads cost more than the bank conflicts it saves
+// when a brick holds a few dozen particles) and keep the bin order.
+#ifndef MPM_LANE_TABLE_MIN
+#define MPM_LANE_TABLE_MIN 128
+#endif
 // 1: arena stage bodies use packed f32x2 products (mpm_math_x2.cuh).
 #ifndef MPM_PACKED_MATH
 #define MPM_PACKED_MATH 1
@@ -517,7 +523,8 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
         int4* __restrict__ grid = grid_all + (size_t)bb * 64;
         int tbx = 0, tby = 0, tbz = 0;
         if (task.brick >= 0) brick_coords(g, task.brick, tbx, tby, tbz);
-        const bool table = task.brick >= 0 && task.count <= kMaxSort;  // uniform
+        const bool table = task.brick >= 0 && task.count <= kMaxSort &&
+                           task.count >= MPM_LANE_TABLE_MIN;  // uniform
         if (table) build_lane_table(P, g, d, task, tbx, tby, tbz, s_lt);
         for (int j = threadIdx.x; j < task.count; j += kTask) {
             const int slot = table ? (int)s_lt.slot[j] : (int)d.order[task.first + j];
