@@ -87,22 +87,6 @@ struct Node {
     float dist[3];
 };
 
-__device__ __forceinline__ float node_weight(const Sten& s, int gx, int gy, int gz) {
-    return (s.w[0][gx] * s.w[1][gy]) * s.w[2][gz];
-}
-
-__device__ __forceinline__ void node_geom(const Sten& s, const float x[3], int gx, int gy, int gz,
-                                          Node& nd) {
-    const float wx = s.w[0][gx], wy = s.w[1][gy], wz = s.w[2][gz];
-    nd.w = (wx * wy) * wz;
-    nd.gw[0] = (s.dw[0][gx] * wy) * wz;
-    nd.gw[1] = (wx * s.dw[1][gy]) * wz;
-    nd.gw[2] = (wx * wy) * s.dw[2][gz];
-    nd.dist[0] = ((s.cf[0] + (float)gx - 1.0f) + 0.5f) - x[0];
-    nd.dist[1] = ((s.cf[1] + (float)gy - 1.0f) + 0.5f) - x[1];
-    nd.dist[2] = ((s.cf[2] + (float)gz - 1.0f) + 0.5f) - x[2];
-}
-
 // Flat index of the stencil cell in the scene's grid, -1 where the forward
 // dropped it (outside [0, grid_count)).
 __device__ __forceinline__ int node_index(const Sten& s, int gx, int gy, int gz, const SimConsts& k) {
