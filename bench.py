@@ -331,7 +331,7 @@ def measure_batched(pkg, torch, stream, repeats: int = 3) -> dict:
         "timing": f"CUDA events around each {K}-substep rollout, best of {repeats}, after a "
                   f"{K}-substep warm-up (batch and loop over the same substeps); "
                   "loop = MLSMPMSimulator.execute(substeps=100) per scene, back to back; "
-                  "from_initial_state: upload + the first 100 substeps, best of 2",
+                  "from_initial_state: the first 100 substeps after an upload, best of 2",
     }
 
 
