@@ -32,6 +32,13 @@ def test_null_handles_are_rejected(pkg):
     assert lib.mpm_set_real_box(None, None) == pkg._lib.MPM_E_INVALID
     assert lib.mpm_num_particles(None) == 0
     assert lib.mpm_destroy(None) == 0
+    E = pkg._lib.MPM_E_INVALID
+    assert lib.mpm_download_posvel_async(None, None, None) == E
+    assert lib.mpm_wait_posvel(None, None) == E
+    assert lib.mpm_batch_upload(None, None) == E
+    assert lib.mpm_backward(None, None, None, 0, None, None, None) == E
+    assert lib.mpm_backward_list(None, None, None, 0, None, None, None) == E
+    assert lib.mpm_sph_set_graph(None, 1) == E
 
 
 def test_default_params_are_the_reference_constants(pkg):
