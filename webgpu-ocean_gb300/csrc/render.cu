@@ -192,8 +192,36 @@ __global__ void k_resolve(const float4* __restrict__ posvel, Uni u, Consts c,
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-__global__ void k_bilateral(const float* __restrict__ src, float* __restrict__ dst, Consts c, int dx,
-                            int dy) {
+// Spatial weights of the two filters, which depend only on the filter
+// half-width and the tap offset: bilateral exp(-(x^2 + x^2) / (2 sigma^2)),
+// sigma = fs / 3, for fs in [0, kMaxFs] and |x| <= fs (row fs at fs * kWRow);
+// gaussian exp(-x^2 / (2 sigma^2)), sigma = 10, |x| <= 30.  Computed once
+// with the same operations the filter bodies use, so a table read is
+// bit-identical to evaluating the weight in place.
+constexpr int kMaxFs = 100;
+constexpr int kWRow = kMaxFs + 1;
+constexpr int kGaussFs = 30;
+
+__global__ void k_weight_tables(float* __restrict__ wtab, float* __restrict__ gtab) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < kWRow * kWRow) {
+        const int fs = e / kWRow, x = e % kWRow;
+        const float sigma = dvd((float)fs, 3.0f);
+        const float two_sigma = mul(mul(2.0f, sigma), sigma);
+        const float xf = (float)x;
+        const float rr = add(mul(xf, xf), mul(xf, xf));
+        wtab[e] = exp_r(dvd(-rr, two_sigma));
+    }
+    if (e <= kGaussFs) {
+        const float sigma = dvd((float)kGaussFs, 3.0f);
+        const float two_sigma = mul(mul(2.0f, sigma), sigma);
+        const float xf = (float)e;
+        gtab[e] = exp_r(dvd(mul(-xf, xf), two_sigma));
+    }
+}
+
+__global__ void k_bilateral(const float* __restrict__ src, float* __restrict__ dst, Consts c,
+                            const float* __restrict__ wtab, int dx, int dy) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= c.W * c.H) return;
     const int px = p % c.W, py = p / c.W;
@@ -203,17 +231,14 @@ __global__ void k_bilateral(const float* __restrict__ src, float* __restrict__ d
         return;
     }
     const int fs = min(__float2int_rz(c.max_filter_size), __float2int_rz(ceilf(dvd(c.ppc, depth))));
-    const float sigma = dvd((float)fs, 3.0f);
-    const float two_sigma = mul(mul(2.0f, sigma), sigma);
+    const float* wrow = wtab + fs * kWRow;  // fs <= max_filter_size = kMaxFs
     const float sd = dvd(c.depth_threshold, 3.0f);
     const float two_sd = mul(mul(2.0f, sd), sd);
     float sum = 0.0f, wsum = 0.0f;
     for (int x = -fs; x <= fs; ++x) {
-        const float xf = (float)x;
         const int ix = clampi(px + x * dx, 0, c.W - 1), iy = clampi(py + x * dy, 0, c.H - 1);
         const float sampled = fabsf(src[(size_t)iy * c.W + ix]);
-        const float rr = add(mul(xf, xf), mul(xf, xf));
-        const float w = exp_r(dvd(-rr, two_sigma));
+        const float w = __ldg(wrow + (x < 0 ? -x : x));
         const float rd = sub(sampled, depth);
         const float wd = exp_r(dvd(mul(-rd, rd), two_sd));
         sum = add(sum, mul(mul(sampled, w), wd));
@@ -222,8 +247,8 @@ __global__ void k_bilateral(const float* __restrict__ src, float* __restrict__ d
     dst[p] = dvd(sum, wsum);
 }
 
-__global__ void k_gaussian(const float* __restrict__ src, float* __restrict__ dst, Consts c, int dx,
-                           int dy) {
+__global__ void k_gaussian(const float* __restrict__ src, float* __restrict__ dst, Consts c,
+                           const float* __restrict__ gtab, int dx, int dy) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= c.W * c.H) return;
     const int px = p % c.W, py = p / c.W;
@@ -232,15 +257,12 @@ __global__ void k_gaussian(const float* __restrict__ src, float* __restrict__ ds
         dst[p] = 0.0f;
         return;
     }
-    constexpr int fs = 30;
-    const float sigma = dvd((float)fs, 3.0f);
-    const float two_sigma = mul(mul(2.0f, sigma), sigma);
+    constexpr int fs = kGaussFs;
     float sum = 0.0f, wsum = 0.0f;
     for (int x = -fs; x <= fs; ++x) {
-        const float xf = (float)x;
         const int ix = clampi(px + x * dx, 0, c.W - 1), iy = clampi(py + x * dy, 0, c.H - 1);
         const float sampled = src[(size_t)iy * c.W + ix];
-        const float w = exp_r(dvd(mul(-xf, xf), two_sigma));
+        const float w = __ldg(gtab + (x < 0 ? -x : x));
         sum = add(sum, mul(sampled, w));
         wsum = add(wsum, w);
     }
@@ -380,6 +402,8 @@ struct mpm_renderer {
     uchar4* color8 = nullptr;
     float4* env = nullptr;
     int env_size = 0;
+    float* wtab = nullptr;  // bilateral spatial weights, kWRow x kWRow
+    float* gtab = nullptr;  // gaussian weights, kGaussFs + 1
 };
 
 namespace {
@@ -394,6 +418,8 @@ void free_renderer(mpm_renderer* r) {
     cudaFree(r->color);
     cudaFree(r->color8);
     cudaFree(r->env);
+    cudaFree(r->wtab);
+    cudaFree(r->gtab);
     delete r;
 }
 
@@ -476,6 +502,13 @@ int mpm_renderer_create(int width, int height, float radius, float fov, mpm_rend
     }
     if (e == cudaSuccess) e = cudaMalloc(&r->color, sizeof(float4) * np);
     if (e == cudaSuccess) e = cudaMalloc(&r->color8, sizeof(uchar4) * np);
+    if (e == cudaSuccess) e = cudaMalloc(&r->wtab, sizeof(float) * kWRow * kWRow);
+    if (e == cudaSuccess) e = cudaMalloc(&r->gtab, sizeof(float) * (kGaussFs + 1));
+    if (e == cudaSuccess) {
+        k_weight_tables<<<(kWRow * kWRow + 255) / 256, 256>>>(r->wtab, r->gtab);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         const int rc = cuda_fail(e, "mpm_renderer_create");
         free_renderer(r);
@@ -518,11 +551,11 @@ int mpm_renderer_execute(mpm_renderer* r, const void* posvel, int n,
     if (n > 0) k_splat<<<(n + 127) / 128, 128, 0, st>>>(pv, n, u, c, r->dkey, r->tacc);
     k_resolve<<<pb, 256, 0, st>>>(pv, u, c, r->dkey, r->tacc, r->depth[0], r->thick[0]);
     for (int it = 0; it < 4; ++it) {  // fluidRender.ts:455-466
-        k_bilateral<<<pb, 256, 0, st>>>(r->depth[0], r->depth[1], c, 1, 0);
-        k_bilateral<<<pb, 256, 0, st>>>(r->depth[1], r->depth[0], c, 0, 1);
+        k_bilateral<<<pb, 256, 0, st>>>(r->depth[0], r->depth[1], c, r->wtab, 1, 0);
+        k_bilateral<<<pb, 256, 0, st>>>(r->depth[1], r->depth[0], c, r->wtab, 0, 1);
     }
-    k_gaussian<<<pb, 256, 0, st>>>(r->thick[0], r->thick[1], c, 1, 0);  // :474-486
-    k_gaussian<<<pb, 256, 0, st>>>(r->thick[1], r->thick[0], c, 0, 1);
+    k_gaussian<<<pb, 256, 0, st>>>(r->thick[0], r->thick[1], c, r->gtab, 1, 0);  // :474-486
+    k_gaussian<<<pb, 256, 0, st>>>(r->thick[1], r->thick[0], c, r->gtab, 0, 1);
     k_shade<<<pb, 256, 0, st>>>(r->depth[0], r->thick[0], r->env, r->env_size, u, c, r->color,
                                 r->color8);
     const cudaError_t e = cudaGetLastError();
