@@ -246,3 +246,33 @@ def test_repeated_backward_after_one_forward(cuda, pkg, tape):
                                    atol=1e-5 * float(np.abs(outs[0][0]).max()))
         np.testing.assert_allclose(p, outs[0][1], rtol=1e-4)
     assert np.isfinite(outs[0][0]).all()
+
+
+@pytest.mark.parametrize("tape", ["fixed", "fp64"])
+def test_large_batch_uses_the_sorted_path(cuda, pkg, tape):
+    """Above 512 particles per SM the adjoint kernels walk a per-substep
+    brick sort with one thread per particle; below it they use three threads
+    per particle in particle order.  Each scene of a large batch must get the
+    gradients its own (small) adjoint gives."""
+    import torch
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    descs, recs = pkg.batch_scenes(16, seed=11, n_range=(5000, 8000), sides=(32,))
+    offs = np.concatenate([[0], np.cumsum([d.num_particles for d in descs])])
+    assert offs[-1] >= 512 * nsm, "the batch must be large enough for the sorted path"
+    T, every = 12, 4
+    adj = pkg.MLSMPMAdjoint(descs, T, every, tape=tape)
+    adj.forward(recs, T)
+    L, seed = pkg.centroid_loss(adj.state(T), TARGET, adj.sceneOffsets)
+    g, pg = adj.backward({T: seed})
+    adj.close()
+    assert np.isfinite(g).all()
+    for s in (0, 7, 15):
+        d = descs[s]
+        one = pkg.MLSMPMAdjoint([d], T, every, tape=tape)
+        one.forward(recs[offs[s]:offs[s + 1]], T)
+        _, seed1 = pkg.centroid_loss(one.state(T), TARGET)
+        g1, pg1 = one.backward({T: seed1})
+        one.close()
+        np.testing.assert_allclose(g[offs[s]:offs[s + 1]], g1, rtol=1e-4,
+                                   atol=1e-5 * float(np.abs(g1).max()))
+        np.testing.assert_allclose(pg[s], pg1[0], rtol=1e-4, atol=1e-9)
