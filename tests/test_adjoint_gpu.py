@@ -276,3 +276,29 @@ def test_large_batch_uses_the_sorted_path(cuda, pkg, tape):
         np.testing.assert_allclose(g[offs[s]:offs[s + 1]], g1, rtol=1e-4,
                                    atol=1e-5 * float(np.abs(g1).max()))
         np.testing.assert_allclose(pg[s], pg1[0], rtol=1e-4, atol=1e-9)
+
+
+def test_contiguous_seed_block_abi(cuda, pkg):
+    """mpm_backward (all seed blocks in one array) gives what the pointer-list
+    entry point the Python class uses gives."""
+    import ctypes
+    from oracle import scene as scene_mod
+    recs = lattice_with_velocity(scene_mod, 10, 9.0)
+    adj = pkg.MLSMPMAdjoint([pkg.scene_desc(len(recs), [32.0, 32.0, 32.0])], 20, 10, tape="fixed")
+    adj.forward(recs, 20)
+    _, s10 = pkg.centroid_loss(adj.state(10), TARGET)
+    _, s20 = pkg.centroid_loss(adj.state(20), TARGET)
+    g_list, p_list = adj.backward({10: s10, 20: s20})
+    n = len(recs)
+    block = np.ascontiguousarray(np.stack([s10, s20]), dtype=np.float32)
+    steps = (ctypes.c_int32 * 2)(10, 20)
+    grad = np.zeros((n, 20), np.float32)
+    pgrad = np.zeros((1, 2), np.float64)
+    fp = ctypes.POINTER(ctypes.c_float)
+    rc = adj._lib.mpm_backward(adj._handle, block.ctypes.data_as(fp), steps, 2,
+                               grad.ctypes.data_as(fp),
+                               pgrad.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), None)
+    adj.close()
+    assert rc == 0
+    np.testing.assert_allclose(grad, g_list, rtol=1e-4, atol=1e-5 * float(np.abs(g_list).max()))
+    np.testing.assert_allclose(pgrad, p_list, rtol=1e-4)
