@@ -60,7 +60,13 @@ def fit_parameters(adj: MLSMPMAdjoint, init: np.ndarray, observed: dict, substep
     m = np.zeros_like(theta)
     v = np.zeros_like(theta)
     steps = sorted(observed)
-    per_particle = np.repeat(counts, np.diff(offs))[:, None]  # its scene's particle count
+    n = int(offs[-1])
+    # dL/dx = 2 (x - x_obs) / (its scene's particle count); seed records are
+    # zero except their position columns, so the buffers are made once
+    scale = (2.0 / np.repeat(counts, np.diff(offs))).astype(np.float32)[:, None]
+    obs32 = {t: np.asarray(observed[t], dtype=np.float32) for t in steps}
+    seeds = {t: np.zeros((n, 20), dtype=np.float32) for t in steps}
+    x = np.empty((n, 20), dtype=np.float32)
     history = []
     t0 = time.perf_counter()
     for it in range(iters):
@@ -68,14 +74,13 @@ def fit_parameters(adj: MLSMPMAdjoint, init: np.ndarray, observed: dict, substep
         for s in range(S):
             adj.setScene(s, with_constants(base[s], params[s, 0], params[s, 1]))
         adj.forward(init, substeps)
-        seeds, loss = {}, np.zeros(S)
+        loss = np.zeros(S)
         for t in steps:
-            x = adj.state(t)
-            diff = x[:, 0:3].astype(np.float64) - observed[t]
-            loss += np.add.reduceat(np.einsum("ij,ij->i", diff, diff), offs[:-1]) / counts
-            seed = np.zeros_like(x)
-            seed[:, 0:3] = (2.0 * diff / per_particle).astype(np.float32)
-            seeds[t] = seed
+            adj.state(t, out=x)
+            diff = x[:, 0:3] - obs32[t]
+            sq = np.einsum("ij,ij->i", diff, diff, dtype=np.float64)
+            loss += np.add.reduceat(sq, offs[:-1]) / counts
+            np.multiply(diff, scale, out=seeds[t][:, 0:3])
         _, pgrad = adj.backward(seeds)
         g = pgrad * params  # d/d log(p) = p * d/dp
         m = betas[0] * m + (1 - betas[0]) * g

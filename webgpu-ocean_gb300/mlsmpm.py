@@ -588,8 +588,14 @@ class MLSMPMAdjoint:
                "forward")
         self.substeps = int(substeps)
 
-    def state(self, substep: int) -> np.ndarray:
-        out = np.zeros((self.numParticles, 20), dtype=np.float32)
+    def state(self, substep: int, out: np.ndarray | None = None) -> np.ndarray:
+        """The state after `substep` substeps of the last forward (a
+        checkpoint), as (N, 20) records; written into `out` when given."""
+        if out is None:
+            out = np.empty((self.numParticles, 20), dtype=np.float32)
+        elif (out.dtype != np.float32 or out.shape != (self.numParticles, 20)
+              or not out.flags.c_contiguous):
+            raise ValueError("out must be a C-contiguous float32 (N, 20) array")
         _check(self._lib.mpm_adjoint_state(self._handle, int(substep),
                                            out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
                "state")
