@@ -64,3 +64,21 @@ def test_loss_seeds_and_adam_step(pkg):
     theta1 = np.log(start) - 0.1 * g / (np.abs(g) + 1e-12)
     np.testing.assert_allclose(fit["history"][1]["params"], np.exp(theta1), rtol=1e-9)
     assert len(adj.set_calls) == 2 * 3
+
+
+def test_centroid_loss_seed_is_its_gradient(pkg):
+    rng = np.random.default_rng(2)
+    state = rng.normal(10.0, 3.0, (12, 20)).astype(np.float32)
+    offs = [0, 5, 12]
+    target = [30.0, 10.0, 30.0]
+    loss, seed = pkg.centroid_loss(state, target, offs)
+    assert not seed[:, 3:].any()
+    eps = 1e-3
+    for i, a in ((0, 0), (4, 2), (7, 1), (11, 0)):
+        up, dn = state.astype(np.float64).copy(), state.astype(np.float64).copy()
+        up[i, a] += eps
+        dn[i, a] -= eps
+        lu, _ = pkg.centroid_loss(up, target, offs)
+        ld, _ = pkg.centroid_loss(dn, target, offs)
+        fd = (lu - ld).sum() / (2 * eps)
+        assert abs(fd - seed[i, a]) < 1e-3 * max(1.0, abs(fd))
