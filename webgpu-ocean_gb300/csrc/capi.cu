@@ -1394,11 +1394,19 @@ int enqueue_backward(mpm_adjoint* a, const int* seed_steps, int nseeds, cudaStre
                 return cuda_fail(e, "mpm_backward recompute");
             for (int t = t0; t < t1; ++t) {
                 if (sorted_step(b->sorted, &b->ps, b->posvel, b->counters, b->consts[0], 1, st,
-                                &b->prof, b->graph) != 0 ||
-                    sorted_export_all(b->sorted, a->gtape + (size_t)(t - t0) * nc, st, &b->prof) != 0)
+                                &b->prof, b->graph) != 0)
                     return fail(MPM_E_CUDA, std::string("backward recompute: ") + sorted_error());
                 b->stepped = true;
-                if (t + 1 < t1) batch_canonical_to(b, a->seg[(size_t)(t + 1 - t0)], st);
+                // the updated grid, and the state after the substep when the
+                // segment goes on, in one launch
+                int4* gt = a->gtape + (size_t)(t - t0) * nc;
+                const int rc = t + 1 < t1
+                                   ? sorted_export_all_canonical(b->sorted, gt, b->ps,
+                                                                 a->seg[(size_t)(t + 1 - t0)], n, st,
+                                                                 &b->prof)
+                                   : sorted_export_all(b->sorted, gt, st, &b->prof);
+                if (rc != 0)
+                    return fail(MPM_E_CUDA, std::string("backward recompute: ") + sorted_error());
             }
         }
         // adjoint substeps in reverse
@@ -1577,14 +1585,15 @@ int mpm_forward_ckpt(mpm_adjoint* a, const float* init, int substeps, void* stre
         while (t < substeps) {
             if (tape_last && t >= last_t0) {  // one substep at a time, recording
                 if (sorted_step(b->sorted, &b->ps, b->posvel, b->counters, b->consts[0], 1, st,
-                                &b->prof, b->graph) != 0 ||
-                    sorted_export_all(b->sorted, a->gtape + (size_t)(t - last_t0) * nc, st,
-                                      &b->prof) != 0)
+                                &b->prof, b->graph) != 0)
                     return fail(MPM_E_CUDA, std::string("forward: ") + sorted_error());
                 b->stepped = true;
+                int4* gt = a->gtape + (size_t)(t - last_t0) * nc;
                 ++t;
-                if (t < substeps) batch_canonical_to(b, a->seg[(size_t)(t - last_t0)], st);
-                else batch_canonical_to(b, a->ckpt[(size_t)ckpt_slot(a, t, substeps)], st);
+                const Particles& dst = t < substeps ? a->seg[(size_t)(t - last_t0)]
+                                                    : a->ckpt[(size_t)ckpt_slot(a, t, substeps)];
+                if (sorted_export_all_canonical(b->sorted, gt, b->ps, dst, n, st, &b->prof) != 0)
+                    return fail(MPM_E_CUDA, std::string("forward: ") + sorted_error());
                 continue;
             }
             const int ns = substeps - t < a->every ? substeps - t : a->every;
@@ -1592,12 +1601,15 @@ int mpm_forward_ckpt(mpm_adjoint* a, const float* init, int substeps, void* stre
                             &b->prof, b->graph) != 0)
                 return fail(MPM_E_CUDA, std::string("forward: ") + sorted_error());
             b->stepped = true;
-            if (full_tape(a) &&
-                sorted_export_all(b->sorted, a->gtape + (size_t)t * (size_t)a->ncells, st,
-                                  &b->prof) != 0)
-                return fail(MPM_E_CUDA, std::string("forward: ") + sorted_error());
+            const Particles& dst = a->ckpt[(size_t)ckpt_slot(a, t + ns, substeps)];
+            if (full_tape(a)) {
+                if (sorted_export_all_canonical(b->sorted, a->gtape + (size_t)t * (size_t)a->ncells,
+                                                b->ps, dst, n, st, &b->prof) != 0)
+                    return fail(MPM_E_CUDA, std::string("forward: ") + sorted_error());
+            } else {
+                batch_canonical_to(b, dst, st);
+            }
             t += ns;
-            batch_canonical_to(b, a->ckpt[(size_t)ckpt_slot(a, t, substeps)], st);
         }
     }
     MPM_CUDA(cudaGetLastError());

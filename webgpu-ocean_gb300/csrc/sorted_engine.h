@@ -62,6 +62,12 @@ int sorted_export_scene_grid(SortedEngine* e, int scene, int4* out, cudaStream_t
 // the scenes' reference-layout grids (scene order).
 int sorted_export_all(SortedEngine* e, int4* out, cudaStream_t st, LaunchProfiler* prof);
 
+// sorted_export_all plus the particles of `ps` (n of them) in index order
+// into dst, in one launch.
+int sorted_export_all_canonical(SortedEngine* e, int4* out, const ParticleStore& ps,
+                                const Particles& dst, int n, cudaStream_t st,
+                                LaunchProfiler* prof);
+
 const char* sorted_error();
 
 }  // namespace mpm
