@@ -24,10 +24,10 @@ LIB = os.path.join(BUILD, "libmpm.so")
 REPO = os.path.dirname(HERE)
 INCLUDE = os.path.join(REPO, "include")
 
-SOURCES = ["capi.cu", "kernels_dispatch.cu", "kernels_sorted.cu", "profiler.cu", "noalloc.cu",
-           "adjoint.cu", "render.cu", "sph.cu"]
+SOURCES = ["capi.cu", "capi_batch.cu", "capi_adjoint.cu", "kernels_dispatch.cu",
+           "kernels_sorted.cu", "profiler.cu", "noalloc.cu", "adjoint.cu", "render.cu", "sph.cu"]
 HEADERS = ["mpm_math.cuh", "mpm_math_x2.cuh", "mpm_internal.h", "sorted_engine.h", "adjoint.h",
-           "render_math.cuh"]
+           "render_math.cuh", "capi_internal.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xptxas=--fmad=false",
