@@ -280,9 +280,12 @@ int64_t mpm_batch_launch_count(const mpm_batch* batch);
  * evaluated along the solver's own trajectory.  mpm_forward_ckpt runs the
  * solver and keeps the state every `checkpoint_every` substeps; mpm_backward
  * recomputes each segment from its checkpoint (states and updated grids of
- * every substep) and runs the adjoint substeps in reverse.  checkpoint_every
- * = 1 keeps every substep's state and updated grid (max_substeps grids of
- * device memory) and the backward recomputes nothing. */
+ * every substep) and runs the adjoint substeps in reverse; when max_substeps
+ * > checkpoint_every it keeps two segment tapes (2 x checkpoint_every states
+ * and grids) and recomputes segment j - 1 on a second stream while it
+ * differentiates segment j.  checkpoint_every = 1 keeps every substep's state
+ * and updated grid (max_substeps grids of device memory) and the backward
+ * recomputes nothing. */
 typedef struct mpm_adjoint mpm_adjoint;
 
 /* Tapes (the trajectory the derivative is evaluated along):

@@ -22,14 +22,19 @@ struct mpm_adjoint {
     int nck = 0;                     // checkpoint slots
     // fixed-point tape
     std::vector<Particles> ckpt;     // states after 0, every, 2*every, ..., T substeps
-    std::vector<Particles> seg;      // states inside a segment (seg[0] unused)
-    int4* gtape = nullptr;           // every x ncells: updated grids of a segment
-                                     // (max_substeps x ncells for a full tape)
+    std::vector<Particles> seg[2];   // states inside a segment (seg[.][0] unused)
+    int4* gtape[2] = {nullptr, nullptr};  // every x ncells: updated grids of a segment
+                                          // (max_substeps x ncells for a full tape)
+    // Segment tape sets: two when a backward can have more than one segment,
+    // so that the recompute of segment j - 1 fills one while the adjoint of
+    // segment j reads the other.  Segment j of a T-substep run uses set
+    // tape_set(a, j); the forward records its last segment in set 0.
+    int sets = 1;
     // FP64 tape
     std::vector<double*> ckpt64;
-    std::vector<double*> seg64;
+    std::vector<double*> seg64[2];
     double* scratch64[2] = {nullptr, nullptr};
-    double4* gtape64 = nullptr;
+    double4* gtape64[2] = {nullptr, nullptr};
     // adjoint state
     Particles adj[2]{};
     float4* gadj = nullptr;
@@ -129,52 +134,64 @@ void batch_canonical_to(mpm_batch* b, const Particles& dst, cudaStream_t st) {
 
 void free_tapes(mpm_adjoint* a) {
     for (Particles& P : a->ckpt) free_particles(P);
-    for (Particles& P : a->seg) free_particles(P);
     a->ckpt.clear();
-    a->seg.clear();
-    cudaFree(a->gtape);
-    a->gtape = nullptr;
     for (double* p : a->ckpt64) cudaFree(p);
-    for (double* p : a->seg64) cudaFree(p);
     a->ckpt64.clear();
-    a->seg64.clear();
-    for (double*& p : a->scratch64) {
-        cudaFree(p);
-        p = nullptr;
+    for (int k = 0; k < 2; ++k) {
+        for (Particles& P : a->seg[k]) free_particles(P);
+        a->seg[k].clear();
+        cudaFree(a->gtape[k]);
+        a->gtape[k] = nullptr;
+        for (double* p : a->seg64[k]) cudaFree(p);
+        a->seg64[k].clear();
+        cudaFree(a->gtape64[k]);
+        a->gtape64[k] = nullptr;
+        cudaFree(a->scratch64[k]);
+        a->scratch64[k] = nullptr;
     }
-    cudaFree(a->gtape64);
-    a->gtape64 = nullptr;
 }
 
 // checkpoint_every == 1 keeps every substep's state and updated grid (a full
 // tape): the backward then recomputes nothing.
 bool full_tape(const mpm_adjoint* a) { return a->every == 1; }
 int tape_grids(const mpm_adjoint* a) { return full_tape(a) ? a->max_substeps : a->every; }
+// The segment tape set of segment j of a forward of T substeps: the last
+// segment uses set 0 (the forward's record), the ones before it alternate.
+int tape_set(const mpm_adjoint* a, int j) {
+    const int nseg = (a->T + a->every - 1) / a->every;
+    return (nseg - 1 - j) & (a->sets - 1);
+}
 
 // Allocates the buffers of the selected tape (and frees the other's).
 cudaError_t alloc_tape(mpm_adjoint* a) {
     free_tapes(a);
     const size_t np = (size_t)(a->b->n > 0 ? a->b->n : 1);
     const size_t nc = (size_t)a->ncells;
+    a->sets = !full_tape(a) && a->max_substeps > a->every ? 2 : 1;
     cudaError_t e = cudaSuccess;
     if (a->tape == MPM_TAPE_FIXED_POINT) {
         a->ckpt.resize((size_t)a->nck);
         for (int i = 0; i < a->nck && e == cudaSuccess; ++i) e = alloc_particles(a->ckpt[(size_t)i], np);
-        a->seg.resize((size_t)a->every);
-        for (int i = 1; i < a->every && e == cudaSuccess; ++i)
-            e = alloc_particles(a->seg[(size_t)i], np);
-        if (e == cudaSuccess) e = cudaMalloc(&a->gtape, sizeof(int4) * (size_t)tape_grids(a) * nc);
+        for (int k = 0; k < a->sets && e == cudaSuccess; ++k) {
+            a->seg[k].resize((size_t)a->every);
+            for (int i = 1; i < a->every && e == cudaSuccess; ++i)
+                e = alloc_particles(a->seg[k][(size_t)i], np);
+            if (e == cudaSuccess)
+                e = cudaMalloc(&a->gtape[k], sizeof(int4) * (size_t)tape_grids(a) * nc);
+        }
     } else {
         a->ckpt64.assign((size_t)a->nck, nullptr);
         for (int i = 0; i < a->nck && e == cudaSuccess; ++i)
             e = cudaMalloc(&a->ckpt64[(size_t)i], sizeof(double) * kRec64 * np);
-        a->seg64.assign((size_t)a->every, nullptr);
-        for (int i = 1; i < a->every && e == cudaSuccess; ++i)
-            e = cudaMalloc(&a->seg64[(size_t)i], sizeof(double) * kRec64 * np);
+        for (int k = 0; k < a->sets && e == cudaSuccess; ++k) {
+            a->seg64[k].assign((size_t)a->every, nullptr);
+            for (int i = 1; i < a->every && e == cudaSuccess; ++i)
+                e = cudaMalloc(&a->seg64[k][(size_t)i], sizeof(double) * kRec64 * np);
+            if (e == cudaSuccess)
+                e = cudaMalloc(&a->gtape64[k], sizeof(double4) * (size_t)tape_grids(a) * nc);
+        }
         for (int i = 0; i < 2 && e == cudaSuccess; ++i)
             e = cudaMalloc(&a->scratch64[i], sizeof(double) * kRec64 * np);
-        if (e == cudaSuccess)
-            e = cudaMalloc(&a->gtape64, sizeof(double4) * (size_t)tape_grids(a) * nc);
     }
     return e;
 }
@@ -232,16 +249,25 @@ int adj_lanes(long long n) {
 }
 
 // The whole backward of the last forward, enqueued on `st` (kernels,
-// memsets and device copies only, so it can be captured): for each
-// checkpoint segment from the last, recompute its states and updated grids
-// (unless the full tape kept them), then run its adjoint substeps in reverse,
-// adding the seeds at their substeps.  *cur_out: the adjoint buffer that
-// ends up holding dL/dS_0.
+// memsets, device copies and event dependencies only, so it can be
+// captured): for each checkpoint segment from the last, recompute its states
+// and updated grids (unless the forward or a full tape kept them), then run
+// its adjoint substeps in reverse, adding the seeds at their substeps.
+// With two tape sets and a second stream `rs` (ev: 5 events), the recompute
+// runs on `rs` one segment ahead: segment j - 1 is recomputed into one set
+// while the adjoint of segment j reads the other; the recompute of j - 1
+// waits for the adjoint of j + 1 (the last reader of its set), the adjoint of
+// j for the recompute of j.  rs == st (or one set) runs them in turn.
+// *cur_out: the adjoint buffer that ends up holding dL/dS_0.
 int enqueue_backward(mpm_adjoint* a, const int* seed_steps, int nseeds, cudaStream_t st,
-                     int* cur_out) {
+                     cudaStream_t rs, cudaEvent_t* ev, int* cur_out) {
     mpm_batch* b = a->b;
     const int n = b->n, S = (int)b->consts.size();
     const bool f64 = a->tape == MPM_TAPE_FP64;
+    const bool overlap = rs != nullptr && rs != st && a->sets == 2;
+    cudaStream_t r = overlap ? rs : st;
+    cudaEvent_t* ev_rec = overlap ? ev : nullptr;      // [set]: recompute into it done
+    cudaEvent_t* ev_adj = overlap ? ev + 2 : nullptr;  // [set]: adjoint of its segment done
     auto add_seeds = [&](int step, const Particles& A) {
         for (int i = 0; i < nseeds; ++i)
             if (seed_steps[i] == step) launch_particles_axpy(A, a->seedbuf[(size_t)i], n, st);
@@ -253,57 +279,96 @@ int enqueue_backward(mpm_adjoint* a, const int* seed_steps, int nseeds, cudaStre
     add_seeds(a->T, a->adj[cur]);
     const int nseg = (a->T + a->every - 1) / a->every;
     const size_t nc = (size_t)a->ncells;
-    for (int j = nseg - 1; j >= 0; --j) {
-        const int t0 = j * a->every;
-        const int t1 = t0 + a->every < a->T ? t0 + a->every : a->T;
-        // recompute the segment: states and updated grids of every substep
-        // (a full tape kept them all)
-        const size_t g0 = full_tape(a) ? (size_t)t0 : 0;  // tape grid of substep t0
-        if (full_tape(a) || (a->last_taped && j == nseg - 1)) {
-        } else if (f64) {
+    auto seg_range = [&](int j, int& t0, int& t1) {
+        t0 = j * a->every;
+        t1 = t0 + a->every < a->T ? t0 + a->every : a->T;
+    };
+    auto recomputed = [&](int j) { return !full_tape(a) && !(a->last_taped && j == nseg - 1); };
+    // recompute segment j on stream r into its tape set: states and updated
+    // grids of every substep
+    auto recompute = [&](int j) -> int {
+        if (!recomputed(j)) return MPM_OK;
+        const int k = tape_set(a, j);
+        if (overlap && j + 2 <= nseg - 1) MPM_CUDA(cudaStreamWaitEvent(r, ev_adj[k], 0));
+        int t0 = 0, t1 = 0;
+        seg_range(j, t0, t1);
+        if (f64) {
             const double* curS = a->ckpt64[(size_t)j];
             for (int t = t0; t < t1; ++t) {
-                double* dst = t + 1 < t1 ? a->seg64[(size_t)(t + 1 - t0)] : a->scratch64[0];
-                launch_substep64(curS, a->gtape64 + (size_t)(t - t0) * nc, dst, a->scenes_d, S,
-                                 a->pscene_d, n, a->ncells, st);
+                double* dst = t + 1 < t1 ? a->seg64[k][(size_t)(t + 1 - t0)] : a->scratch64[0];
+                launch_substep64(curS, a->gtape64[k] + (size_t)(t - t0) * nc, dst, a->scenes_d, S,
+                                 a->pscene_d, n, a->ncells, r);
                 curS = dst;
             }
         } else {
-            if (cudaError_t e = batch_load_device(b, a->ckpt[(size_t)j], st); e != cudaSuccess)
+            if (cudaError_t e = batch_load_device(b, a->ckpt[(size_t)j], r); e != cudaSuccess)
                 return cuda_fail(e, "mpm_backward recompute");
             for (int t = t0; t < t1; ++t) {
-                if (sorted_step(b->sorted, &b->ps, b->posvel, b->counters, b->consts[0], 1, st,
+                if (sorted_step(b->sorted, &b->ps, b->posvel, b->counters, b->consts[0], 1, r,
                                 &b->prof, b->graph) != 0)
                     return fail(MPM_E_CUDA, std::string("backward recompute: ") + sorted_error());
                 b->stepped = true;
                 // the updated grid, and the state after the substep when the
                 // segment goes on, in one launch
-                int4* gt = a->gtape + (size_t)(t - t0) * nc;
+                int4* gt = a->gtape[k] + (size_t)(t - t0) * nc;
                 const int rc = t + 1 < t1
                                    ? sorted_export_all_canonical(b->sorted, gt, b->ps,
-                                                                 a->seg[(size_t)(t + 1 - t0)], n, st,
-                                                                 &b->prof)
-                                   : sorted_export_all(b->sorted, gt, st, &b->prof);
+                                                                 a->seg[k][(size_t)(t + 1 - t0)],
+                                                                 n, r, &b->prof)
+                                   : sorted_export_all(b->sorted, gt, r, &b->prof);
                 if (rc != 0)
                     return fail(MPM_E_CUDA, std::string("backward recompute: ") + sorted_error());
             }
         }
-        // adjoint substeps in reverse
+        if (overlap) MPM_CUDA(cudaEventRecord(ev_rec[k], r));
+        return MPM_OK;
+    };
+    // the adjoint substeps of segment j in reverse, on st
+    auto adjoint = [&](int j) -> int {
+        const int k = tape_set(a, j);
+        if (overlap && recomputed(j)) MPM_CUDA(cudaStreamWaitEvent(st, ev_rec[k], 0));
+        int t0 = 0, t1 = 0;
+        seg_range(j, t0, t1);
+        const size_t g0 = full_tape(a) ? (size_t)t0 : 0;  // tape grid of substep t0
         for (int t = t1 - 1; t >= t0; --t) {
             if (f64) {
-                const double* Sx = t == t0 ? a->ckpt64[(size_t)j] : a->seg64[(size_t)(t - t0)];
-                launch_adjoint_substep64(Sx, a->gtape64 + (g0 + (size_t)(t - t0)) * nc, a->adj[cur],
-                                         a->adj[cur ^ 1], a->gadj, a->scenes_d, S, a->pscene_d, n,
-                                         a->ncells, a->pgrad_d, a->sort, st);
+                const double* Sx = t == t0 ? a->ckpt64[(size_t)j] : a->seg64[k][(size_t)(t - t0)];
+                launch_adjoint_substep64(Sx, a->gtape64[k] + (g0 + (size_t)(t - t0)) * nc,
+                                         a->adj[cur], a->adj[cur ^ 1], a->gadj, a->scenes_d, S,
+                                         a->pscene_d, n, a->ncells, a->pgrad_d, a->sort, st);
             } else {
-                const Particles& Sx = t == t0 ? a->ckpt[(size_t)j] : a->seg[(size_t)(t - t0)];
-                launch_adjoint_substep(Sx, a->gtape + (g0 + (size_t)(t - t0)) * nc, a->adj[cur],
+                const Particles& Sx = t == t0 ? a->ckpt[(size_t)j] : a->seg[k][(size_t)(t - t0)];
+                launch_adjoint_substep(Sx, a->gtape[k] + (g0 + (size_t)(t - t0)) * nc, a->adj[cur],
                                        a->adj[cur ^ 1], a->gadj, a->scenes_d, S, a->pscene_d, n,
                                        a->ncells, a->pgrad_d, a->sort, st);
             }
             cur ^= 1;
             add_seeds(t, a->adj[cur]);
         }
+        if (overlap) MPM_CUDA(cudaEventRecord(ev_adj[k], st));
+        return MPM_OK;
+    };
+    int rc = MPM_OK;
+    if (overlap) {  // fork the recompute stream off st
+        MPM_CUDA(cudaEventRecord(ev[4], st));
+        MPM_CUDA(cudaStreamWaitEvent(r, ev[4], 0));
+        if (nseg > 0) rc = recompute(nseg - 1);
+        for (int j = nseg - 1; j >= 0 && rc == MPM_OK; --j) {
+            if (j > 0) rc = recompute(j - 1);
+            if (rc == MPM_OK) rc = adjoint(j);
+        }
+        // join it back, also after a failure (a capture must end joined)
+        const cudaError_t e1 = cudaEventRecord(ev[4], r);
+        const cudaError_t e2 = cudaStreamWaitEvent(st, ev[4], 0);
+        if (rc != MPM_OK) return rc;
+        MPM_CUDA(e1);
+        MPM_CUDA(e2);
+    } else {
+        for (int j = nseg - 1; j >= 0 && rc == MPM_OK; --j) {
+            rc = recompute(j);
+            if (rc == MPM_OK) rc = adjoint(j);
+        }
+        if (rc != MPM_OK) return rc;
     }
     MPM_CUDA(cudaGetLastError());
     *cur_out = cur;
@@ -449,10 +514,10 @@ int mpm_forward_ckpt(mpm_adjoint* a, const float* init, int substeps, void* stre
         for (int t = 0; t < substeps; ++t) {
             const int slot = ckpt_slot(a, t + 1, substeps);
             double* dst = slot >= 0 ? a->ckpt64[(size_t)slot] : a->scratch64[t & 1];
-            double4* G = a->gtape64 + (full_tape(a) ? (size_t)t * nc : 0);
+            double4* G = a->gtape64[0] + (full_tape(a) ? (size_t)t * nc : 0);
             if (tape_last && t >= last_t0) {
-                G = a->gtape64 + (size_t)(t - last_t0) * nc;
-                if (t + 1 < substeps) dst = a->seg64[(size_t)(t + 1 - last_t0)];
+                G = a->gtape64[0] + (size_t)(t - last_t0) * nc;
+                if (t + 1 < substeps) dst = a->seg64[0][(size_t)(t + 1 - last_t0)];
             }
             launch_substep64(cur, G, dst, a->scenes_d, S, a->pscene_d, n, a->ncells, st);
             cur = dst;
@@ -467,9 +532,9 @@ int mpm_forward_ckpt(mpm_adjoint* a, const float* init, int substeps, void* stre
                                 &b->prof, b->graph) != 0)
                     return fail(MPM_E_CUDA, std::string("forward: ") + sorted_error());
                 b->stepped = true;
-                int4* gt = a->gtape + (size_t)(t - last_t0) * nc;
+                int4* gt = a->gtape[0] + (size_t)(t - last_t0) * nc;
                 ++t;
-                const Particles& dst = t < substeps ? a->seg[(size_t)(t - last_t0)]
+                const Particles& dst = t < substeps ? a->seg[0][(size_t)(t - last_t0)]
                                                     : a->ckpt[(size_t)ckpt_slot(a, t, substeps)];
                 if (sorted_export_all_canonical(b->sorted, gt, b->ps, dst, n, st, &b->prof) != 0)
                     return fail(MPM_E_CUDA, std::string("forward: ") + sorted_error());
@@ -482,7 +547,7 @@ int mpm_forward_ckpt(mpm_adjoint* a, const float* init, int substeps, void* stre
             b->stepped = true;
             const Particles& dst = a->ckpt[(size_t)ckpt_slot(a, t + ns, substeps)];
             if (full_tape(a)) {
-                if (sorted_export_all_canonical(b->sorted, a->gtape + (size_t)t * (size_t)a->ncells,
+                if (sorted_export_all_canonical(b->sorted, a->gtape[0] + (size_t)t * (size_t)a->ncells,
                                                 b->ps, dst, n, st, &b->prof) != 0)
                     return fail(MPM_E_CUDA, std::string("forward: ") + sorted_error());
             } else {
@@ -552,30 +617,38 @@ int mpm_backward_list(mpm_adjoint* a, const float* const* seeds, const int* seed
         MPM_CUDA(upload_records(a->seedbuf[(size_t)i], seeds[i], n, a->stage, st));
     const std::vector<int> steps(seed_steps, seed_steps + nseeds);
     int cur = 0;
-    if (b->prof.enabled) {  // per-launch profiling: no graph
-        if (int rc = enqueue_backward(a, seed_steps, nseeds, st, &cur)) return rc;
+    if (b->prof.enabled) {  // per-launch profiling: no graph, one stream
+        if (int rc = enqueue_backward(a, seed_steps, nseeds, st, st, nullptr, &cur)) return rc;
     } else if (a->bgraph && a->bg_T == a->T && a->bg_every == a->every && a->bg_tape == a->tape &&
                a->bg_last_taped == a->last_taped && a->bg_steps == steps) {
         MPM_CUDA(cudaGraphLaunch(a->bgraph, st));
         cur = a->bg_cur;
     } else {
         drop_backward_graph(a);
-        cudaStream_t cs = nullptr;
-        MPM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        // capture stream, recompute stream and the events that order them
+        cudaStream_t cs = nullptr, rs = nullptr;
+        cudaEvent_t ev[5] = {};
+        cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&rs, cudaStreamNonBlocking);
+        for (int i = 0; i < 5 && e == cudaSuccess; ++i)
+            e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
         const bool engine_graph = b->graph;
         b->graph = false;  // the engine's kernels go straight into this graph
         cudaGraph_t graph = nullptr;
         int rc = 0;
-        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            rc = enqueue_backward(a, seed_steps, nseeds, cs, &cur);
+            rc = enqueue_backward(a, seed_steps, nseeds, cs, rs, ev, &cur);
             e = cudaStreamEndCapture(cs, &graph);
         }
         b->graph = engine_graph;
         cudaGraphExec_t exec = nullptr;
         if (e == cudaSuccess && rc == 0) e = cudaGraphInstantiate(&exec, graph, 0);
         if (graph) cudaGraphDestroy(graph);
-        cudaStreamDestroy(cs);
+        for (cudaEvent_t x : ev)
+            if (x) cudaEventDestroy(x);
+        if (rs) cudaStreamDestroy(rs);
+        if (cs) cudaStreamDestroy(cs);
         if (rc) return rc;
         if (e != cudaSuccess) return cuda_fail(e, "mpm_backward capture");
         a->bgraph = exec;
