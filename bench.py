@@ -47,6 +47,7 @@ sys.path.insert(0, REPO)
 METRIC = "MLS-MPM particle-substeps/s at 1M (bit-exact grid)"
 UNIT = "particle-substeps/s"
 SUBSTEPS = 2                  # per execute(), mls-mpm/mls-mpm.ts:247
+AUTOTUNE_SUBSTEPS = 8         # timed per (task size, lane-table threshold) candidate
 N_PER_AXIS = 100              # 100^3 = 1,000,000 particles
 ORIGIN, SPACING, JITTER, SEED = 4.0, 0.5, 0.05, 20240601
 BOX = [128.0, 128.0, 128.0]
@@ -236,6 +237,7 @@ def measure_batched(pkg, torch, stream, repeats: int = 3) -> dict:
     descs, recs = pkg.batch_scenes(BATCH_SCENES, seed=BATCH_SEED)
     S, K = len(descs), BATCH_SUBSTEPS
     batch = pkg.MLSMPMBatch(descs, recs, graph=True)
+    tuned = {"task_size": batch.autotune(4), "lane_table_min": batch.laneTableMin}
     batch.step(K, stream)  # captures the graph and warms up
     stream.synchronize()
     l0 = batch.launchCount()
@@ -328,13 +330,15 @@ def measure_batched(pkg, torch, stream, repeats: int = 3) -> dict:
         "speedup_vs_loop_plain": plain_ms / batch_ms,
         "speedup_vs_loop_graph": graph_ms / batch_ms,
         "bit_exact_vs_single_scene": bool(exact),
+        "batch_autotune": tuned,
         "from_initial_state": {"ms_per_rollout": first_ms,
                                "scene_substeps_per_s": S * K / (first_ms / 1e3),
                                "particle_substeps_per_s": total * K / (first_ms / 1e3)},
         "timing": f"CUDA events around each {K}-substep rollout, best of {repeats}, after a "
                   f"{K}-substep warm-up (batch and loop over the same substeps); "
-                  "loop = MLSMPMSimulator.execute(substeps=100) per scene, back to back; "
-                  "from_initial_state: the first 100 substeps after an upload, best of 2",
+                  "loop = MLSMPMSimulator.execute(substeps=100) per scene, back to back "
+                  "(default task size and lane table; the batch's are autotuned on its initial "
+                  "state); from_initial_state: the first 100 substeps after an upload, best of 2",
     }
 
 
@@ -625,6 +629,15 @@ def run_ours(args) -> None:
     for _ in range(args.warmup):
         sim.execute(stream)
     stream.synchronize()
+    # task size and lane-table threshold tuned on the state the timed steps
+    # start from (the autotuner restores it), then the same start again so
+    # the graphs of the chosen configuration are captured before timing
+    tuned = {"task_size": sim.autotune(AUTOTUNE_SUBSTEPS), "lane_table_min": sim.laneTableMin,
+             "autotune": f"{AUTOTUNE_SUBSTEPS} substeps after the warm-up steps"}
+    sim.upload(parts, BOX)
+    for _ in range(args.warmup):
+        sim.execute(stream)
+    stream.synchronize()
 
     # --- timed region: device-resident throughput ----------------------
     K = args.steps
@@ -823,7 +836,7 @@ def run_ours(args) -> None:
         "scaling": "weak", "vs_baseline": None, "dtype": DTYPE,
         "data": "synthetic (seeded jittered lattice)",
         "config": {"workload": WORKLOAD, "particles": n, "grid": "128x128x128",
-                   "substeps_per_step": SUBSTEPS, "engine": "sorted",
+                   "substeps_per_step": SUBSTEPS, "engine": "sorted", **tuned,
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "flushed between timed steps (256 MiB write, outside the events)",
                    "timing": "CUDA events per step on the launch stream, summed"},

@@ -219,10 +219,21 @@ int mpm_set_graph(mpm_sim* sim, int enable);
  * otherwise 64 ... 2^30.  Results do not depend on it. */
 int mpm_set_task_size(mpm_sim* sim, int task_size);
 int mpm_get_task_size(const mpm_sim* sim);
+/* Sorted engine: tasks of at least `min_particles` particles spread them over
+ * the warp lanes by shared-memory bank class before p2g_2 (the lane table:
+ * fewer bank conflicts on the arena atomics, at the price of its barriers
+ * and position loads); smaller tasks keep the bin order.  0 restores the
+ * default (128); a value above 1024 turns the table off.  Results do not
+ * depend on it. */
+int mpm_set_lane_table_min(mpm_sim* sim, int min_particles);
+int mpm_get_lane_table_min(const mpm_sim* sim);
 /* Autotuner: times `substeps` substeps for each task size in {64, 128, 256,
- * 512, 1024} from the current state, keeps the fastest and restores the
+ * 512, 1024} and each lane-table threshold in {32, 128, 512, off} from the
+ * current state (each pair once untimed first, so its CUDA graphs are
+ * captured outside the timing), keeps the fastest pair and restores the
  * state (particles, posvel, counters and grid are as before the call).
- * Writes the choice to *chosen_task_size when non-null.  Synchronizes. */
+ * Writes the task size to *chosen_task_size when non-null (the threshold:
+ * mpm_get_lane_table_min).  Synchronizes. */
 int mpm_autotune(mpm_sim* sim, int substeps, int* chosen_task_size);
 
 /* Batches: many independent scenes that advance together, one launch per
@@ -262,6 +273,9 @@ int mpm_batch_upload(mpm_batch* batch, const float* aos80);
 int mpm_batch_set_scene(mpm_batch* batch, int scene, const mpm_scene_desc* desc);
 int mpm_batch_set_graph(mpm_batch* batch, int enable); /* default 1 */
 int mpm_batch_set_task_size(mpm_batch* batch, int task_size); /* see mpm_set_task_size */
+int mpm_batch_get_task_size(const mpm_batch* batch);
+int mpm_batch_set_lane_table_min(mpm_batch* batch, int min_particles); /* see mpm_set_lane_table_min */
+int mpm_batch_get_lane_table_min(const mpm_batch* batch);
 /* See mpm_autotune: the batch's particles and posvel are as before the call;
  * mpm_batch_download_grid returns zeros until the next step. */
 int mpm_batch_autotune(mpm_batch* batch, int substeps, int* chosen_task_size);

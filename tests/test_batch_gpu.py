@@ -172,7 +172,9 @@ def test_batch_task_size_and_autotune(cuda, pkg, oracle_mod):
     batch = pkg.MLSMPMBatch(descs, recs)
     batch.step(2)
     before = batch.downloadParticles()
-    assert batch.autotune(2) in (64, 128, 256, 512, 1024)
+    chosen = batch.autotune(2)
+    assert chosen in (64, 128, 256, 512, 1024) and batch.taskSize == chosen
+    assert batch.laneTableMin in (32, 128, 512, 1 << 30)
     assert_bits_equal(batch.downloadParticles(), before, "particles after autotune")
     batch.step(4)
     assert_bits_equal(batch.downloadParticles(), results[0], "after autotune")

@@ -307,6 +307,33 @@ def test_task_size_does_not_change_results(cuda, pkg, oracle_mod, cap):
     sim.close()
 
 
+def test_lane_table_threshold_does_not_change_results(cuda, pkg, oracle_mod):
+    """The lane table on every task (1), on none (2^30), or from 32 / 128
+    particles: same bits as the oracle."""
+    box = [40.0, 30.0, 60.0]
+    sims = []
+    for lane in (1, 32, 128, 1 << 30):
+        sim = make_sim(pkg, "sorted")
+        sim.reset(70000, box)
+        sim.laneTableMin = lane
+        assert sim.laneTableMin == lane
+        sims.append((lane, sim))
+    ref = oracle_mod.OracleSim(sims[0][1].downloadParticles(), box)
+    for _ in range(5):
+        for _, sim in sims:
+            sim.execute()
+        ref.execute(2, NTHREADS)
+    for lane, sim in sims:
+        assert_state_equal(sim, ref, f"lane table from {lane} particles")
+        sim.close()
+    sim = make_sim(pkg, "sorted")
+    sim.laneTableMin = 0
+    assert sim.laneTableMin == 128
+    with pytest.raises(Exception):
+        sim.laneTableMin = -1
+    sim.close()
+
+
 def test_autotune_keeps_the_state(cuda, pkg, oracle_mod):
     box = [40.0, 30.0, 60.0]
     sim = make_sim(pkg, "sorted")
@@ -318,6 +345,7 @@ def test_autotune_keeps_the_state(cuda, pkg, oracle_mod):
     before = (sim.downloadParticles(), sim.downloadGrid(), sim.downloadPosvel())
     chosen = sim.autotune(4)
     assert chosen in (64, 128, 256, 512, 1024) and sim.taskSize == chosen
+    assert sim.laneTableMin in (32, 128, 512, 1 << 30)
     assert_bits_equal(sim.downloadParticles(), before[0], "particles after autotune")
     assert_bits_equal(sim.downloadGrid(), before[1], "grid after autotune")
     assert_bits_equal(sim.downloadPosvel(), before[2], "posvel after autotune")

@@ -467,6 +467,17 @@ int mpm_set_task_size(mpm_sim* s, int cap) {
 
 int mpm_get_task_size(const mpm_sim* s) { return s ? sorted_task_cap(s->sorted) : MPM_E_INVALID; }
 
+int mpm_set_lane_table_min(mpm_sim* s, int min_particles) {
+    if (int rc = check_sim(s)) return rc;
+    if (sorted_set_lane_table_min(s->sorted, min_particles) != 0)
+        return fail(MPM_E_INVALID, sorted_error());
+    return MPM_OK;
+}
+
+int mpm_get_lane_table_min(const mpm_sim* s) {
+    return s ? sorted_lane_table_min(s->sorted) : MPM_E_INVALID;
+}
+
 
 int mpm_autotune(mpm_sim* s, int substeps, int* chosen_task_size) {
     if (int rc = check_sim(s)) return rc;
@@ -485,7 +496,7 @@ int mpm_autotune(mpm_sim* s, int substeps, int* chosen_task_size) {
                            s->graph);
     };
     const int rc = tune_task_cap(s->sorted, s->ps, s->n, s->posvel, s->counters, substeps,
-                                 s->internal, step, chosen_task_size, nullptr);
+                                 s->internal, step, chosen_task_size, nullptr, nullptr);
     s->ref_current = true;  // the grid from before the call
     return rc;
 }

@@ -194,6 +194,21 @@ int mpm_batch_set_task_size(mpm_batch* b, int cap) {
     return MPM_OK;
 }
 
+int mpm_batch_get_task_size(const mpm_batch* b) {
+    return b && b->sorted ? sorted_task_cap(b->sorted) : MPM_E_INVALID;
+}
+
+int mpm_batch_set_lane_table_min(mpm_batch* b, int min_particles) {
+    if (int rc = check_batch(b)) return rc;
+    if (sorted_set_lane_table_min(b->sorted, min_particles) != 0)
+        return fail(MPM_E_INVALID, sorted_error());
+    return MPM_OK;
+}
+
+int mpm_batch_get_lane_table_min(const mpm_batch* b) {
+    return b && b->sorted ? sorted_lane_table_min(b->sorted) : MPM_E_INVALID;
+}
+
 int mpm_batch_autotune(mpm_batch* b, int substeps, int* chosen_task_size) {
     if (int rc = check_batch(b)) return rc;
     if (substeps < 1) return fail(MPM_E_INVALID, "substeps must be positive");
@@ -204,7 +219,7 @@ int mpm_batch_autotune(mpm_batch* b, int substeps, int* chosen_task_size) {
                            &b->prof, b->graph);
     };
     const int rc = tune_task_cap(b->sorted, b->ps, b->n, b->posvel, b->counters, substeps, nullptr,
-                                 step, chosen_task_size, nullptr);
+                                 step, chosen_task_size, nullptr, nullptr);
     b->stepped = false;
     return rc;
 }

@@ -64,14 +64,17 @@ long long grid_count_of(const float b[3]);
 // (capi_batch.cu).
 int scene_consts(const mpm_scene_desc& d, SimConsts& k);
 
-// Times `substeps` sorted-engine substeps for each candidate task size from
-// the same saved state and keeps the fastest.  The state after the call is
-// the state before it (particles, posvel, counters, grid).
+// Times `substeps` sorted-engine substeps for each pair of task size and
+// lane-table threshold from the same saved state and keeps the fastest.
+// Each candidate first runs once untimed, so that the CUDA graphs the timed
+// run replays are captured outside it.  The state after the call is the
+// state before it (particles, posvel, counters, grid).
 template <class StepFn>
 int tune_task_cap(SortedEngine* e, ParticleStore& ps, int n, float4* posvel,
                   unsigned long long* counters, int substeps, cudaStream_t st, StepFn step,
-                  int* chosen, double* ms_out) {
-    static const int kCands[] = {64, 128, 256, 512, 1024};
+                  int* chosen, int* chosen_lane, double* ms_out) {
+    static const int kCaps[] = {64, 128, 256, 512, 1024};
+    static const int kLanes[] = {32, 128, 512, 1 << 30};  // 1 << 30: no lane table
     Particles save{};
     float4* pv = nullptr;
     unsigned long long cnt[2] = {0, 0};
@@ -116,20 +119,29 @@ int tune_task_cap(SortedEngine* e, ParticleStore& ps, int n, float4* posvel,
         sorted_invalidate(e);
         return cudaGetLastError();
     };
-    int best = 0;
+    int best = 0, best_lane = 0;
     double best_ms = 0.0;
-    for (int cap : kCands) {
-        if (err != cudaSuccess) break;
-        if (sorted_set_task_cap(e, cap) != 0) continue;
-        if ((err = restore()) != cudaSuccess) break;
-        if (step(1) != 0) { err = cudaErrorLaunchFailure; break; }  // primes
-        cudaEventRecord(a, st);
-        if (step(substeps) != 0) { err = cudaErrorLaunchFailure; break; }
-        cudaEventRecord(b, st);
-        if ((err = cudaEventSynchronize(b)) != cudaSuccess) break;
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, a, b);
-        if (!best || ms < best_ms) { best = cap; best_ms = ms; }
+    for (int cap : kCaps) {
+        for (int lane : kLanes) {
+            if (err != cudaSuccess) break;
+            if (sorted_set_task_cap(e, cap) != 0 || sorted_set_lane_table_min(e, lane) != 0)
+                continue;
+            if ((err = restore()) != cudaSuccess) break;
+            if (step(1) != 0 || step(substeps) != 0) { err = cudaErrorLaunchFailure; break; }
+            if ((err = restore()) != cudaSuccess) break;
+            if (step(1) != 0) { err = cudaErrorLaunchFailure; break; }  // primes
+            cudaEventRecord(a, st);
+            if (step(substeps) != 0) { err = cudaErrorLaunchFailure; break; }
+            cudaEventRecord(b, st);
+            if ((err = cudaEventSynchronize(b)) != cudaSuccess) break;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            if (!best || ms < best_ms) {
+                best = cap;
+                best_lane = lane;
+                best_ms = ms;
+            }
+        }
     }
     if (err == cudaSuccess) err = restore();
     if (err == cudaSuccess)
@@ -138,8 +150,12 @@ int tune_task_cap(SortedEngine* e, ParticleStore& ps, int n, float4* posvel,
     if (err == cudaSuccess) err = cudaStreamSynchronize(st);
     cleanup();
     if (err != cudaSuccess) return cuda_fail(err, "autotune");
-    if (best) sorted_set_task_cap(e, best);
+    if (best) {
+        sorted_set_task_cap(e, best);
+        sorted_set_lane_table_min(e, best_lane);
+    }
     if (chosen) *chosen = best;
+    if (chosen_lane) *chosen_lane = best_lane;
     if (ms_out) *ms_out = best_ms;
     return MPM_OK;
 }

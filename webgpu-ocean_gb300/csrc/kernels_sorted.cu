@@ -86,9 +86,10 @@ constexpr int kMaxTaskCap = 1 << 30;
 #ifndef MPM_P2G2_MIN_BLOCKS
 #define MPM_P2G2_MIN_BLOCKS (1024 / MPM_TASK_THREADS)
 #endif
-// Tasks with fewer particles than this skip the bank-class lane table (its
-// barriers and position loads cost more than the bank conflicts it saves
-// when a brick holds a few dozen particles) and keep the bin order.
+// Default for Dev::lane_min: tasks with fewer particles skip the bank-class
+// lane table (its barriers and position loads cost more than the bank
+// conflicts it saves when a brick holds a few dozen particles) and keep the
+// bin order.  The autotuner chooses it per workload.
 #ifndef MPM_LANE_TABLE_MIN
 #define MPM_LANE_TABLE_MIN 128
 #endif
@@ -150,6 +151,7 @@ struct Dev {
     const uint32_t* bin_scene;    // global bin -> scene
     int nscenes;
     int task_cap;                 // most particles per task
+    int lane_min;                 // tasks of at least this many particles use the lane table
 };
 
 // The scene of a task: the table entry in a batch, else the kernel's own.
@@ -524,7 +526,7 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
         int tbx = 0, tby = 0, tbz = 0;
         if (task.brick >= 0) brick_coords(g, task.brick, tbx, tby, tbz);
         const bool table = task.brick >= 0 && task.count <= kMaxSort &&
-                           task.count >= MPM_LANE_TABLE_MIN;  // uniform
+                           task.count >= d.lane_min;  // uniform
         if (table) build_lane_table(P, g, d, task, tbx, tby, tbz, s_lt);
         for (int j = threadIdx.x; j < task.count; j += kTask) {
             const int slot = table ? (int)s_lt.slot[j] : (int)d.order[task.first + j];
@@ -1201,6 +1203,7 @@ int sorted_create(SortedEngine** out, int max_particles) {
     e->max_particles = max_particles;
     e->d.nscenes = 1;
     e->d.task_cap = kMaxSort;
+    e->d.lane_min = MPM_LANE_TABLE_MIN;
     const size_t np = (size_t)(max_particles > 0 ? max_particles : 1);
     cudaError_t r = cudaMalloc(&e->d.bin_of, 4 * np);
     if (r == cudaSuccess) r = cudaMalloc(&e->d.rank_of, 4 * np);
@@ -1339,6 +1342,19 @@ int sorted_set_task_cap(SortedEngine* e, int cap) {
 }
 
 int sorted_task_cap(const SortedEngine* e) { return e->d.task_cap; }
+
+int sorted_set_lane_table_min(SortedEngine* e, int min_particles) {
+    if (min_particles < 0) {
+        g_err = "lane table threshold must be >= 0 (0: default)";
+        return -1;
+    }
+    const int v = min_particles == 0 ? MPM_LANE_TABLE_MIN : min_particles;
+    if (v != e->d.lane_min) drop_graphs(e);  // the captured launches carry it
+    e->d.lane_min = v;
+    return 0;
+}
+
+int sorted_lane_table_min(const SortedEngine* e) { return e->d.lane_min; }
 
 int sorted_set_scene_consts(SortedEngine* e, int scene, const SimConsts& k, cudaStream_t st) {
     if (!e->configured || !e->batch || scene < 0 || scene >= (int)e->scenes.size()) {

@@ -32,6 +32,14 @@ int sorted_set_scene_consts(SortedEngine* e, int scene, const SimConsts& k, cuda
 int sorted_set_task_cap(SortedEngine* e, int cap);
 int sorted_task_cap(const SortedEngine* e);
 
+// Tasks of at least `min_particles` particles order them into the bank-class
+// lane table before p2g_2 (fewer shared-memory bank conflicts, at the price
+// of the table's barriers and position loads); smaller tasks keep the bin
+// order.  0 restores the default (128); a value above 1024 turns the table
+// off.  Results do not depend on it.
+int sorted_set_lane_table_min(SortedEngine* e, int min_particles);
+int sorted_lane_table_min(const SortedEngine* e);
+
 // Forgets the carried-over state (the next step re-bins and redoes p2g_1).
 void sorted_invalidate(SortedEngine* e);
 

@@ -239,8 +239,20 @@ class MLSMPMSimulator:
     def taskSize(self, cap: int) -> None:
         _check(self._lib.mpm_set_task_size(self._handle, int(cap)), "taskSize")
 
+    @property
+    def laneTableMin(self) -> int:
+        """Smallest sorted-engine task that orders its particles by bank class
+        (0 to set: the default; above 1024: never)."""
+        return _check(self._lib.mpm_get_lane_table_min(self._handle), "laneTableMin")
+
+    @laneTableMin.setter
+    def laneTableMin(self, min_particles: int) -> None:
+        _check(self._lib.mpm_set_lane_table_min(self._handle, int(min_particles)),
+               "laneTableMin")
+
     def autotune(self, substeps: int = 8) -> int:
-        """Picks the fastest task size for the current scene; state unchanged."""
+        """Picks the fastest task size and lane-table threshold for the
+        current scene (returns the task size); state unchanged."""
         out = ctypes.c_int(0)
         _check(self._lib.mpm_autotune(self._handle, int(substeps), ctypes.byref(out)), "autotune")
         return int(out.value)
@@ -467,7 +479,22 @@ class MLSMPMBatch:
     def setTaskSize(self, cap: int) -> None:
         _check(self._lib.mpm_batch_set_task_size(self._handle, int(cap)), "setTaskSize")
 
+    @property
+    def taskSize(self) -> int:
+        return _check(self._lib.mpm_batch_get_task_size(self._handle), "taskSize")
+
+    @property
+    def laneTableMin(self) -> int:
+        """See MLSMPMSimulator.laneTableMin."""
+        return _check(self._lib.mpm_batch_get_lane_table_min(self._handle), "laneTableMin")
+
+    @laneTableMin.setter
+    def laneTableMin(self, min_particles: int) -> None:
+        _check(self._lib.mpm_batch_set_lane_table_min(self._handle, int(min_particles)),
+               "laneTableMin")
+
     def autotune(self, substeps: int = 4) -> int:
+        """Task size and lane-table threshold, as MLSMPMSimulator.autotune."""
         out = ctypes.c_int(0)
         _check(self._lib.mpm_batch_autotune(self._handle, int(substeps), ctypes.byref(out)),
                "autotune")
