@@ -22,8 +22,11 @@ Our arm (default):
   roofline  the dominant kernel's algorithmic bytes per launch over its mean
           CUDA-event duration, against the measured HBM copy bandwidth;
           issue_roofline: its warp-instructions per launch against the SMs'
-          issue rate.  The profiling pass and both e2e loops restart from
-          the timed region's state (upload + the same warm-up).
+          issue rate; path_roofline: the whole substep's algorithmic bytes
+          as the reference's six dispatches define them (204 B per
+          particle + 100 B per grid cell) at the measured substep rate.
+          The profiling pass and both e2e loops restart from the timed
+          region's state (upload + the same warm-up).
   cpu_baseline  the C oracle (oracle/) on the host cores, bounded sample.
 --impl reference: the oracle (the CPU restatement of the reference's kernels)
 on all host threads, same workload and metric.  Under torchrun, rank 0 alone
@@ -222,6 +225,29 @@ def algorithmic_bytes(kernel: str, n: int, cells: int) -> float | None:
         # x, C in (48); mass in (4), momentum read-modify-write (12 + 12)
         return n * 48 + cells * 28
     return None
+
+
+# The whole substep's algorithmic bytes as the reference's six dispatches
+# define them (each stage reads its inputs once and writes its outputs once,
+# an atomic result counted as one write per cell): per particle p2g_1 reads
+# x, v, C (60 B), p2g_2 x, C (48), g2p x (12) and writes x, v, C (60),
+# copyPosition writes pos, v (24); per grid cell (all gridCount cells, which
+# clearGrid and updateGrid visit) clear 16, p2g_1 16, p2g_2 mass 4 and
+# momentum read + write 24, updateGrid 16 + 12, g2p 12.
+PATH_BYTES_PER_PARTICLE = 60 + 48 + 12 + 60 + 24
+PATH_BYTES_PER_CELL = 16 + 16 + 4 + 24 + 16 + 12 + 12
+
+
+def path_roofline(n: int, grid_cells: int, particle_substeps_per_s: float, peak: dict) -> dict:
+    """The whole substep against HBM: its algorithmic bytes per substep
+    times substeps per second, over the measured copy bandwidth."""
+    per_substep = PATH_BYTES_PER_PARTICLE * n + PATH_BYTES_PER_CELL * grid_cells
+    achieved = per_substep * (particle_substeps_per_s / n) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / peak["hbm_gbs"], "peak_source": peak["source"],
+            "bytes_per_substep": per_substep,
+            "definition": f"({PATH_BYTES_PER_PARTICLE} B x particles + {PATH_BYTES_PER_CELL} B x "
+                          "gridCount cells) per substep x substeps/s (value / particles)"}
 
 
 BATCH_SCENES, BATCH_SUBSTEPS, BATCH_SEED = 256, 100, 20240601
@@ -850,6 +876,7 @@ def run_ours(args) -> None:
                 "serialized_api": ("changeBoxSize(host) + execute() + downloadPosvel() into pinned "
                                    "host memory, per-step events, L2 flushed outside them")},
         "roofline": roof,
+        "path_roofline": path_roofline(n, 128 ** 3, value, peaks),
         "cpu_baseline": cpu,
         "clocks": clocks,
         "issue_roofline": issue,
