@@ -337,6 +337,22 @@ int mpm_backward(mpm_adjoint* adj, const float* seeds_aos80, const int* seed_sub
 int mpm_backward_list(mpm_adjoint* adj, const float* const* seeds_aos80, const int* seed_substeps,
                       int num_seeds, float* grad_init_aos80, double* grad_params, void* stream);
 
+/* Position observations for inverse problems, computed on the device so the
+ * states and seeds never leave it.  mpm_adjoint_set_observations replaces
+ * the observations: `count` blocks of n x 3 floats (positions in particle
+ * order), block j observed after substeps[j] substeps.  After a forward,
+ * mpm_adjoint_observation_loss writes per scene s
+ *   loss[s] = sum_j (1 / n_s) sum_{i in s} |x_i(substeps[j]) - obs_j,i|^2
+ * (FP64 sums of f32 differences; the observed substeps must be checkpoints
+ * of that forward) and keeps the seeds dL/dx = f32(2 / n_s) * (x - obs) on
+ * the device; mpm_backward_observed then runs mpm_backward with them.
+ * Both synchronize. */
+int mpm_adjoint_set_observations(mpm_adjoint* adj, int count, const int* substeps,
+                                 const float* const* obs_xyz);
+int mpm_adjoint_observation_loss(mpm_adjoint* adj, double* loss_per_scene, void* stream);
+int mpm_backward_observed(mpm_adjoint* adj, float* grad_init_aos80, double* grad_params,
+                          void* stream);
+
 /* Headless screen-space renderer (render/fluidRender.ts, fluid path):
  * depth splat, 4 x bilateral filter, thickness splat, gaussian filter and
  * shading, from the posvel records the simulator writes, into an image in

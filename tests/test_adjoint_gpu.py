@@ -229,6 +229,55 @@ def test_inverse_problem_recovers_constants(cuda, pkg):
 
 
 @pytest.mark.parametrize("tape", ["fixed", "fp64"])
+def test_observation_loss_matches_host_loss(cuda, pkg, tape):
+    """observationLoss / backwardObserved (loss and seeds on the device)
+    against the same loss, seeds and backward computed on the host from the
+    read-back states."""
+    inv = pkg.inverse
+    descs, recs, _ = inv.inverse_scenes(3, seed=4, n_range=(3000, 5000), side=32)
+    T, steps = 30, [10, 20, 30]
+    adj = pkg.MLSMPMAdjoint(descs, T, 10, tape=tape)
+    for s in range(3):
+        adj.setScene(s, inv.with_constants(descs[s], 2.5, 0.15))
+    observed = inv.observe(adj, recs, T, steps)
+    for s in range(3):
+        adj.setScene(s, descs[s])
+    adj.setObservations(observed)
+    adj.forward(recs, T)
+    loss_dev = adj.observationLoss()
+    g_dev, p_dev = adj.backwardObserved()
+
+    offs = adj.sceneOffsets
+    counts = np.diff(offs)
+    scale = (2.0 / np.repeat(counts.astype(np.float64), counts)).astype(np.float32)[:, None]
+    loss_host = np.zeros(3)
+    seeds = {}
+    for t in steps:
+        x = adj.state(t)
+        diff = x[:, 0:3] - observed[t].astype(np.float32)
+        sq = np.einsum("ij,ij->i", diff, diff, dtype=np.float64)
+        loss_host += np.add.reduceat(sq, offs[:-1]) / counts
+        seeds[t] = np.zeros_like(x)
+        seeds[t][:, 0:3] = diff * scale
+    assert (loss_host > 0).all()
+    np.testing.assert_allclose(loss_dev, loss_host, rtol=1e-12)
+    g_host, p_host = adj.backward(seeds)
+    # the same seeds; float atomics make the summation order differ
+    np.testing.assert_allclose(g_dev, g_host, rtol=1e-4, atol=1e-5 * float(np.abs(g_host).max()))
+    np.testing.assert_allclose(p_dev, p_host, rtol=1e-4)
+    assert np.isfinite(g_dev).all()
+
+    # the seeds belong to one forward; observed substeps must be checkpoints
+    adj.forward(recs, T)
+    with pytest.raises(pkg.MPMError):
+        adj.backwardObserved()
+    adj.setObservations({15: observed[10]})
+    with pytest.raises(pkg.MPMError):
+        adj.observationLoss()
+    adj.close()
+
+
+@pytest.mark.parametrize("tape", ["fixed", "fp64"])
 def test_repeated_backward_after_one_forward(cuda, pkg, tape):
     """A second and third backward after the same forward (the first one used
     the forward's record of the last segment, later ones recompute it) give

@@ -43,7 +43,8 @@ def test_loss_seeds_and_adam_step(pkg):
     pgrad = np.array([[0.5, -2.0], [-1.0, 0.25], [3.0, 1.0]])
     adj = FakeAdjoint(pkg, counts, states, pgrad)
     start = np.array([[3.0, 0.1], [2.0, 0.2], [2.5, 0.05]])
-    fit = pkg.inverse.fit_parameters(adj, None, observed, 8, start, iters=2, lr=0.1)
+    fit = pkg.inverse.fit_parameters(adj, None, observed, 8, start, iters=2, lr=0.1,
+                                     device_loss=False)
 
     offs = adj.sceneOffsets
     want_loss = np.zeros(3)

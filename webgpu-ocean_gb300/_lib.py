@@ -183,6 +183,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "mpm_adjoint_state": (i32, [vp, i32, fp]),
         "mpm_backward": (i32, [vp, fp, ip, i32, fp, dp, vp]),
         "mpm_backward_list": (i32, [vp, ctypes.POINTER(fp), ip, i32, fp, dp, vp]),
+        "mpm_adjoint_set_observations": (i32, [vp, i32, ip, ctypes.POINTER(fp)]),
+        "mpm_adjoint_observation_loss": (i32, [vp, dp, vp]),
+        "mpm_backward_observed": (i32, [vp, fp, dp, vp]),
         "mpm_renderer_create": (i32, [i32, i32, f32, f32, ctypes.POINTER(vp)]),
         "mpm_renderer_destroy": (i32, [vp]),
         "mpm_renderer_set_envmap": (i32, [vp, i32, fp]),

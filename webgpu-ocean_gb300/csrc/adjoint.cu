@@ -718,6 +718,54 @@ __global__ void k_rec64_to_records(const double* __restrict__ S, float* __restri
         for (int r = 0; r < 3; ++r) P[8 + 4 * c + r] = (float)q[6 + 3 * c + r];
 }
 
+// Squared-distance loss of one observed substep (inverse problems), per
+// particle i of scene s: d = x_i - obs_i in f32, seed_i = the adjoint record
+// whose position is scale[s] * d (scale = f32(2 / particles of s)) and whose
+// other entries are 0, and loss[s] += |d|^2 summed in FP64.  A warp whose
+// particles all belong to one scene adds one reduced term.
+template <bool F64>
+__global__ void k_obs_loss(Particles X, const double* __restrict__ X64,
+                           const float4* __restrict__ obs, const int* __restrict__ pscene,
+                           const float* __restrict__ scale, Particles seed,
+                           double* __restrict__ loss, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = i < n;
+    int s = -1;
+    double sq = 0.0;
+    if (act) {
+        float x0, x1, x2;
+        if (F64) {
+            const double* q = X64 + (size_t)kRec64 * i;
+            x0 = (float)q[0];
+            x1 = (float)q[1];
+            x2 = (float)q[2];
+        } else {
+            const float4 a = X.p0[i];
+            x0 = a.x;
+            x1 = a.y;
+            x2 = a.z;
+        }
+        const float4 o = obs[i];
+        const float dx = __fsub_rn(x0, o.x), dy = __fsub_rn(x1, o.y), dz = __fsub_rn(x2, o.z);
+        s = pscene[i];
+        const float c = scale[s];
+        const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        seed.p0[i] = make_float4(__fmul_rn(dx, c), __fmul_rn(dy, c), __fmul_rn(dz, c), 0.0f);
+        seed.p1[i] = zero;
+        seed.p2[i] = zero;
+        seed.p3[i] = zero;
+        sq = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    }
+    const int s0 = __shfl_sync(0xffffffffu, s, 0);
+    if (__all_sync(0xffffffffu, !act || s == s0)) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) sq += __shfl_down_sync(0xffffffffu, sq, off);
+        if ((threadIdx.x & 31) == 0 && s0 >= 0) atomicAdd(loss + s0, sq);
+    } else if (act) {
+        atomicAdd(loss + s, sq);
+    }
+}
+
 // A += B over n records (all four streams).
 __global__ void k_axpy(Particles A, Particles B, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1007,6 +1055,18 @@ void launch_records_to_rec64(const float* rec, double* S, int n, cudaStream_t st
 void launch_rec64_to_records(const double* S, float* rec, int n, cudaStream_t st) {
     if (n <= 0) return;
     k_rec64_to_records<<<blocks(n), kThreads, 0, st>>>(S, rec, n);
+}
+
+void launch_obs_loss(const Particles* X, const double* X64, const float4* obs, const int* pscene,
+                     const float* scale, const Particles& seed, double* loss, int n,
+                     cudaStream_t st) {
+    if (n <= 0) return;
+    if (X64)
+        k_obs_loss<true><<<blocks(n), kThreads, 0, st>>>(Particles{}, X64, obs, pscene, scale,
+                                                         seed, loss, n);
+    else
+        k_obs_loss<false><<<blocks(n), kThreads, 0, st>>>(*X, nullptr, obs, pscene, scale, seed,
+                                                          loss, n);
 }
 
 void launch_particles_axpy(const Particles& A, const Particles& B, int n, cudaStream_t st) {

@@ -67,4 +67,12 @@ void launch_rec64_to_records(const double* S, float* rec, int n, cudaStream_t st
 // A += B, record-wise over n particles.
 void launch_particles_axpy(const Particles& A, const Particles& B, int n, cudaStream_t st);
 
+// Squared-distance loss of one observed substep: state X (fixed-point tape)
+// or X64 (FP64 tape, when non-null) against obs (n float4, xyz), seeds into
+// `seed` (position = scale[scene] * (x - obs), rest 0), |x - obs|^2 summed
+// per scene into loss (FP64).
+void launch_obs_loss(const Particles* X, const double* X64, const float4* obs, const int* pscene,
+                     const float* scale, const Particles& seed, double* loss, int n,
+                     cudaStream_t st);
+
 }  // namespace mpm

@@ -44,6 +44,12 @@ struct mpm_adjoint {
     double* pgrad_d = nullptr;
     AdjSort sort;                    // per-substep spatial sort of the adjoint kernels
     std::vector<Particles> seedbuf;  // seeds of mpm_backward, kept between calls
+    // observation loss (mpm_adjoint_set_observations)
+    std::vector<float4*> obs;        // observed positions (n float4 each)
+    std::vector<int> obs_steps;      // their substeps
+    float* obs_scale = nullptr;      // per scene: f32(2 / its particle count)
+    double* obs_loss = nullptr;      // per scene: sum of |x - obs|^2
+    bool obs_seeded = false;         // seedbuf[0 .. obs) hold the seeds of the last forward
     // The backward as one CUDA graph, captured for (T, every, tape, seed
     // substeps) and replayed while they stay the same.
     cudaGraphExec_t bgraph = nullptr;
@@ -202,8 +208,18 @@ void drop_backward_graph(mpm_adjoint* a) {
     a->bg_T = -1;
 }
 
+void free_observations(mpm_adjoint* a) {
+    for (float4* p : a->obs) cudaFree(p);
+    a->obs.clear();
+    a->obs_steps.clear();
+    a->obs_seeded = false;
+}
+
 void free_adjoint(mpm_adjoint* a) {
     drop_backward_graph(a);
+    free_observations(a);
+    cudaFree(a->obs_scale);
+    cudaFree(a->obs_loss);
     for (Particles& P : a->seedbuf) free_particles(P);
     free_tapes(a);
     free_particles(a->adj[0]);
@@ -383,6 +399,87 @@ int ckpt_slot(const mpm_adjoint* a, int step, int T) {
     return -1;
 }
 
+// At least `count` seed buffers (device streams kept between calls: a
+// captured backward reads them at fixed addresses).
+int ensure_seed_buffers(mpm_adjoint* a, int count) {
+    while ((int)a->seedbuf.size() < count) {
+        drop_backward_graph(a);
+        Particles P{};
+        const cudaError_t e = alloc_particles(P, (size_t)(a->b->n > 0 ? a->b->n : 1));
+        if (e != cudaSuccess) {
+            free_particles(P);
+            return cuda_fail(e, "mpm_backward seeds");
+        }
+        a->seedbuf.push_back(P);
+    }
+    return MPM_OK;
+}
+
+// The backward of the last forward with seedbuf[i] added at substep
+// steps[i]: replays the captured graph when (T, interval, tape, seed
+// substeps) match the last capture, else captures it (plain launches while
+// kernels are profiled); then reads the gradients back.  Synchronizes.
+int run_backward(mpm_adjoint* a, const std::vector<int>& steps, float* grad_init,
+                 double* grad_params, cudaStream_t st) {
+    mpm_batch* b = a->b;
+    const int n = b->n, S = (int)b->consts.size(), nseeds = (int)steps.size();
+    int cur = 0;
+    if (b->prof.enabled) {  // per-launch profiling: no graph, one stream
+        if (int rc = enqueue_backward(a, steps.data(), nseeds, st, st, nullptr, &cur)) return rc;
+    } else if (a->bgraph && a->bg_T == a->T && a->bg_every == a->every && a->bg_tape == a->tape &&
+               a->bg_last_taped == a->last_taped && a->bg_steps == steps) {
+        MPM_CUDA(cudaGraphLaunch(a->bgraph, st));
+        cur = a->bg_cur;
+    } else {
+        drop_backward_graph(a);
+        // capture stream, recompute stream and the events that order them
+        cudaStream_t cs = nullptr, rs = nullptr;
+        cudaEvent_t ev[5] = {};
+        cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&rs, cudaStreamNonBlocking);
+        for (int i = 0; i < 5 && e == cudaSuccess; ++i)
+            e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
+        const bool engine_graph = b->graph;
+        b->graph = false;  // the engine's kernels go straight into this graph
+        cudaGraph_t graph = nullptr;
+        int rc = 0;
+        if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            rc = enqueue_backward(a, steps.data(), nseeds, cs, rs, ev, &cur);
+            e = cudaStreamEndCapture(cs, &graph);
+        }
+        b->graph = engine_graph;
+        cudaGraphExec_t exec = nullptr;
+        if (e == cudaSuccess && rc == 0) e = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        for (cudaEvent_t x : ev)
+            if (x) cudaEventDestroy(x);
+        if (rs) cudaStreamDestroy(rs);
+        if (cs) cudaStreamDestroy(cs);
+        if (rc) return rc;
+        if (e != cudaSuccess) return cuda_fail(e, "mpm_backward capture");
+        a->bgraph = exec;
+        a->bg_T = a->T;
+        a->bg_every = a->every;
+        a->bg_tape = a->tape;
+        a->bg_last_taped = a->last_taped;
+        a->bg_steps = steps;
+        a->bg_cur = cur;
+        MPM_CUDA(cudaGraphLaunch(exec, st));
+    }
+    // the recompute of the earlier segments reused the buffers that held the
+    // forward's record of the last one: a further backward recomputes it
+    a->last_taped = false;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "mpm_backward");
+    if (grad_init) MPM_CUDA(download_records(a->adj[cur], grad_init, n, a->stage, st));
+    if (grad_params)
+        MPM_CUDA(cudaMemcpy(grad_params, a->pgrad_d, sizeof(double) * 2 * (size_t)S,
+                            cudaMemcpyDeviceToHost));
+    return MPM_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -500,6 +597,7 @@ int mpm_forward_ckpt(mpm_adjoint* a, const float* init, int substeps, void* stre
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int n = b->n, S = (int)b->consts.size();
     a->T = -1;
+    a->obs_seeded = false;
     MPM_CUDA(cudaStreamSynchronize(st));
     // The last checkpoint segment is the first one the backward needs: its
     // states and updated grids are recorded here, as the backward's
@@ -599,78 +697,97 @@ int mpm_backward_list(mpm_adjoint* a, const float* const* seeds, const int* seed
             return fail(MPM_E_INVALID, "seed substep outside [0, T]");
     DeviceGuard g(b->device);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int n = b->n, S = (int)b->consts.size();
     MPM_CUDA(cudaStreamSynchronize(st));
-    // seeds into device streams kept between calls (a captured backward
-    // reads them at fixed addresses)
-    while ((int)a->seedbuf.size() < nseeds) {
-        drop_backward_graph(a);
-        Particles P{};
-        const cudaError_t e = alloc_particles(P, (size_t)(n > 0 ? n : 1));
-        if (e != cudaSuccess) {
-            free_particles(P);
-            return cuda_fail(e, "mpm_backward seeds");
-        }
-        a->seedbuf.push_back(P);
-    }
+    if (int rc = ensure_seed_buffers(a, nseeds)) return rc;
+    a->obs_seeded = false;  // the buffers now hold these seeds
     for (int i = 0; i < nseeds; ++i)
-        MPM_CUDA(upload_records(a->seedbuf[(size_t)i], seeds[i], n, a->stage, st));
-    const std::vector<int> steps(seed_steps, seed_steps + nseeds);
-    int cur = 0;
-    if (b->prof.enabled) {  // per-launch profiling: no graph, one stream
-        if (int rc = enqueue_backward(a, seed_steps, nseeds, st, st, nullptr, &cur)) return rc;
-    } else if (a->bgraph && a->bg_T == a->T && a->bg_every == a->every && a->bg_tape == a->tape &&
-               a->bg_last_taped == a->last_taped && a->bg_steps == steps) {
-        MPM_CUDA(cudaGraphLaunch(a->bgraph, st));
-        cur = a->bg_cur;
-    } else {
-        drop_backward_graph(a);
-        // capture stream, recompute stream and the events that order them
-        cudaStream_t cs = nullptr, rs = nullptr;
-        cudaEvent_t ev[5] = {};
-        cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&rs, cudaStreamNonBlocking);
-        for (int i = 0; i < 5 && e == cudaSuccess; ++i)
-            e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
-        const bool engine_graph = b->graph;
-        b->graph = false;  // the engine's kernels go straight into this graph
-        cudaGraph_t graph = nullptr;
-        int rc = 0;
-        if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            rc = enqueue_backward(a, seed_steps, nseeds, cs, rs, ev, &cur);
-            e = cudaStreamEndCapture(cs, &graph);
-        }
-        b->graph = engine_graph;
-        cudaGraphExec_t exec = nullptr;
-        if (e == cudaSuccess && rc == 0) e = cudaGraphInstantiate(&exec, graph, 0);
-        if (graph) cudaGraphDestroy(graph);
-        for (cudaEvent_t x : ev)
-            if (x) cudaEventDestroy(x);
-        if (rs) cudaStreamDestroy(rs);
-        if (cs) cudaStreamDestroy(cs);
-        if (rc) return rc;
-        if (e != cudaSuccess) return cuda_fail(e, "mpm_backward capture");
-        a->bgraph = exec;
-        a->bg_T = a->T;
-        a->bg_every = a->every;
-        a->bg_tape = a->tape;
-        a->bg_last_taped = a->last_taped;
-        a->bg_steps = steps;
-        a->bg_cur = cur;
-        MPM_CUDA(cudaGraphLaunch(exec, st));
+        MPM_CUDA(upload_records(a->seedbuf[(size_t)i], seeds[i], b->n, a->stage, st));
+    return run_backward(a, std::vector<int>(seed_steps, seed_steps + nseeds), grad_init,
+                        grad_params, st);
+}
+
+int mpm_adjoint_set_observations(mpm_adjoint* a, int count, const int* substeps,
+                                 const float* const* obs_xyz) {
+    if (!a) return fail(MPM_E_INVALID, "null adjoint handle");
+    if (count < 0 || (count > 0 && (!substeps || !obs_xyz)))
+        return fail(MPM_E_INVALID, "bad observations");
+    const int n = a->b->n;
+    for (int i = 0; i < count; ++i) {
+        if (!obs_xyz[i] && n) return fail(MPM_E_INVALID, "null observation block");
+        if (substeps[i] < 0 || substeps[i] > a->max_substeps)
+            return fail(MPM_E_INVALID, "observed substep outside [0, max_substeps]");
     }
-    // the recompute of the earlier segments reused the buffers that held the
-    // forward's record of the last one: a further backward recomputes it
-    a->last_taped = false;
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return cuda_fail(e, "mpm_backward");
-    if (grad_init) MPM_CUDA(download_records(a->adj[cur], grad_init, n, a->stage, st));
-    if (grad_params)
-        MPM_CUDA(cudaMemcpy(grad_params, a->pgrad_d, sizeof(double) * 2 * (size_t)S,
-                            cudaMemcpyDeviceToHost));
+    DeviceGuard g(a->b->device);
+    MPM_CUDA(cudaDeviceSynchronize());
+    free_observations(a);
+    const size_t np = (size_t)(n > 0 ? n : 1);
+    std::vector<float4> h(np);
+    for (int i = 0; i < count; ++i) {
+        float4* d = nullptr;
+        MPM_CUDA(cudaMalloc(&d, sizeof(float4) * np));
+        a->obs.push_back(d);
+        a->obs_steps.push_back(substeps[i]);
+        for (int j = 0; j < n; ++j)
+            h[(size_t)j] = make_float4(obs_xyz[i][3 * (size_t)j], obs_xyz[i][3 * (size_t)j + 1],
+                                       obs_xyz[i][3 * (size_t)j + 2], 0.0f);
+        MPM_CUDA(cudaMemcpy(d, h.data(), sizeof(float4) * (size_t)n, cudaMemcpyHostToDevice));
+    }
+    const int S = (int)a->b->consts.size();
+    if (!a->obs_scale) MPM_CUDA(cudaMalloc(&a->obs_scale, sizeof(float) * (size_t)S));
+    if (!a->obs_loss) MPM_CUDA(cudaMalloc(&a->obs_loss, sizeof(double) * (size_t)S));
+    std::vector<float> scale((size_t)S);
+    for (int s = 0; s < S; ++s) {
+        const int ns = a->b->desc[(size_t)s].num_particles;
+        scale[(size_t)s] = ns > 0 ? (float)(2.0 / ns) : 0.0f;
+    }
+    MPM_CUDA(cudaMemcpy(a->obs_scale, scale.data(), sizeof(float) * (size_t)S,
+                        cudaMemcpyHostToDevice));
     return MPM_OK;
+}
+
+int mpm_adjoint_observation_loss(mpm_adjoint* a, double* loss_per_scene, void* stream) {
+    if (!a) return fail(MPM_E_INVALID, "null adjoint handle");
+    if (a->T < 0) return fail(MPM_E_STATE, "no forward run");
+    mpm_batch* b = a->b;
+    const int n = b->n, S = (int)b->consts.size(), count = (int)a->obs.size();
+    for (int i = 0; i < count; ++i)
+        if (ckpt_slot(a, a->obs_steps[(size_t)i], a->T) < 0)
+            return fail(MPM_E_INVALID, "an observed substep is not a checkpoint of the last forward");
+    DeviceGuard g(b->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    MPM_CUDA(cudaStreamSynchronize(st));
+    if (int rc = ensure_seed_buffers(a, count)) return rc;
+    if (S > 0) MPM_CUDA(cudaMemsetAsync(a->obs_loss, 0, sizeof(double) * (size_t)S, st));
+    for (int i = 0; i < count; ++i) {
+        const int j = ckpt_slot(a, a->obs_steps[(size_t)i], a->T);
+        const bool f64 = a->tape == MPM_TAPE_FP64;
+        launch_obs_loss(f64 ? nullptr : &a->ckpt[(size_t)j], f64 ? a->ckpt64[(size_t)j] : nullptr,
+                        a->obs[(size_t)i], a->pscene_d, a->obs_scale, a->seedbuf[(size_t)i],
+                        a->obs_loss, n, st);
+    }
+    MPM_CUDA(cudaGetLastError());
+    std::vector<double> sums((size_t)S, 0.0);
+    if (S > 0)
+        MPM_CUDA(cudaMemcpyAsync(sums.data(), a->obs_loss, sizeof(double) * (size_t)S,
+                                 cudaMemcpyDeviceToHost, st));
+    MPM_CUDA(cudaStreamSynchronize(st));
+    for (int s = 0; s < S && loss_per_scene; ++s) {
+        const int ns = b->desc[(size_t)s].num_particles;
+        loss_per_scene[s] = ns > 0 ? sums[(size_t)s] / ns : 0.0;
+    }
+    a->obs_seeded = true;
+    return MPM_OK;
+}
+
+int mpm_backward_observed(mpm_adjoint* a, float* grad_init, double* grad_params, void* stream) {
+    if (!a) return fail(MPM_E_INVALID, "null adjoint handle");
+    if (a->T < 0) return fail(MPM_E_STATE, "no forward run");
+    if (!a->obs_seeded)
+        return fail(MPM_E_STATE, "no observation loss since the last forward");
+    DeviceGuard g(a->b->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    MPM_CUDA(cudaStreamSynchronize(st));
+    return run_backward(a, a->obs_steps, grad_init, grad_params, st);
 }
 
 }  // extern "C"

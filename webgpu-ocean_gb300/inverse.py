@@ -63,8 +63,13 @@ def _host_array(shape) -> np.ndarray:
 
 def fit_parameters(adj: MLSMPMAdjoint, init: np.ndarray, observed: dict, substeps: int,
                    start, iters: int = 50, lr: float = 0.05, betas=(0.9, 0.999),
-                   callback=None) -> dict:
-    """Adam on (log k, log mu) per scene from `start` ((S, 2) array)."""
+                   callback=None, device_loss: bool = True) -> dict:
+    """Adam on (log k, log mu) per scene from `start` ((S, 2) array).  The
+    loss, sum over observed substeps of each scene's mean squared distance to
+    the observed positions, and its seeds are computed on the device
+    (observationLoss / backwardObserved: the states stay there), or with
+    device_loss=False on the host from the read-back states (same f32
+    differences and seeds, FP64 sums)."""
     S = adj.numScenes
     offs = adj.sceneOffsets
     counts = np.diff(offs).astype(np.float64)
@@ -74,12 +79,15 @@ def fit_parameters(adj: MLSMPMAdjoint, init: np.ndarray, observed: dict, substep
     v = np.zeros_like(theta)
     steps = sorted(observed)
     n = int(offs[-1])
-    # dL/dx = 2 (x - x_obs) / (its scene's particle count); seed records are
-    # zero except their position columns, so the buffers are made once
-    scale = (2.0 / np.repeat(counts, np.diff(offs))).astype(np.float32)[:, None]
-    obs32 = {t: np.asarray(observed[t], dtype=np.float32) for t in steps}
-    seeds = {t: _host_array((n, 20)) for t in steps}
-    x = _host_array((n, 20))
+    if device_loss:
+        adj.setObservations(observed)
+    else:
+        # dL/dx = 2 (x - x_obs) / (its scene's particle count); seed records
+        # are zero except their position columns, so the buffers are made once
+        scale = (2.0 / np.repeat(counts, np.diff(offs))).astype(np.float32)[:, None]
+        obs32 = {t: np.asarray(observed[t], dtype=np.float32) for t in steps}
+        seeds = {t: _host_array((n, 20)) for t in steps}
+        x = _host_array((n, 20))
     history = []
     t0 = time.perf_counter()
     for it in range(iters):
@@ -87,14 +95,18 @@ def fit_parameters(adj: MLSMPMAdjoint, init: np.ndarray, observed: dict, substep
         for s in range(S):
             adj.setScene(s, with_constants(base[s], params[s, 0], params[s, 1]))
         adj.forward(init, substeps)
-        loss = np.zeros(S)
-        for t in steps:
-            adj.state(t, out=x)
-            diff = x[:, 0:3] - obs32[t]
-            sq = np.einsum("ij,ij->i", diff, diff, dtype=np.float64)
-            loss += np.add.reduceat(sq, offs[:-1]) / counts
-            np.multiply(diff, scale, out=seeds[t][:, 0:3])
-        _, pgrad = adj.backward(seeds)
+        if device_loss:
+            loss = adj.observationLoss()
+            _, pgrad = adj.backwardObserved(grad_init=False)
+        else:
+            loss = np.zeros(S)
+            for t in steps:
+                adj.state(t, out=x)
+                diff = x[:, 0:3] - obs32[t]
+                sq = np.einsum("ij,ij->i", diff, diff, dtype=np.float64)
+                loss += np.add.reduceat(sq, offs[:-1]) / counts
+                np.multiply(diff, scale, out=seeds[t][:, 0:3])
+            _, pgrad = adj.backward(seeds)
         g = pgrad * params  # d/d log(p) = p * d/dp
         m = betas[0] * m + (1 - betas[0]) * g
         v = betas[1] * v + (1 - betas[1]) * g * g
@@ -111,7 +123,7 @@ def fit_parameters(adj: MLSMPMAdjoint, init: np.ndarray, observed: dict, substep
 def run_inverse_problem(num_scenes: int = 64, seed: int = 0, substeps: int = 100,
                         checkpoint_every: int = 20, iters: int = 50, lr: float = 0.05,
                         tape: str = "fixed", n_range=(16000, 32000), side: int = 48,
-                        observe_every: int = 20) -> dict:
+                        observe_every: int = 20, device_loss: bool = True) -> dict:
     """The whole experiment: hidden constants, observed rollouts, recovery
     from (k, mu) = (3, 0.1); returns the relative errors against the hidden
     values."""
@@ -123,7 +135,8 @@ def run_inverse_problem(num_scenes: int = 64, seed: int = 0, substeps: int = 100
     steps = list(range(observe_every, substeps + 1, observe_every))
     observed = {t: x.astype(np.float64) for t, x in observe(adj, recs, substeps, steps).items()}
     start = np.tile(np.array([[3.0, 0.1]]), (num_scenes, 1))
-    fit = fit_parameters(adj, recs, observed, substeps, start, iters=iters, lr=lr)
+    fit = fit_parameters(adj, recs, observed, substeps, start, iters=iters, lr=lr,
+                         device_loss=device_loss)
     adj.close()
     rel = np.abs(fit["params"] - hidden) / hidden
     return {"hidden": hidden, "recovered": fit["params"], "rel_err": rel,

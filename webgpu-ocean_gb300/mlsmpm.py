@@ -643,6 +643,41 @@ class MLSMPMAdjoint:
                                            _stream_handle(commandEncoder)), "backward")
         return grad, pgrad
 
+    def setObservations(self, observed: dict) -> None:
+        """Observed positions {substep: (N, 3) array} for observationLoss; the
+        substeps must be checkpoints of the forwards that follow."""
+        steps = sorted(observed)
+        n = self.numParticles
+        blocks = [np.ascontiguousarray(observed[t], dtype=np.float32).reshape(n, 3)
+                  for t in steps]
+        fp = ctypes.POINTER(ctypes.c_float)
+        ptrs = (fp * max(len(steps), 1))(*[b.ctypes.data_as(fp) for b in blocks])
+        st = (ctypes.c_int32 * max(len(steps), 1))(*[int(t) for t in steps])
+        _check(self._lib.mpm_adjoint_set_observations(self._handle, len(steps), st, ptrs),
+               "setObservations")
+
+    def observationLoss(self, commandEncoder=None) -> np.ndarray:
+        """Per scene: the sum over observed substeps of the mean squared
+        distance of its particles to the observed positions, for the last
+        forward; leaves the seeds of backwardObserved on the device."""
+        loss = np.zeros(self.numScenes, dtype=np.float64)
+        _check(self._lib.mpm_adjoint_observation_loss(
+            self._handle, loss.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+            _stream_handle(commandEncoder)), "observationLoss")
+        return loss
+
+    def backwardObserved(self, commandEncoder=None, grad_init: bool = True):
+        """backward() with the seeds of the last observationLoss; returns
+        (dL/d initial state or None, (S, 2) dL/d(stiffness, viscosity))."""
+        fp = ctypes.POINTER(ctypes.c_float)
+        grad = np.empty((self.numParticles, 20), dtype=np.float32) if grad_init else None
+        pgrad = np.zeros((self.numScenes, 2), dtype=np.float64)
+        _check(self._lib.mpm_backward_observed(
+            self._handle, grad.ctypes.data_as(fp) if grad is not None else None,
+            pgrad.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+            _stream_handle(commandEncoder)), "backwardObserved")
+        return grad, pgrad
+
     def close(self) -> None:
         if self._handle:
             self._lib.mpm_adjoint_destroy(self._handle)
