@@ -461,7 +461,8 @@ def measure_adjoint(pkg, torch, repeats: int = 3) -> dict:
         "note": "forward_ms and plain_batched_forward_ms include uploading the initial state from host memory"}
     out["timing"] = ("host wall clock around synchronised calls, best of "
                      f"{repeats}; plain forward = upload of the same initial state + "
-                     "MLSMPMSimulator.execute(substeps=200) (CUDA graph, autotuned task size), "
+                     "MLSMPMSimulator.execute(substeps=200) (CUDA graph, autotuned task size and "
+                     "lane-table threshold), "
                      "batch: upload + MLSMPMBatch.step(100)")
     return out
 
@@ -482,7 +483,12 @@ def measure_inverse(pkg) -> dict:
             "stiffness_rel_err_max": float(rel[:, 0].max()),
             "viscosity_rel_err_median": float(np.median(rel[:, 1])),
             "viscosity_rel_err_max": float(rel[:, 1].max()),
-            "loss_first": float(h[0]["loss"].mean()), "loss_last": float(h[-1]["loss"].mean())}
+            "loss_first": float(h[0]["loss"].mean()), "loss_last": float(h[-1]["loss"].mean()),
+            "loss": "per scene, mean squared distance to the observed positions summed over the "
+                    "observed substeps; loss and seeds computed on the device "
+                    "(MLSMPMAdjoint.observationLoss / backwardObserved)",
+            "timing": "host wall clock around the 50 iterations (scene constants, forward with "
+                      "checkpoints, loss, backward, Adam step)"}
 
 
 def measure_render(pkg, torch, frames: int = 10) -> dict:
