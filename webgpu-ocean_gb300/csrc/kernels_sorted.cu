@@ -11,8 +11,9 @@
 //    its position in the bin order of the other particle buffer (an id array
 //    rides along), so the next substep reads nearly contiguous memory.
 //  * A task is one brick's particles; CTAs claim tasks from an atomic work
-//    counter and walk a task in chunks of one particle per thread.  p2g_2
-//    first reorders the brick's particles into a lane table that puts
+//    counter and walk a task in chunks of one particle per thread.  In tasks
+//    of at least Dev::lane_min particles (a runtime parameter, autotuned),
+//    p2g_2 first reorders the brick's particles into a lane table that puts
 //    particles of 32 different shared-memory bank classes in the 32 lanes of
 //    a warp (build_lane_table); g2p reuses that order.  The CTA keeps the
 //    cells the task's stencils reach (its "arena") in shared memory: the
