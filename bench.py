@@ -133,11 +133,11 @@ def cpu_threads() -> int:
         return os.cpu_count() or 1
 
 
-def time_oracle(parts, steps: int, warmup: int, budget_s: float, nthreads: int):
+def time_oracle(parts, steps: int, warmup: int, budget_s: float, nthreads: int, box=None):
     """Runs the oracle for warmup + up to `steps` execute() calls (2 substeps
     each), stopping when `budget_s` of timed work is exceeded."""
     from oracle import oracle
-    sim = oracle.OracleSim(parts, BOX)
+    sim = oracle.OracleSim(parts, BOX if box is None else box)
     for _ in range(warmup):
         sim.execute(SUBSTEPS, nthreads)
     done, t0 = 0, time.perf_counter()
@@ -148,6 +148,45 @@ def time_oracle(parts, steps: int, warmup: int, budget_s: float, nthreads: int):
             break
     dt = time.perf_counter() - t0
     return done, dt
+
+
+def cpu_model() -> str:
+    """The host CPU's name from /proc/cpuinfo (model name on x86; implementer
+    and part numbers on Arm), else the machine type."""
+    import platform
+    fields = {}
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if ":" in line:
+                    k, v = line.split(":", 1)
+                    fields.setdefault(k.strip(), v.strip())
+    except OSError:
+        pass
+    if fields.get("model name"):
+        return fields["model name"]
+    if fields.get("CPU part"):
+        return (f"{platform.machine()} CPU implementer {fields.get('CPU implementer', '?')} "
+                f"part {fields['CPU part']}")
+    return platform.machine()
+
+
+def cpu_baseline_detail(pkg, budget_s: float = 3.0) -> dict:
+    """The oracle on the 64,000-particle / 64^3 lattice (40^3 points from 3,
+    spacing 0.5) and on the 1M-particle / 128^3 workload, on one host thread
+    and on all of them, each a bounded sample from the initial state."""
+    nt = cpu_threads()
+    out = {"cpu": cpu_model(), "nproc": os.cpu_count(), "threads_all": nt,
+           "budget_s_per_case": budget_s}
+    cases = {"64k_64": (pkg.scene_lattice(40, 3.0, SPACING, JITTER, SEED), [64.0, 64.0, 64.0]),
+             "1M_128": (make_scene(pkg), BOX)}
+    for name, (parts, box) in cases.items():
+        for threads in (1, nt):
+            done, dt = time_oracle(parts, 1000, 0, budget_s, threads, box)
+            out[f"{name}_{threads}t"] = {
+                "particle_substeps_per_s": len(parts) * SUBSTEPS * done / dt,
+                "substeps": done * SUBSTEPS, "seconds": dt}
+    return out
 
 
 def dist_setup():
@@ -860,7 +899,8 @@ def run_ours(args) -> None:
         done, dt = time_oracle(parts, 1000, 0, 10.0, nt)
         cpu = {"value": n * SUBSTEPS * done / dt, "unit": UNIT, "cores": nt, "kind": "port",
                "sample": f"{done} steps of the same 1M-particle workload from its initial "
-                         f"state ({done * SUBSTEPS} substeps, {dt:.1f} s) on {nt} host threads"}
+                         f"state ({done * SUBSTEPS} substeps, {dt:.1f} s) on {nt} host threads",
+               "detail": cpu_baseline_detail(pkg)}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
