@@ -39,6 +39,14 @@ def test_null_handles_are_rejected(pkg):
     assert lib.mpm_backward(None, None, None, 0, None, None, None) == E
     assert lib.mpm_backward_list(None, None, None, 0, None, None, None) == E
     assert lib.mpm_sph_set_graph(None, 1) == E
+    assert lib.mpm_set_lane_table_min(None, 128) == E
+    assert lib.mpm_get_lane_table_min(None) == E
+    assert lib.mpm_batch_set_lane_table_min(None, 128) == E
+    assert lib.mpm_batch_get_lane_table_min(None) == E
+    assert lib.mpm_batch_get_task_size(None) == E
+    assert lib.mpm_adjoint_set_observations(None, 0, None, None) == E
+    assert lib.mpm_adjoint_observation_loss(None, None, None) == E
+    assert lib.mpm_backward_observed(None, None, None, None) == E
 
 
 def test_default_params_are_the_reference_constants(pkg):

@@ -722,19 +722,25 @@ int mpm_adjoint_set_observations(mpm_adjoint* a, int count, const int* substeps,
     free_observations(a);
     const size_t np = (size_t)(n > 0 ? n : 1);
     std::vector<float4> h(np);
-    for (int i = 0; i < count; ++i) {
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < count && e == cudaSuccess; ++i) {
         float4* d = nullptr;
-        MPM_CUDA(cudaMalloc(&d, sizeof(float4) * np));
+        e = cudaMalloc(&d, sizeof(float4) * np);
+        if (e != cudaSuccess) break;
         a->obs.push_back(d);
         a->obs_steps.push_back(substeps[i]);
         for (int j = 0; j < n; ++j)
             h[(size_t)j] = make_float4(obs_xyz[i][3 * (size_t)j], obs_xyz[i][3 * (size_t)j + 1],
                                        obs_xyz[i][3 * (size_t)j + 2], 0.0f);
-        MPM_CUDA(cudaMemcpy(d, h.data(), sizeof(float4) * (size_t)n, cudaMemcpyHostToDevice));
+        e = cudaMemcpy(d, h.data(), sizeof(float4) * (size_t)n, cudaMemcpyHostToDevice);
     }
     const int S = (int)a->b->consts.size();
-    if (!a->obs_scale) MPM_CUDA(cudaMalloc(&a->obs_scale, sizeof(float) * (size_t)S));
-    if (!a->obs_loss) MPM_CUDA(cudaMalloc(&a->obs_loss, sizeof(double) * (size_t)S));
+    if (e == cudaSuccess && !a->obs_scale) e = cudaMalloc(&a->obs_scale, sizeof(float) * (size_t)S);
+    if (e == cudaSuccess && !a->obs_loss) e = cudaMalloc(&a->obs_loss, sizeof(double) * (size_t)S);
+    if (e != cudaSuccess) {  // no partial set of observations
+        free_observations(a);
+        return cuda_fail(e, "mpm_adjoint_set_observations");
+    }
     std::vector<float> scale((size_t)S);
     for (int s = 0; s < S; ++s) {
         const int ns = a->b->desc[(size_t)s].num_particles;
