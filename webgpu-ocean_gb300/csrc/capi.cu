@@ -495,7 +495,7 @@ int mpm_autotune(mpm_sim* s, int substeps, int* chosen_task_size) {
         return sorted_step(s->sorted, &s->ps, s->posvel, s->counters, k, ns, s->internal, &s->prof,
                            s->graph);
     };
-    const int rc = tune_task_cap(s->sorted, s->ps, s->n, s->posvel, s->counters, substeps,
+    const int rc = tune_engine(s->sorted, s->ps, s->n, s->posvel, s->counters, substeps,
                                  s->internal, step, chosen_task_size, nullptr, nullptr);
     s->ref_current = true;  // the grid from before the call
     return rc;

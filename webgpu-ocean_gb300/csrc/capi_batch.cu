@@ -218,7 +218,7 @@ int mpm_batch_autotune(mpm_batch* b, int substeps, int* chosen_task_size) {
         return sorted_step(b->sorted, &b->ps, b->posvel, b->counters, b->consts[0], ns, nullptr,
                            &b->prof, b->graph);
     };
-    const int rc = tune_task_cap(b->sorted, b->ps, b->n, b->posvel, b->counters, substeps, nullptr,
+    const int rc = tune_engine(b->sorted, b->ps, b->n, b->posvel, b->counters, substeps, nullptr,
                                  step, chosen_task_size, nullptr, nullptr);
     b->stepped = false;
     return rc;

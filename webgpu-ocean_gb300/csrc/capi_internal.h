@@ -70,7 +70,7 @@ int scene_consts(const mpm_scene_desc& d, SimConsts& k);
 // run replays are captured outside it.  The state after the call is the
 // state before it (particles, posvel, counters, grid).
 template <class StepFn>
-int tune_task_cap(SortedEngine* e, ParticleStore& ps, int n, float4* posvel,
+int tune_engine(SortedEngine* e, ParticleStore& ps, int n, float4* posvel,
                   unsigned long long* counters, int substeps, cudaStream_t st, StepFn step,
                   int* chosen, int* chosen_lane, double* ms_out) {
     static const int kCaps[] = {64, 128, 256, 512, 1024};
