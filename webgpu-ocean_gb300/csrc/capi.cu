@@ -496,7 +496,7 @@ int mpm_autotune(mpm_sim* s, int substeps, int* chosen_task_size) {
                            s->graph);
     };
     const int rc = tune_engine(s->sorted, s->ps, s->n, s->posvel, s->counters, substeps,
-                                 s->internal, step, chosen_task_size, nullptr, nullptr);
+                               s->internal, step, chosen_task_size, nullptr, nullptr);
     s->ref_current = true;  // the grid from before the call
     return rc;
 }

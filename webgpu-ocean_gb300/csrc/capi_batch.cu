@@ -219,7 +219,7 @@ int mpm_batch_autotune(mpm_batch* b, int substeps, int* chosen_task_size) {
                            &b->prof, b->graph);
     };
     const int rc = tune_engine(b->sorted, b->ps, b->n, b->posvel, b->counters, substeps, nullptr,
-                                 step, chosen_task_size, nullptr, nullptr);
+                               step, chosen_task_size, nullptr, nullptr);
     b->stepped = false;
     return rc;
 }

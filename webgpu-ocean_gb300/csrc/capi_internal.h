@@ -71,8 +71,8 @@ int scene_consts(const mpm_scene_desc& d, SimConsts& k);
 // state before it (particles, posvel, counters, grid).
 template <class StepFn>
 int tune_engine(SortedEngine* e, ParticleStore& ps, int n, float4* posvel,
-                  unsigned long long* counters, int substeps, cudaStream_t st, StepFn step,
-                  int* chosen, int* chosen_lane, double* ms_out) {
+                unsigned long long* counters, int substeps, cudaStream_t st, StepFn step,
+                int* chosen, int* chosen_lane, double* ms_out) {
     static const int kCaps[] = {64, 128, 256, 512, 1024};
     static const int kLanes[] = {32, 128, 512, 1 << 30};  // 1 << 30: no lane table
     Particles save{};
