@@ -110,16 +110,52 @@ def cases():
         q[:, 8 + 4 * c: 11 + 4 * c] = rng.uniform(-0.2, 0.2, (80, 3))
     out["fractional_box"] = dict(parts=q, init_box=[15.5, 14.25, 16.75],
                                  real_box=[15.5, 14.25, 16.75], substeps=2, per_kernel=False)
+    out["wall_impact"] = dict(parts=wall_impact_particles(), init_box=[16.0, 16.0, 16.0],
+                              real_box=[16.0, 16.0, 16.0], substeps=3, per_kernel=True)
     return out
+
+
+def wall_impact_particles() -> np.ndarray:
+    """8 particles 0.6-2.5 cells from each of the six walls moving at it at
+    2-6 cells per unit time (g2p's position clamp on both sides and wall
+    push, updateGrid's boundary band; stencils that start outside the box
+    alias (y, z) or fall out of range (x)), and a 4 x 4 x 3 cluster at
+    spacing 0.3 (gathered density 4.3-6.5, above rest: positive pressure)
+    with small random v and C."""
+    rng = np.random.default_rng(20240611)
+    p = np.zeros((96, 20), dtype=np.float32)
+    i = 0
+    for axis in range(3):
+        for side in (0, 1):
+            for _ in range(8):
+                x = rng.uniform(4.0, 12.0, 3)
+                gap = rng.uniform(0.6, 2.5)
+                x[axis] = gap if side == 0 else 16.0 - gap
+                v = rng.uniform(-0.5, 0.5, 3)
+                v[axis] = -rng.uniform(2.0, 6.0) if side == 0 else rng.uniform(2.0, 6.0)
+                p[i, 0:3], p[i, 4:7] = x, v
+                i += 1
+    for a in range(4):
+        for b in range(4):
+            for c in range(3):
+                p[i, 0:3] = [7.0 + 0.3 * a, 7.0 + 0.3 * b, 7.2 + 0.3 * c]
+                p[i, 4:7] = rng.uniform(-0.2, 0.2, 3)
+                for col in range(3):
+                    p[i, 8 + 4 * col: 11 + 4 * col] = rng.uniform(-0.1, 0.1, 3)
+                i += 1
+    return p
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--only", nargs="*", help="fixture names to (re)generate (default: all)")
     args = ap.parse_args()
     src_dir = os.path.join(args.reference, "mls-mpm")
     np.seterr(all="ignore")
     for name, c in cases().items():
+        if args.only and name not in args.only:
+            continue
         modules = {k: W.Module(open(os.path.join(src_dir, f"{k}.wgsl")).read(), OVERRIDES)
                    for k in KERNELS}
         res, oob = run_case(modules, c["parts"], c["init_box"], c["real_box"], c["substeps"],

@@ -464,6 +464,7 @@ class Module:
         self.funcs = {}
         self.consts = {}
         self.oob = 0
+        self._oob_last = None  # (array, index) of the access just before, if out of range
         for d in self.decls:
             if d[0] == "struct":
                 self.structs[d[1]] = T("struct", fields=[(f, self.resolve(ty)) for f, ty in d[2]],
@@ -499,6 +500,15 @@ class Module:
         raise TypeError(f"unknown type {ty}")
 
     # ---- entry point ------------------------------------------------------
+    def count_oob(self, arr, i):
+        """Counts out-of-range element accesses once per visit: consecutive
+        accesses of one invocation to the same element (a stencil cell's
+        four atomics or three field reads) are one, as in the C oracle."""
+        key = (id(arr), i)
+        if key != self._oob_last:
+            self.oob += 1
+            self._oob_last = key
+
     def entry(self, name):
         d = self.funcs[name]
         fn = self.compile_fn(d)
@@ -656,17 +666,19 @@ class Module:
                     arr = bget(env)
                     i = int(iv(env))
                     if 0 <= i < len(arr):
+                        self._oob_last = None
                         return arr[i]
-                    self.oob += 1
+                    self.count_oob(arr, i)
                     return zero_value(et)
 
                 def setv(env, v):
                     arr = bget(env)
                     i = int(iv(env))
                     if 0 <= i < len(arr):
+                        self._oob_last = None
                         arr[i] = v
                     else:
-                        self.oob += 1
+                        self.count_oob(arr, i)
                 return get, setv, et
             if bt.kind in ("vec", "mat"):
                 et = bt.elem if bt.kind == "vec" else vec(bt.elem, bt.n)
@@ -1063,4 +1075,5 @@ def dispatch(module: Module, entry: str, buffers: dict, invocations: int, workgr
     run, _, params = module.entry(entry)
     total = -(-invocations // workgroup) * workgroup
     for i in range(total):
+        module._oob_last = None
         run(buffers, (i, 0, 0))

@@ -12,7 +12,7 @@ import pytest
 from helpers import assert_bits_equal
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["dambreak", "random_vc", "shrunk_box", "fractional_box"]
+CASES = ["dambreak", "random_vc", "shrunk_box", "fractional_box", "wall_impact"]
 KERNELS = ["clearGrid", "p2g_1", "p2g_2", "updateGrid", "g2p", "copyPosition"]
 
 
@@ -40,13 +40,18 @@ def test_oracle_reproduces_wgsl_golden(oracle_mod, name):
 
 def test_golden_fixtures_cover_the_paths():
     """The fixtures exercise aliasing (dambreak starts at y = 0), a shrunk real
-    box, a non-integer box and non-zero initial v and C."""
+    box, a non-integer box, non-zero initial v and C, and particles hitting
+    the walls (g2p's clamp on both sides, stencils out of range)."""
     d = load("dambreak")
     assert (np.floor(d["particles"][:, 1]) == 0).any()
     assert load("shrunk_box")["real_box"][2] < load("shrunk_box")["init_box"][2]
     fb = load("fractional_box")["init_box"]
     assert (fb != np.floor(fb)).all()
     assert np.abs(load("random_vc")["particles"][:, 8:19]).max() > 0
+    w = load("wall_impact")
+    x0 = w["s0_particles"][:, 0:3]
+    assert (x0 == 1.0).any() and (x0 == w["real_box"][0] - 2.0).any()  # g2p.wgsl clamp
+    assert int(w["oob"]) > 0
 
 
 @pytest.mark.gpu
