@@ -336,6 +336,10 @@ class Parser:
             self.expect(")")
             body = self.block()
             return ("for", init, cond, upd, body)
+        if t[1] in ("continue", "break"):
+            self.next()
+            self.expect(";")
+            return (t[1],)
         if t[1] == "return":
             self.next()
             e = None
@@ -450,6 +454,14 @@ class Parser:
 class ReturnSignal(Exception):
     def __init__(self, value):
         self.value = value
+
+
+class ContinueSignal(Exception):
+    pass
+
+
+class BreakSignal(Exception):
+    pass
 
 
 SWZ = {"x": 0, "y": 1, "z": 2, "w": 3, "r": 0, "g": 1, "b": 2, "a": 3}
@@ -607,8 +619,21 @@ class Module:
             def run(env):
                 init(env)
                 while cond(env):
-                    body(env)
+                    try:
+                        body(env)
+                    except ContinueSignal:
+                        pass
+                    except BreakSignal:
+                        break
                     upd(env)
+            return run
+        if k == "continue":
+            def run(env):
+                raise ContinueSignal()
+            return run
+        if k == "break":
+            def run(env):
+                raise BreakSignal()
             return run
         if k == "return":
             if s[1] is None:
@@ -844,10 +869,44 @@ class Module:
             return self.construct(self.resolve(callee), args, scope)
         name = callee
         ctor = {"vec3f": vec(TF32), "vec2f": vec(TF32, 2), "vec4f": vec(TF32, 4),
+                "vec3i": vec(TI32), "vec3u": vec(TU32),
                 "mat3x3f": mat(TF32), "f32": TF32, "i32": TI32, "u32": TU32}
         if name in ctor:
             return self.construct(ctor[name], args, scope)
         evs = [self.compile_expr(a, scope) for a in args]
+        if name == "vec3":
+            # element type inferred from the components; an abstract float
+            # vector concretises to vec3f, an abstract int one to vec3i
+            kinds = {scalar_of(t).kind for _, t in evs}
+            if kinds & {"f32", "absfloat"}:
+                return self.construct(vec(TF32), args, scope)
+            if "u32" in kinds:
+                return self.construct(vec(TU32), args, scope)
+            return self.construct(vec(TI32), args, scope)
+        if name == "sqrt":
+            (v, t), = evs
+            if t.kind == "vec":
+                return (lambda env: tuple(F32(np.sqrt(F32(x))) for x in v(env))), t
+            if is_abstract(t):
+                return (lambda env: float(np.sqrt(v(env)))), t
+            return (lambda env: F32(np.sqrt(F32(v(env))))), t
+        if name == "dot":
+            # ((x0*y0 + x1*y1) + x2*y2), every product and sum rounded to f32
+            (a, at), (b, bt) = evs
+
+            def run(env):
+                return _dot(a(env), b(env))
+            return run, at.elem
+        if name == "normalize":
+            # v / sqrt(dot(v, v)) component by component (WGSL leaves the
+            # precision to the implementation; the C oracle does the same)
+            (v, t), = evs
+
+            def run(env):
+                x = v(env)
+                n = F32(np.sqrt(_dot(x, x)))
+                return tuple(F32(F32(c) / n) for c in x)
+            return run, t
         if name == "atomicAdd":
             (pv, pt), (vv, vt) = evs
             target = pt.elem if pt.kind == "ptr" else pt
@@ -932,6 +991,13 @@ class Module:
 
 
 CMP = ("<", ">", "<=", ">=", "==", "!=")
+
+
+def _dot(x, y):
+    acc = F32(F32(x[0]) * F32(y[0]))
+    for i in range(1, len(x)):
+        acc = F32(acc + F32(F32(x[i]) * F32(y[i])))
+    return acc
 
 
 def _copy(v):
