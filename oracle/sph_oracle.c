@@ -7,13 +7,17 @@
  * TEST INFRASTRUCTURE ONLY: loaded by tests/ as the checker of the CUDA SPH
  * solver, never by the product.
  *
- * Parity unpinned against the reference itself (WGSL needs a WebGPU
- * runtime; unavailable on this machine).  The restatement follows the shaders
- * operation for operation in f32 (build with -ffp-contract=off), with the
- * choices the library documents: neighbours within a cell in ascending
- * particle index (the reference's in-cell order comes from atomic arrival),
- * particles whose flat cell id is outside [0, gridCount) left out of the
- * grid, exactly n particles (no ghost threads).
+ * Pinned to the reference's own shaders: tests/golden/make_golden_sph.py
+ * runs sph/grid/*.wgsl and sph/{density,force,integrate,copyPosition}.wgsl
+ * (read as text) through the WGSL interpreter in the dispatch order of
+ * SPHSimulator.execute, and this restatement reproduces those fixtures bit
+ * for bit.  It follows the shaders operation for operation in f32 (build with
+ * -ffp-contract=off), with the choices the library documents: neighbours
+ * within a cell in ascending particle index (the reference's in-cell order
+ * comes from atomic arrival; the fixtures take the legal schedule that gives
+ * it), particles whose flat cell id is outside [0, gridCount) left out of the
+ * grid, exactly n particles (no ghost threads), dot = (x*x + y*y) + z*z and
+ * normalize(u) = u / sqrt(dot(u, u)).
  *
  * Particle records: 16 floats (64 bytes, sph.ts:13,205-211): position
  * [0..2], v [4..6], force [8..10], density [11], nearDensity [12].
