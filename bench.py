@@ -295,14 +295,15 @@ BATCH_WORKLOAD = ("256 independent scenes, particles uniform in [4000, 64000], c
                   "x0.3, stiffness uniform [2, 4]; 100 substeps per rollout")
 
 
-def measure_batched(pkg, torch, stream, repeats: int = 3) -> dict:
+def measure_batched(pkg, torch, stream, repeats: int = 3, autotune: bool = True) -> dict:
     """Scene-substeps/s of one batch (one launch per stage for all scenes,
     CUDA graph) against looping single-scene simulators over the same scenes."""
     import numpy as np
     descs, recs = pkg.batch_scenes(BATCH_SCENES, seed=BATCH_SEED)
     S, K = len(descs), BATCH_SUBSTEPS
     batch = pkg.MLSMPMBatch(descs, recs, graph=True)
-    tuned = {"task_size": batch.autotune(4), "lane_table_min": batch.laneTableMin}
+    tuned = {"task_size": batch.autotune(4) if autotune else batch.taskSize,
+             "lane_table_min": batch.laneTableMin}
     batch.step(K, stream)  # captures the graph and warms up
     stream.synchronize()
     l0 = batch.launchCount()
@@ -642,13 +643,13 @@ def measure_adjoint_batch(pkg, torch, substeps: int = 40, every: int = 10) -> di
             "grad_finite": bool(np.isfinite(g).all())}
 
 
-def run_only(which: str) -> None:
+def run_only(which: str, autotune: bool = True) -> None:
     import torch
     import __graft_entry__ as entry
     entry.build()
     pkg = entry.load_package()
     if which == "batched":
-        out = measure_batched(pkg, torch, torch.cuda.Stream())
+        out = measure_batched(pkg, torch, torch.cuda.Stream(), autotune=autotune)
     elif which == "adjoint":
         out = measure_adjoint(pkg, torch)
     elif which == "render":
@@ -703,12 +704,16 @@ def run_ours(args) -> None:
     # task size and lane-table threshold tuned on the state the timed steps
     # start from (the autotuner restores it), then the same start again so
     # the graphs of the chosen configuration are captured before timing
-    tuned = {"task_size": sim.autotune(AUTOTUNE_SUBSTEPS), "lane_table_min": sim.laneTableMin,
-             "autotune": f"{AUTOTUNE_SUBSTEPS} substeps after the warm-up steps"}
-    sim.upload(parts, BOX)
-    for _ in range(args.warmup):
-        sim.execute(stream)
-    stream.synchronize()
+    if args.no_autotune:
+        tuned = {"task_size": sim.taskSize, "lane_table_min": sim.laneTableMin,
+                 "autotune": "off (engine defaults)"}
+    else:
+        tuned = {"task_size": sim.autotune(AUTOTUNE_SUBSTEPS), "lane_table_min": sim.laneTableMin,
+                 "autotune": f"{AUTOTUNE_SUBSTEPS} substeps after the warm-up steps"}
+        sim.upload(parts, BOX)
+        for _ in range(args.warmup):
+            sim.execute(stream)
+        stream.synchronize()
 
     # --- timed region: device-resident throughput ----------------------
     K = args.steps
@@ -868,7 +873,8 @@ def run_ours(args) -> None:
     assert np.isfinite(hosts[(K - 1) % 2][:, 0:3]).all(), "posvel read back non-finite positions"
     sim.close()
 
-    batched = None if args.skip_batched else measure_batched(pkg, torch, stream)
+    batched = None if args.skip_batched else measure_batched(pkg, torch, stream,
+                                                             autotune=not args.no_autotune)
     adjoint = None if args.skip_adjoint else measure_adjoint(pkg, torch)
     inverse = None if args.skip_adjoint else measure_inverse(pkg)
     render = None if args.skip_batched else measure_render(pkg, torch)
@@ -959,13 +965,16 @@ def main():
                     help="run one side measurement alone and print its JSON (profiling)")
     ap.add_argument("--quick", action="store_true",
                     help="time the device-resident steps only (for profiler captures)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the engine's default task size and lane-table threshold (the "
+                         "configuration of the committed ncu captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
     elif args.only:
-        run_only(args.only)
+        run_only(args.only, autotune=not args.no_autotune)
     else:
         run_ours(args)
 
