@@ -260,6 +260,13 @@ def _render_lib():
             getattr(L, name).restype = ctypes.c_float
         L.ro_pow.argtypes = [ctypes.c_float, ctypes.c_float]
         L.ro_pow.restype = ctypes.c_float
+        L.ro_bilateral_pass.argtypes = [f32p, f32p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                        ctypes.c_float]
+        L.ro_bilateral_pass.restype = None
+        L.ro_gaussian_pass.argtypes = [f32p, f32p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int]
+        L.ro_gaussian_pass.restype = None
         L._ro_ready = True
     return L
 
@@ -286,6 +293,33 @@ def render(posvel: np.ndarray, uniforms_f32: np.ndarray, width: int, height: int
 
 def render_scalar(name: str, *args) -> float:
     return float(getattr(_render_lib(), "ro_" + name)(*args))
+
+
+def filter_constants(height: int, radius: float, fov: float):
+    """(depth_threshold, max_filter_size, projected_particle_constant) of the
+    filter passes for a screen height, particle radius and field of view."""
+    L = _render_lib()
+    dt, mf, ppc = ctypes.c_float(), ctypes.c_float(), ctypes.c_float()
+    L.ro_filter_constants(height, radius, fov, ctypes.byref(dt), ctypes.byref(mf), ctypes.byref(ppc))
+    return dt.value, mf.value, ppc.value
+
+
+def render_filter_pass(kind: str, img: np.ndarray, direction, depth_threshold: float = 0.0,
+                       max_filter_size: float = 0.0, ppc: float = 0.0) -> np.ndarray:
+    """One pass of the renderer's bilateral depth filter or gaussian thickness
+    filter over an (H, W) float32 image along direction (1, 0) or (0, 1)."""
+    L = _render_lib()
+    src = np.ascontiguousarray(img, dtype=np.float32)
+    h, w = src.shape
+    dst = np.zeros_like(src)
+    dx, dy = (int(direction[0]), int(direction[1]))
+    if kind == "bilateral":
+        L.ro_bilateral_pass(src, dst, w, h, dx, dy, depth_threshold, max_filter_size, ppc)
+    elif kind == "gaussian":
+        L.ro_gaussian_pass(src, dst, w, h, dx, dy)
+    else:
+        raise ValueError(kind)
+    return dst
 
 
 # ---------------------------------------------------------------------------

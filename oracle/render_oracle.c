@@ -265,6 +265,68 @@ static v3 sample_cube(const float* env, int size, v3 d) {
  * floats, after filtering).  env: 6 x size x size x 4 floats.  Filter
  * constants as fluidRender.ts:38-46.  Returns 0, or -1 on allocation failure.
  */
+/* One pass of bilateral.wgsl:18-75 over a W x H depth image along (dx, dy):
+ * texel coordinates outside the image are clamped to its edge (WGSL lets an
+ * out-of-bounds textureLoad return any texel within bounds). */
+static void bilateral_pass(const float* src, float* dst, int W, int H, int dx, int dy,
+                           float depth_threshold, float max_filter_size, float ppc) {
+    for (int py = 0; py < H; ++py)
+        for (int px = 0; px < W; ++px) {
+            const size_t p = (size_t)py * W + px;
+            const float depth = fabsf(src[p]);
+            if (depth >= 1e4f || depth <= 0.0f) {
+                dst[p] = depth;
+                continue;
+            }
+            const int a = f2i_sat(max_filter_size), c = f2i_sat(ceilf(ppc / depth));
+            const int fs = a < c ? a : c;
+            const float sigma = (float)fs / 3.0f;
+            const float two_sigma = (2.0f * sigma) * sigma;
+            const float sd = depth_threshold / 3.0f;
+            const float two_sd = (2.0f * sd) * sd;
+            float sum = 0.0f, wsum = 0.0f;
+            for (int x = -fs; x <= fs; ++x) {
+                const float xf = (float)x;
+                const int ix = clampi(px + x * dx, 0, W - 1), iy = clampi(py + x * dy, 0, H - 1);
+                const float sampled = fabsf(src[(size_t)iy * W + ix]);
+                const float rr = xf * xf + xf * xf;
+                const float w = exp_r(-rr / two_sigma);
+                const float rd = sampled - depth;
+                const float wd = exp_r((-rd * rd) / two_sd);
+                sum = sum + (sampled * w) * wd;
+                wsum = wsum + w * wd;
+            }
+            dst[p] = sum / wsum;
+        }
+}
+
+/* One pass of gaussian.wgsl:14-42 over a W x H thickness image along
+ * (dx, dy), the result stored into the r16float target (rounded to half). */
+static void gaussian_pass(const float* src, float* dst, int W, int H, int dx, int dy) {
+    for (int py = 0; py < H; ++py)
+        for (int px = 0; px < W; ++px) {
+            const size_t p = (size_t)py * W + px;
+            const float t = src[p];
+            if (t == 0.0f) {
+                dst[p] = 0.0f;
+                continue;
+            }
+            const int fs = 30;
+            const float sigma = (float)fs / 3.0f;
+            const float two_sigma = (2.0f * sigma) * sigma;
+            float sum = 0.0f, wsum = 0.0f;
+            for (int x = -fs; x <= fs; ++x) {
+                const float xf = (float)x;
+                const int ix = clampi(px + x * dx, 0, W - 1), iy = clampi(py + x * dy, 0, H - 1);
+                const float sampled = src[(size_t)iy * W + ix];
+                const float w = exp_r((-xf * xf) / two_sigma);
+                sum = sum + sampled * w;
+                wsum = wsum + w;
+            }
+            dst[p] = half_round(sum / wsum);
+        }
+}
+
 int ro_render(const float* posvel, int64_t n, const ro_uniforms* u, int W, int H,
               float depth_threshold, float max_filter_size, float ppc, const float* env,
               int env_size, float* color, uint8_t* color8, float* depth_out, float* thick_out) {
@@ -312,67 +374,12 @@ int ro_render(const float* posvel, int64_t n, const ro_uniforms* u, int W, int H
         t0[p] = half_round((float)tacc[p] * 2.3283064365386963e-10f);
     }
     /* bilateral depth filter, 4 x (X, Y) */
-    for (int it = 0; it < 8; ++it) {
-        const float* src = (it & 1) ? d1 : d0;
-        float* dst = (it & 1) ? d0 : d1;
-        const int dx = (it & 1) ? 0 : 1, dy = (it & 1) ? 1 : 0;
-        for (int py = 0; py < H; ++py)
-            for (int px = 0; px < W; ++px) {
-                const size_t p = (size_t)py * W + px;
-                const float depth = fabsf(src[p]);
-                if (depth >= 1e4f || depth <= 0.0f) {
-                    dst[p] = depth;
-                    continue;
-                }
-                const int a = f2i_sat(max_filter_size), c = f2i_sat(ceilf(ppc / depth));
-                const int fs = a < c ? a : c;
-                const float sigma = (float)fs / 3.0f;
-                const float two_sigma = (2.0f * sigma) * sigma;
-                const float sd = depth_threshold / 3.0f;
-                const float two_sd = (2.0f * sd) * sd;
-                float sum = 0.0f, wsum = 0.0f;
-                for (int x = -fs; x <= fs; ++x) {
-                    const float xf = (float)x;
-                    const int ix = clampi(px + x * dx, 0, W - 1), iy = clampi(py + x * dy, 0, H - 1);
-                    const float sampled = fabsf(src[(size_t)iy * W + ix]);
-                    const float rr = xf * xf + xf * xf;
-                    const float w = exp_r(-rr / two_sigma);
-                    const float rd = sampled - depth;
-                    const float wd = exp_r((-rd * rd) / two_sd);
-                    sum = sum + (sampled * w) * wd;
-                    wsum = wsum + w * wd;
-                }
-                dst[p] = sum / wsum;
-            }
-    }
+    for (int it = 0; it < 8; ++it)
+        bilateral_pass((it & 1) ? d1 : d0, (it & 1) ? d0 : d1, W, H, (it & 1) ? 0 : 1,
+                       (it & 1) ? 1 : 0, depth_threshold, max_filter_size, ppc);
     /* gaussian thickness filter, X then Y */
-    for (int it = 0; it < 2; ++it) {
-        const float* src = it ? t1 : t0;
-        float* dst = it ? t0 : t1;
-        const int dx = it ? 0 : 1, dy = it ? 1 : 0;
-        for (int py = 0; py < H; ++py)
-            for (int px = 0; px < W; ++px) {
-                const size_t p = (size_t)py * W + px;
-                const float t = src[p];
-                if (t == 0.0f) {
-                    dst[p] = 0.0f;
-                    continue;
-                }
-                const int fs = 30;
-                const float sigma = (float)fs / 3.0f;
-                const float two_sigma = (2.0f * sigma) * sigma;
-                float sum = 0.0f, wsum = 0.0f;
-                for (int x = -fs; x <= fs; ++x) {
-                    const float xf = (float)x;
-                    const int ix = clampi(px + x * dx, 0, W - 1), iy = clampi(py + x * dy, 0, H - 1);
-                    const float sampled = src[(size_t)iy * W + ix];
-                    const float w = exp_r((-xf * xf) / two_sigma);
-                    sum = sum + sampled * w;
-                    wsum = wsum + w;
-                }
-                dst[p] = half_round(sum / wsum);
-            }
-    }
+    for (int it = 0; it < 2; ++it)
+        gaussian_pass(it ? t1 : t0, it ? t0 : t1, W, H, it ? 0 : 1, it ? 1 : 0);
     /* shading */
     for (int py = 0; py < H; ++py)
         for (int px = 0; px < W; ++px) {
@@ -445,6 +452,15 @@ void ro_filter_constants(int H, double radius, double fov, float* depth_threshol
 }
 
 /* The scalar helpers, for tests of the restatement itself. */
+/* One filter pass alone (the golden tests run it against the reference's
+ * own fragment shaders). */
+void ro_bilateral_pass(const float* src, float* dst, int W, int H, int dx, int dy,
+                       float depth_threshold, float max_filter_size, float ppc) {
+    bilateral_pass(src, dst, W, H, dx, dy, depth_threshold, max_filter_size, ppc);
+}
+void ro_gaussian_pass(const float* src, float* dst, int W, int H, int dx, int dy) {
+    gaussian_pass(src, dst, W, H, dx, dy);
+}
 float ro_exp(float x) { return exp_r(x); }
 float ro_log(float x) { return log_r(x); }
 float ro_pow(float x, float y) { return pow_r(x, y); }

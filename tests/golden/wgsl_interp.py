@@ -204,12 +204,13 @@ class Parser:
             e = self.parse_type()
             self.expect(">")
             return ("vec", int(name[3]), e)
-        if name in ("vec2f", "vec3f", "vec4f"):
-            return ("vec", int(name[3]), ("f32",))
-        if name in ("vec3i",):
-            return ("vec", 3, ("i32",))
-        if name in ("vec3u",):
-            return ("vec", 3, ("u32",))
+        if len(name) == 5 and name[:3] == "vec" and name[3] in "234" and name[4] in "fiu":
+            return ("vec", int(name[3]), ({"f": "f32", "i": "i32", "u": "u32"}[name[4]],))
+        if name == "texture_2d":
+            self.expect("<")
+            e = self.parse_type()
+            self.expect(">")
+            return ("texture", e)
         if name == "mat3x3f":
             return ("mat", 3, ("f32",))
         if name == "mat3x3":
@@ -294,6 +295,7 @@ class Parser:
                     self.accept(",")
                 ret = None
                 if self.accept("->"):
+                    self.attributes()  # @location / @builtin of an entry point's result
                     ret = self.parse_type()
                 body = self.block()
                 decls.append(("fn", name, params, ret, body, attrs))
@@ -466,6 +468,9 @@ class BreakSignal(Exception):
 
 SWZ = {"x": 0, "y": 1, "z": 2, "w": 3, "r": 0, "g": 1, "b": 2, "a": 3}
 
+# exp(x) for f32 x; a fixture generator installs the project's restatement
+EXP_F32 = lambda x: np.exp(np.float32(x))  # noqa: E731
+
 
 class Module:
     def __init__(self, src: str, overrides: dict):
@@ -507,6 +512,8 @@ class Module:
             return T("atomic", self.resolve(ty[1]))
         if k == "array":
             return T("array", self.resolve(ty[1]), ty[2] or 0)
+        if k == "texture":
+            return T("texture", self.resolve(ty[1]))
         if k in self.structs:
             return self.structs[k]
         raise TypeError(f"unknown type {ty}")
@@ -869,7 +876,8 @@ class Module:
             return self.construct(self.resolve(callee), args, scope)
         name = callee
         ctor = {"vec3f": vec(TF32), "vec2f": vec(TF32, 2), "vec4f": vec(TF32, 4),
-                "vec3i": vec(TI32), "vec3u": vec(TU32),
+                "vec3i": vec(TI32), "vec3u": vec(TU32), "vec2i": vec(TI32, 2),
+                "vec2u": vec(TU32, 2), "vec4i": vec(TI32, 4), "vec4u": vec(TU32, 4),
                 "mat3x3f": mat(TF32), "f32": TF32, "i32": TI32, "u32": TU32}
         if name in ctor:
             return self.construct(ctor[name], args, scope)
@@ -883,6 +891,33 @@ class Module:
             if "u32" in kinds:
                 return self.construct(vec(TU32), args, scope)
             return self.construct(vec(TI32), args, scope)
+        if name == "abs":
+            (v, t), = evs
+            if t.kind == "vec":
+                return (lambda env: tuple(_cast(abs(x), t.elem) for x in v(env))), t
+            if is_abstract(t):
+                return (lambda env: abs(v(env))), t
+            return (lambda env: _cast(abs(v(env)), t)), t
+        if name == "exp":
+            # WGSL leaves exp's precision to the implementation: the project's
+            # restatement is used wherever it is installed (EXP_F32)
+            (v, t), = evs
+            v = self.coerce(v, t, TF32)
+            return (lambda env: F32(EXP_F32(F32(v(env))))), TF32
+        if name == "textureLoad":
+            # a single-channel texture as an (H, W) float32 array; a texel
+            # outside it reads the nearest edge texel (WGSL lets an
+            # out-of-bounds load return any texel within bounds)
+            (tv, tt), (cv, ct), _level = evs
+
+            def run(env):
+                img = tv(env)
+                x, y = (int(c) for c in cv(env))
+                h, w = img.shape
+                x = min(max(x, 0), w - 1)
+                y = min(max(y, 0), h - 1)
+                return (F32(img[y, x]), F32(0.0), F32(0.0), F32(1.0))
+            return run, vec(TF32, 4)
         if name == "sqrt":
             (v, t), = evs
             if t.kind == "vec":
@@ -977,6 +1012,34 @@ class Module:
                 v, vt = evs[0]
                 v = self.coerce(v, vt, st)
                 return (lambda env: tuple(_cast(v(env), st) for _ in range(t.n))), t
+            if any(vt.kind == "vec" for _, vt in evs):
+                # vector components are spread; a single vector of another
+                # element type is converted component by component
+                parts = []
+                for v, vt in evs:
+                    if vt.kind == "vec":
+                        parts.append((v, vt.n, vt.elem))
+                    else:
+                        parts.append((self.coerce(v, vt, st), 0, st))
+
+                def conv(x, src):
+                    if st.kind == src.kind:
+                        return _cast(x, st)
+                    if st.kind == "u32":
+                        return f2u(x) if src.kind in ("f32", "absfloat") else int(x) & 0xFFFFFFFF
+                    if st.kind == "i32":
+                        return f2i(x) if src.kind in ("f32", "absfloat") else wrap32(int(x))
+                    return F32(x)
+
+                def run(env):
+                    out = []
+                    for v, n, src in parts:
+                        if n:
+                            out.extend(conv(x, src) for x in v(env))
+                        else:
+                            out.append(_cast(v(env), st))
+                    return tuple(out)
+                return run, t
             comps = [self.coerce(v, vt, st) for v, vt in evs]
             return (lambda env: tuple(_cast(c(env), st) for c in comps)), t
         if t.kind == "mat":

@@ -40,3 +40,28 @@ def test_half_rounding_matches_ieee(oracle_mod):
         got = np.float32(oracle_mod.render_scalar("half_round", float(v)))
         want = np.float32(np.float16(v))
         assert got == want or (np.isinf(got) and np.isinf(want)), (v, got, want)
+
+
+def test_filter_passes_reproduce_wgsl_golden():
+    """The renderer restatement's bilateral (depth) and gaussian (thickness)
+    passes against the reference's own fragment shaders run per pixel by the
+    WGSL interpreter (tests/golden/make_golden_render.py): X then Y pass, bit
+    for bit.  The CUDA renderer equals the restatement end to end."""
+    import os
+    from oracle import oracle as O
+    here = os.path.dirname(os.path.abspath(__file__))
+    f = dict(np.load(os.path.join(here, "golden", "render_filters.npz")))
+    dt, mf, ppc = (float(x) for x in f["constants"])
+    bx = O.render_filter_pass("bilateral", f["depth"], (1, 0), dt, mf, ppc)
+    by = O.render_filter_pass("bilateral", f["depth_x"], (0, 1), dt, mf, ppc)
+    gx = O.render_filter_pass("gaussian", f["thickness"], (1, 0))
+    gy = O.render_filter_pass("gaussian", f["thickness_x"], (0, 1))
+    for got, key in ((bx, "depth_x"), (by, "depth_xy"), (gx, "thickness_x"), (gy, "thickness_xy")):
+        assert np.array_equal(got.view(np.uint32), f[key].view(np.uint32)), key
+    # coverage: background and the >= 1e4 texel pass through, filter sizes
+    # reach the cap (depth < ppc / 100) and stay small elsewhere
+    d = f["depth"]
+    assert (f["depth_xy"][d == 0] == 0).all() and (d >= 1e4).any()
+    fluid = (d > 0) & (d < 1e4)
+    assert (ppc / d[fluid] > mf).any() and (ppc / d[fluid] < 10).any()
+    assert (f["depth_xy"][fluid] != d[fluid]).any()
