@@ -267,6 +267,12 @@ def _render_lib():
         L.ro_gaussian_pass.argtypes = [f32p, f32p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_int]
         L.ro_gaussian_pass.restype = None
+        L.ro_shade_pass.argtypes = [f32p, f32p, f32p, f32p, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int, f32p, u8p]
+        L.ro_shade_pass.restype = None
+        L.ro_sample_cube.argtypes = [f32p, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                     ctypes.c_float, f32p]
+        L.ro_sample_cube.restype = None
         L._ro_ready = True
     return L
 
@@ -302,6 +308,32 @@ def filter_constants(height: int, radius: float, fov: float):
     dt, mf, ppc = ctypes.c_float(), ctypes.c_float(), ctypes.c_float()
     L.ro_filter_constants(height, radius, fov, ctypes.byref(dt), ctypes.byref(mf), ctypes.byref(ppc))
     return dt.value, mf.value, ppc.value
+
+
+def render_shade_pass(depth: np.ndarray, thickness: np.ndarray, uniforms_f32: np.ndarray,
+                      env: np.ndarray) -> np.ndarray:
+    """The renderer's shading pass alone over filtered (H, W) depth and
+    thickness images: (H, W, 4) float32 colour."""
+    L = _render_lib()
+    d = np.ascontiguousarray(depth, dtype=np.float32)
+    t = np.ascontiguousarray(thickness, dtype=np.float32)
+    h, w = d.shape
+    u = np.ascontiguousarray(uniforms_f32, dtype=np.float32).reshape(68)
+    e = np.ascontiguousarray(env, dtype=np.float32)
+    color = np.zeros((h, w, 4), np.float32)
+    color8 = np.zeros((h, w, 4), np.uint8)
+    L.ro_shade_pass(d, t, u, e, e.shape[1], w, h, color, color8)
+    return color
+
+
+def sample_cube(env: np.ndarray, direction) -> np.ndarray:
+    """The shading pass's cube-map lookup for one direction: rgb float32."""
+    L = _render_lib()
+    e = np.ascontiguousarray(env, dtype=np.float32)
+    out = np.zeros(3, np.float32)
+    L.ro_sample_cube(e, e.shape[1], float(direction[0]), float(direction[1]),
+                     float(direction[2]), out)
+    return out
 
 
 def render_filter_pass(kind: str, img: np.ndarray, direction, depth_threshold: float = 0.0,

@@ -331,60 +331,10 @@ static void gaussian_pass(const float* src, float* dst, int W, int H, int dx, in
         }
 }
 
-int ro_render(const float* posvel, int64_t n, const ro_uniforms* u, int W, int H,
-              float depth_threshold, float max_filter_size, float ppc, const float* env,
-              int env_size, float* color, uint8_t* color8, float* depth_out, float* thick_out) {
-    const size_t np = (size_t)W * H;
-    uint64_t* dkey = (uint64_t*)malloc(8 * np);
-    int64_t* tacc = (int64_t*)calloc(np, 8);
-    float* d0 = (float*)malloc(4 * np);
-    float* d1 = (float*)malloc(4 * np);
-    float* t0 = (float*)malloc(4 * np);
-    float* t1 = (float*)malloc(4 * np);
-    if (!dkey || !tacc || !d0 || !d1 || !t0 || !t1) {
-        free(dkey); free(tacc); free(d0); free(d1); free(t0); free(t1);
-        return -1;
-    }
-    const uint64_t clear_key = ((uint64_t)0x3f800000u << 32) | 0xffffffffu;
-    for (size_t p = 0; p < np; ++p) dkey[p] = clear_key;
-    /* splats */
-    for (int64_t i = 0; i < n; ++i) {
-        billboard_t b;
-        if (!billboard(posvel, i, u, W, H, &b)) continue;
-        for (int py = b.y0; py <= b.y1; ++py)
-            for (int px = b.x0; px <= b.x1; ++px) {
-                frag_t f;
-                if (!fragment(&b, px, py, u, &f)) continue;
-                const size_t p = (size_t)py * W + px;
-                if (f.depth < 1.0f) {
-                    const uint64_t key = ((uint64_t)bitsf(f.depth) << 32) | (uint32_t)i;
-                    if (key < dkey[p]) dkey[p] = key;
-                }
-                const float t = 0.05f * f.nz;
-                tacc[p] += (int64_t)llrintf(t * 4294967296.0f);
-            }
-    }
-    /* resolve */
-    for (size_t p = 0; p < np; ++p) {
-        float d = 0.0f;
-        if (dkey[p] != clear_key) {
-            billboard_t b;
-            frag_t f;
-            const int64_t i = (int64_t)(dkey[p] & 0xffffffffu);
-            if (billboard(posvel, i, u, W, H, &b) && fragment(&b, (int)(p % W), (int)(p / W), u, &f))
-                d = f.vz;
-        }
-        d0[p] = d;
-        t0[p] = half_round((float)tacc[p] * 2.3283064365386963e-10f);
-    }
-    /* bilateral depth filter, 4 x (X, Y) */
-    for (int it = 0; it < 8; ++it)
-        bilateral_pass((it & 1) ? d1 : d0, (it & 1) ? d0 : d1, W, H, (it & 1) ? 0 : 1,
-                       (it & 1) ? 1 : 0, depth_threshold, max_filter_size, ppc);
-    /* gaussian thickness filter, X then Y */
-    for (int it = 0; it < 2; ++it)
-        gaussian_pass(it ? t1 : t0, it ? t0 : t1, W, H, it ? 0 : 1, it ? 1 : 0);
-    /* shading */
+/* fluid.wgsl:19-98 over W x H pixels: the filtered depth d0 and thickness
+ * t0 in, colour (W*H*4 floats) and its rgba8unorm store (color8) out. */
+static void shade_pass(const float* d0, const float* t0, const ro_uniforms* u, const float* env,
+                       int env_size, int W, int H, float* color, uint8_t* color8) {
     for (int py = 0; py < H; ++py)
         for (int px = 0; px < W; ++px) {
             const size_t p = (size_t)py * W + px;
@@ -439,6 +389,63 @@ int ro_render(const float* posvel, int64_t n, const ro_uniforms* u, int W, int H
             color[4 * p + 3] = 1.0f;
             color8[4 * p + 3] = 255;
         }
+}
+
+int ro_render(const float* posvel, int64_t n, const ro_uniforms* u, int W, int H,
+              float depth_threshold, float max_filter_size, float ppc, const float* env,
+              int env_size, float* color, uint8_t* color8, float* depth_out, float* thick_out) {
+    const size_t np = (size_t)W * H;
+    uint64_t* dkey = (uint64_t*)malloc(8 * np);
+    int64_t* tacc = (int64_t*)calloc(np, 8);
+    float* d0 = (float*)malloc(4 * np);
+    float* d1 = (float*)malloc(4 * np);
+    float* t0 = (float*)malloc(4 * np);
+    float* t1 = (float*)malloc(4 * np);
+    if (!dkey || !tacc || !d0 || !d1 || !t0 || !t1) {
+        free(dkey); free(tacc); free(d0); free(d1); free(t0); free(t1);
+        return -1;
+    }
+    const uint64_t clear_key = ((uint64_t)0x3f800000u << 32) | 0xffffffffu;
+    for (size_t p = 0; p < np; ++p) dkey[p] = clear_key;
+    /* splats */
+    for (int64_t i = 0; i < n; ++i) {
+        billboard_t b;
+        if (!billboard(posvel, i, u, W, H, &b)) continue;
+        for (int py = b.y0; py <= b.y1; ++py)
+            for (int px = b.x0; px <= b.x1; ++px) {
+                frag_t f;
+                if (!fragment(&b, px, py, u, &f)) continue;
+                const size_t p = (size_t)py * W + px;
+                if (f.depth < 1.0f) {
+                    const uint64_t key = ((uint64_t)bitsf(f.depth) << 32) | (uint32_t)i;
+                    if (key < dkey[p]) dkey[p] = key;
+                }
+                const float t = 0.05f * f.nz;
+                tacc[p] += (int64_t)llrintf(t * 4294967296.0f);
+            }
+    }
+    /* resolve */
+    for (size_t p = 0; p < np; ++p) {
+        float d = 0.0f;
+        if (dkey[p] != clear_key) {
+            billboard_t b;
+            frag_t f;
+            const int64_t i = (int64_t)(dkey[p] & 0xffffffffu);
+            if (billboard(posvel, i, u, W, H, &b) && fragment(&b, (int)(p % W), (int)(p / W), u, &f))
+                d = f.vz;
+        }
+        d0[p] = d;
+        t0[p] = half_round((float)tacc[p] * 2.3283064365386963e-10f);
+    }
+    /* bilateral depth filter, 4 x (X, Y) */
+    for (int it = 0; it < 8; ++it)
+        bilateral_pass((it & 1) ? d1 : d0, (it & 1) ? d0 : d1, W, H, (it & 1) ? 0 : 1,
+                       (it & 1) ? 1 : 0, depth_threshold, max_filter_size, ppc);
+    /* gaussian thickness filter, X then Y */
+    for (int it = 0; it < 2; ++it)
+        gaussian_pass(it ? t1 : t0, it ? t0 : t1, W, H, it ? 0 : 1, it ? 1 : 0);
+    /* shading */
+    shade_pass(d0, t0, u, env, env_size, W, H, color, color8);
     memcpy(depth_out, d0, 4 * np);
     memcpy(thick_out, t0, 4 * np);
     free(dkey); free(tacc); free(d0); free(d1); free(t0); free(t1);
@@ -464,6 +471,18 @@ void ro_bilateral_pass(const float* src, float* dst, int W, int H, int dx, int d
 }
 void ro_gaussian_pass(const float* src, float* dst, int W, int H, int dx, int dy) {
     gaussian_pass(src, dst, W, H, dx, dy);
+}
+void ro_shade_pass(const float* d0, const float* t0, const ro_uniforms* u, const float* env,
+                   int env_size, int W, int H, float* color, uint8_t* color8) {
+    shade_pass(d0, t0, u, env, env_size, W, H, color, color8);
+}
+/* The cube-map lookup of the shading pass (bilinear within the face the
+ * direction selects), for the golden tests' interpreter. */
+void ro_sample_cube(const float* env, int size, float x, float y, float z, float* out3) {
+    const v3 c = sample_cube(env, size, mk(x, y, z));
+    out3[0] = c.x;
+    out3[1] = c.y;
+    out3[2] = c.z;
 }
 float ro_exp(float x) { return exp_r(x); }
 float ro_log(float x) { return log_r(x); }

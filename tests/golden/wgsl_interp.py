@@ -206,11 +206,15 @@ class Parser:
             return ("vec", int(name[3]), e)
         if len(name) == 5 and name[:3] == "vec" and name[3] in "234" and name[4] in "fiu":
             return ("vec", int(name[3]), ({"f": "f32", "i": "i32", "u": "u32"}[name[4]],))
-        if name == "texture_2d":
+        if name in ("texture_2d", "texture_cube"):
             self.expect("<")
             e = self.parse_type()
             self.expect(">")
-            return ("texture", e)
+            return ("texture" if name == "texture_2d" else "texture_cube", e)
+        if name == "sampler":
+            return ("sampler",)
+        if name == "mat4x4f":
+            return ("mat", 4, ("f32",))
         if name == "mat3x3f":
             return ("mat", 3, ("f32",))
         if name == "mat3x3":
@@ -470,6 +474,11 @@ SWZ = {"x": 0, "y": 1, "z": 2, "w": 3, "r": 0, "g": 1, "b": 2, "a": 3}
 
 # exp(x) for f32 x; a fixture generator installs the project's restatement
 EXP_F32 = lambda x: np.exp(np.float32(x))  # noqa: E731
+# pow(x, y) when installed (the renderer's restatement), else pow(x, 5.0) as a
+# product chain and other exponents through float arithmetic
+POW_F32 = None
+# cube-map lookup of textureSampleLevel, installed by a fixture generator
+CUBE_SAMPLE = None
 
 
 class Module:
@@ -512,8 +521,10 @@ class Module:
             return T("atomic", self.resolve(ty[1]))
         if k == "array":
             return T("array", self.resolve(ty[1]), ty[2] or 0)
-        if k == "texture":
-            return T("texture", self.resolve(ty[1]))
+        if k in ("texture", "texture_cube"):
+            return T(k, self.resolve(ty[1]))
+        if k == "sampler":
+            return T("sampler")
         if k in self.structs:
             return self.structs[k]
         raise TypeError(f"unknown type {ty}")
@@ -738,6 +749,8 @@ class Module:
                         rec[f] = v
                 return get, setv, ft
             if bt.kind == "vec":
+                if len(f) > 1:  # a multi-component swizzle is read as a value
+                    raise SyntaxError("swizzle")
                 c = SWZ[f]
 
                 def get(env):
@@ -821,6 +834,10 @@ class Module:
         base_v, bt = self.compile_expr(e[1], scope)
         if e[0] == "member":
             if bt.kind == "vec":
+                if len(e[2]) > 1:
+                    cs = [SWZ[ch] for ch in e[2]]
+                    return ((lambda env: tuple(base_v(env)[c] for c in cs)), None,
+                            vec(bt.elem, len(cs)))
                 c = SWZ[e[2]]
                 return (lambda env: base_v(env)[c]), None, bt.elem
             ft = dict(bt.fields)[e[2]]
@@ -902,8 +919,48 @@ class Module:
             # WGSL leaves exp's precision to the implementation: the project's
             # restatement is used wherever it is installed (EXP_F32)
             (v, t), = evs
+            if t.kind == "vec":
+                return (lambda env: tuple(F32(EXP_F32(F32(x))) for x in v(env))), t
             v = self.coerce(v, t, TF32)
             return (lambda env: F32(EXP_F32(F32(v(env))))), TF32
+        if name == "cross":
+            (a, at), (b, bt) = evs
+
+            def run(env):
+                x, y = a(env), b(env)
+                return (F32(F32(x[1] * y[2]) - F32(x[2] * y[1])),
+                        F32(F32(x[2] * y[0]) - F32(x[0] * y[2])),
+                        F32(F32(x[0] * y[1]) - F32(x[1] * y[0])))
+            return run, at
+        if name == "reflect":
+            # e1 - 2 * dot(e2, e1) * e2
+            (a, at), (b, bt) = evs
+
+            def run(env):
+                e1, e2 = a(env), b(env)
+                k = F32(F32(2.0) * _dot(e2, e1))
+                return tuple(F32(F32(x) - F32(k * F32(n))) for x, n in zip(e1, e2))
+            return run, at
+        if name == "mix":
+            # e1 * (1 - e3) + e2 * e3, e3 a scalar or a vector
+            (a, at), (b, bt), (c, ct) = evs
+            c = self.coerce(c, ct, at.elem if ct.kind != "vec" else ct)
+
+            def run(env):
+                e1, e2, e3 = a(env), b(env), c(env)
+                ts = e3 if isinstance(e3, tuple) else (e3,) * len(e1)
+                return tuple(F32(F32(x * F32(F32(1.0) - t)) + F32(y * t))
+                             for x, y, t in zip(e1, e2, ts))
+            return run, at
+        if name == "textureSampleLevel":
+            # the sampling unit's filtering is not shader arithmetic: a fixture
+            # generator installs it (CUBE_SAMPLE(texture, direction) -> rgb)
+            (tv, tt), _s, (dv, dt_), _lvl = evs
+
+            def run(env):
+                r, g, b_ = CUBE_SAMPLE(tv(env), dv(env))
+                return (F32(r), F32(g), F32(b_), F32(1.0))
+            return run, vec(TF32, 4)
         if name == "textureLoad":
             # a single-channel texture as an (H, W) float32 array; a texel
             # outside it reads the nearest edge texel (WGSL lets an
@@ -986,7 +1043,7 @@ class Module:
             t = at if not is_abstract(at) else bt
             a = self.coerce(a, at, scalar_of(t))
             b = self.coerce(b, bt, scalar_of(t))
-            return (lambda env: _pow(a(env), b(env))), t
+            return (lambda env: (POW_F32 or _pow)(a(env), b(env))), t
         if name in self.funcs:
             run, ret, params = self.compile_fn(self.funcs[name])
             conv = [self.coerce(ev, et, pt) for (ev, et), (_, pt) in zip(evs, params)]

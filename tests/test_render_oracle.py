@@ -65,3 +65,23 @@ def test_filter_passes_reproduce_wgsl_golden():
     fluid = (d > 0) & (d < 1e4)
     assert (ppc / d[fluid] > mf).any() and (ppc / d[fluid] < 10).any()
     assert (f["depth_xy"][fluid] != d[fluid]).any()
+
+
+def test_shading_pass_reproduces_wgsl_golden():
+    """The restatement's shading against the reference's fluid.wgsl fragment
+    shader run per pixel by the WGSL interpreter over filtered depth and
+    thickness images (tests/golden/make_golden_render.py): every colour bit
+    for bit, the NaNs at silhouettes (a neighbour reads the background depth
+    0) in the same places."""
+    import os
+    from oracle import oracle as O
+    here = os.path.dirname(os.path.abspath(__file__))
+    f = dict(np.load(os.path.join(here, "golden", "render_shading.npz")))
+    got = O.render_shade_pass(f["depth"], f["thickness"], f["uniforms"], f["env"])
+    want = f["color"]
+    nan = np.isnan(want)
+    assert np.array_equal(np.isnan(got), nan)
+    assert np.array_equal(got.view(np.uint32)[~nan], want.view(np.uint32)[~nan])
+    fluid = (f["depth"] > 0) & (f["depth"] < 1e4)
+    assert fluid.any() and (~fluid).any() and nan.any()
+    assert np.allclose(want[~fluid][:, :3], 0.8)  # background colour
