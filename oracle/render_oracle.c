@@ -5,14 +5,14 @@
  * TEST INFRASTRUCTURE ONLY: loaded by tests/ as the checker of the headless
  * CUDA renderer, never by the product.
  *
- * The splats and the shading are unpinned against the reference itself:
- * they are WGSL render pipelines that need a WebGPU implementation and a
- * graphics stack, neither of which exists here (unavailable on this machine).
- * The two filter passes are pinned: tests/golden/make_golden_render.py runs
- * the reference's bilateral.wgsl and gaussian.wgsl fragment shaders (read as
- * text) per pixel through the WGSL interpreter, and bilateral_pass /
- * gaussian_pass reproduce them bit for bit.  This file restates the shader
- * math of
+ * The fullscreen passes are pinned to the reference itself:
+ * tests/golden/make_golden_render.py runs its bilateral.wgsl, gaussian.wgsl
+ * and fluid.wgsl fragment shaders (read as text) per pixel through the WGSL
+ * interpreter, and bilateral_pass / gaussian_pass / shade_pass reproduce them
+ * bit for bit.  The two splats are unpinned: they need rasterisation, depth
+ * testing and blending, i.e. a WebGPU implementation and a graphics stack,
+ * neither of which exists here (unavailable on this machine).  This file restates
+ * the shader math of
  *   depthMap.wgsl:34-79      billboard depth splat, 'less' depth test
  *   thicknessMap.wgsl:27-62  additive thickness splat
  *   bilateral.wgsl:18-75     separable bilateral depth filter (4 x X, Y)
