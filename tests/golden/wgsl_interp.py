@@ -1,17 +1,30 @@
-"""A small WGSL compute-shader interpreter (the subset the MLS-MPM kernels use).
+"""A small WGSL interpreter: the subset the reference's compute shaders
+(MLS-MPM, SPH) and fullscreen fragment shaders (bilateral and gaussian
+filters, shading) use.
 
-TEST INFRASTRUCTURE: make_golden.py runs the reference's own WGSL source text
-(mls-mpm/*.wgsl) through this interpreter to produce golden vectors that pin
-the C oracle.  It is independent of the oracle: it parses the shader and
-evaluates it with WGSL's static typing and abstract-numeric conversion rules,
-rounding every f32 operation separately (numpy float32 scalars).
+TEST INFRASTRUCTURE: make_golden.py, make_golden_sph.py and
+make_golden_render.py run the reference's own WGSL source text through this
+interpreter to produce golden vectors that pin the C oracles.  It is
+independent of the oracles: it parses the shader and evaluates it with
+WGSL's static typing and abstract-numeric conversion rules, rounding every
+f32 operation separately (numpy float32 scalars).  Compute entry points run
+one invocation at a time (dispatch); a fragment entry point is called once
+per pixel with its interpolated inputs.
 
 Choices the WGSL specification leaves to the implementation are fixed the
-same way the oracle fixes them (they cannot be pinned by any source):
-  * mat3x3f * vec3f = (c0*v.x + c1*v.y) + c2*v.z;
-  * pow(x, 5.0) = ((x*x)*(x*x))*x (pow(x, y) for other y uses float64 pow);
-  * f32 -> i32 of NaN is 0; out-of-range conversions saturate (spec);
-  * a storage access outside the bound array reads zero and drops writes.
+same way the oracles fix them (they cannot be pinned by any source):
+  * matrix * vector adds the columns in order: ((c0*v.x + c1*v.y) + c2*v.z) ...;
+  * dot(a, b) = (a.x*b.x + a.y*b.y) + a.z*b.z; normalize(v) = v / sqrt(dot(v, v));
+    sqrt correctly rounded;
+  * pow(x, 5.0) = ((x*x)*(x*x))*x (other exponents through float64 pow) unless
+    a generator installs POW_F32; exp is EXP_F32 (float64 exp by default;
+    the renderer's generator installs the project's restatement);
+  * f32 -> i32 / u32 of NaN is 0; out-of-range conversions saturate (spec);
+  * a storage access outside the bound array reads zero and drops writes, and
+    is counted once per visit (consecutive accesses to one element);
+  * a texture load outside the image reads the nearest edge texel; a cube
+    texture is sampled by CUBE_SAMPLE, which a generator installs (filtering
+    is the sampling unit's work, not shader arithmetic).
 Everything else (operand order, literal conversion, integer wraparound, loop
 structure, which fields are read and written) comes from the shader text.
 """
