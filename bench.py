@@ -189,6 +189,70 @@ def cpu_baseline_detail(pkg, budget_s: float = 3.0) -> dict:
     return out
 
 
+PARITY_FRAMES = (1, 5, 25, 100, 200)
+
+
+def cpu_baseline_and_parity(pkg, parts, stream, skip_parity: bool = False):
+    """One oracle run of the benchmarked configuration from its initial
+    state on all host threads.  Its first ~10 s are the timed CPU baseline;
+    unless skipped, it continues for the configuration's full 200 frames
+    and the GPU's grid, particles and posvel (a fresh simulator, same scene,
+    sorted engine, CUDA graphs) are compared with it bit for bit after
+    frames 1, 5, 25, 100 and 200."""
+    import numpy as np
+    from oracle import oracle
+    nt = cpu_threads()
+    n = len(parts)
+    snaps = {}
+    if not skip_parity:
+        sim = pkg.MLSMPMSimulator(None, None, 1.2, maxParticles=n, maxGrid=(128, 128, 128))
+        sim.upload(parts, BOX)
+        for frame in range(1, PARITY_FRAMES[-1] + 1):
+            sim.execute(stream)
+            if frame in PARITY_FRAMES:
+                stream.synchronize()
+                snaps[frame] = (sim.downloadGrid(), sim.downloadParticles(), sim.downloadPosvel())
+        sim.close()
+    ref = oracle.OracleSim(parts, BOX)
+    frames_timed, timed_s, t0 = 0, None, time.perf_counter()
+    compare_s = 0.0  # comparisons inside the timed window are not CPU-baseline time
+    results = {}
+    last = PARITY_FRAMES[-1] if snaps else 10 ** 9
+    for frame in range(1, last + 1):
+        ref.execute(SUBSTEPS, nt)
+        if timed_s is None:
+            frames_timed = frame
+            if time.perf_counter() - t0 - compare_s > 10.0:
+                timed_s = time.perf_counter() - t0 - compare_s
+                if not snaps:
+                    break
+        if frame in snaps:
+            c0 = time.perf_counter()
+            g, p, pv = snaps.pop(frame)
+            results[frame] = {
+                "grid": bool(np.array_equal(g, ref.cells)),
+                "particles": bool(np.array_equal(p.view(np.uint32),
+                                                 ref.particles.view(np.uint32))),
+                "posvel": bool(np.array_equal(pv.view(np.uint32), ref.posvel.view(np.uint32)))}
+            compare_s += time.perf_counter() - c0
+    if timed_s is None:
+        timed_s = time.perf_counter() - t0 - compare_s
+    cpu = {"value": n * SUBSTEPS * frames_timed / timed_s, "unit": UNIT, "cores": nt,
+           "kind": "port",
+           "sample": f"the first {frames_timed} steps of the same 1M-particle workload from its "
+                     f"initial state ({frames_timed * SUBSTEPS} substeps, {timed_s:.1f} s) on "
+                     f"{nt} host threads"}
+    parity = None
+    if results:
+        parity = {"vs_oracle_frames": sorted(results),
+                  "vs_oracle_bit_exact": all(all(v.values()) for v in results.values()),
+                  "vs_oracle": {str(k): v for k, v in sorted(results.items())},
+                  "vs_oracle_what": "grid, particles and posvel of the benchmarked 1M / 128^3 "
+                                    "configuration (seed 20240601) after frames 1, 5, 25, 100 "
+                                    "and 200 of a fresh run, against the CPU oracle"}
+    return cpu, parity
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -216,10 +280,12 @@ def run_reference(args) -> None:
     world, rank, _ = dist_setup()
     if rank != 0:
         return
-    import __graft_entry__ as entry
-    entry.build()
-    pkg = entry.load_package()
-    parts = make_scene(pkg)
+    # Only the oracle is built and loaded here: the scene comes from its own
+    # builder (bit-identical to the library's, tested), so this arm maps no
+    # file of the product.
+    from oracle import oracle, scene
+    oracle.build()
+    parts = scene.lattice(N_PER_AXIS, ORIGIN, SPACING, JITTER, SEED)
     n = len(parts)
     nt = cpu_threads()
     budget = max(30.0, min(150.0, 15.0 * args.steps))
@@ -603,6 +669,51 @@ def measure_sph(pkg, torch, frames: int = 50) -> dict:
     return out
 
 
+C0_WORKLOAD = ("jittered lattice dam-break: 64,000 particles (40^3, spacing 0.5, jitter +-0.05, "
+               "filling [3,23)^3), 64^3 grid, 2 substeps/step")
+
+
+def measure_c0(pkg, torch, stream, steps: int = 50, warmup: int = 5) -> dict:
+    """The 64,000-particle / 64^3 configuration (the reference's scale:
+    its UI tops out at 200,000 particles on a 64^3 grid): device-resident
+    particle-substeps/s over `steps` steps after `warmup`, per-step CUDA
+    events (inputs far below L2 size, so no flush), and the configuration's
+    whole 100-frame run from the initial state."""
+    parts = pkg.scene_lattice(40, 3.0, SPACING, JITTER, SEED)
+    box = [64.0, 64.0, 64.0]
+    n = len(parts)
+    sim = pkg.MLSMPMSimulator(None, None, 1.2, maxParticles=n, maxGrid=(64, 64, 64))
+    sim.upload(parts, box)
+    for _ in range(warmup):
+        sim.execute(stream)
+    stream.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    for a, b in ev:
+        a.record(stream)
+        sim.execute(stream)
+        b.record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    sim.upload(parts, box)
+    stream.synchronize()
+    fa, fb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fa.record(stream)
+    for _ in range(100):
+        sim.execute(stream)
+    fb.record(stream)
+    torch.cuda.synchronize()
+    full_ms = fa.elapsed_time(fb)
+    sim.close()
+    return {"workload": C0_WORKLOAD, "particles": n, "steps": steps, "warmup": warmup,
+            "ms_per_step": ms / steps,
+            "particle_substeps_per_s": n * SUBSTEPS * steps / (ms / 1e3),
+            "full_100_frame_run": {"ms": full_ms,
+                                   "particle_substeps_per_s": n * SUBSTEPS * 100 / (full_ms / 1e3)},
+            "timing": "CUDA events per step on the launch stream (CUDA graph), summed; "
+                      "full run: one event pair around 100 execute() calls from the upload"}
+
+
 def measure_expanding(pkg, torch, substeps: int = 40) -> dict:
     """The inverse problem's 64 scenes (1.52M particles) stepped from their
     initial state without CUDA graphs (one launch per kernel, for launch-level
@@ -873,6 +984,7 @@ def run_ours(args) -> None:
     assert np.isfinite(hosts[(K - 1) % 2][:, 0:3]).all(), "posvel read back non-finite positions"
     sim.close()
 
+    c0 = measure_c0(pkg, torch, stream)
     batched = None if args.skip_batched else measure_batched(pkg, torch, stream,
                                                              autotune=not args.no_autotune)
     adjoint = None if args.skip_adjoint else measure_adjoint(pkg, torch)
@@ -900,13 +1012,10 @@ def run_ours(args) -> None:
         return
 
     cpu = None
+    vs_oracle = None
     if world == 1 and not args.no_cpu_baseline:
-        nt = cpu_threads()
-        done, dt = time_oracle(parts, 1000, 0, 10.0, nt)
-        cpu = {"value": n * SUBSTEPS * done / dt, "unit": UNIT, "cores": nt, "kind": "port",
-               "sample": f"{done} steps of the same 1M-particle workload from its initial "
-                         f"state ({done * SUBSTEPS} substeps, {dt:.1f} s) on {nt} host threads",
-               "detail": cpu_baseline_detail(pkg)}
+        cpu, vs_oracle = cpu_baseline_and_parity(pkg, parts, stream, args.no_parity)
+        cpu["detail"] = cpu_baseline_detail(pkg)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
@@ -933,6 +1042,7 @@ def run_ours(args) -> None:
         "clocks": clocks,
         "issue_roofline": issue,
         "full_200_frame_run": full_run,
+        "c0_64k_64": c0,
         "gpu_launches": launches,
         "wall_s_timed_region": wall,
         "kernels": kernels,
@@ -941,8 +1051,10 @@ def run_ours(args) -> None:
         "inverse_problem": inverse,
         "render": render,
         "sph": sph,
-        "parity": {"grid_bit_exact_vs_dispatch_engine": grid_exact,
-                   "particles_bit_exact_vs_dispatch_engine": parts_exact, "steps": 3},
+        "parity": {**(vs_oracle or {"vs_oracle": "not run"}),
+                   "engines": {"grid_bit_exact_vs_dispatch_engine": grid_exact,
+                               "particles_bit_exact_vs_dispatch_engine": parts_exact,
+                               "steps": 3}},
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
@@ -955,7 +1067,10 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="leave out the CPU oracle (its timed sample and the 200-frame parity run)")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="time the CPU baseline only; skip the 200-frame comparison with the oracle")
     ap.add_argument("--skip-batched", action="store_true",
                     help="leave out the batched-scenes measurement")
     ap.add_argument("--skip-adjoint", action="store_true",

@@ -434,12 +434,16 @@ int mpm_sph_scene_dambreak(float* out_rec64, int num_particles, const double ini
  * unbounded time) or a plugin host that owns all device memory.  Counts the
  * records among n (each stride_floats floats, 20 for the 80-byte particle
  * layout) that hold a non-finite value and writes the count to *count_out
- * (device memory), asynchronously on `stream`, on the current device.
+ * (device memory), asynchronously on `stream`, on the current device.  With
+ * stride_floats == 20 the 16 state floats of each record are checked, as
+ * mpm_check_health does, and the five padding floats (3, 7, 11, 15, 19) are
+ * skipped; with any other stride every float is checked.
  * Limit: n <= 16,777,216 records; larger n returns MPM_E_CAPACITY.
  * Scratch: a fixed 512 KiB device array inside the library, which every GPU
- * that loads the library holds until exit.  The first call on a device looks
- * up that array's device address (cudaGetSymbolAddress) and zeroes its
- * ticket synchronously; make that first call before any stream capture.
+ * that loads the library holds until exit.  Every call looks up that
+ * array's device address in the current context (cudaGetSymbolAddress,
+ * which allocates nothing); the first call on a device may load the
+ * library's device code, so make it before any stream capture.
  * All calls share the array: calls that overlap on the GPU race.
  */
 int mpm_count_nonfinite_noalloc(const float* records, int stride_floats, int n,

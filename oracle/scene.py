@@ -66,8 +66,38 @@ def dambreak(init_box, num_particles: int, seed: int) -> np.ndarray:
     return out
 
 
+def splitmix64_uniform(seed: int, count: int) -> np.ndarray:
+    """The first `count` draws of SplitMix64(seed).random(), vectorised: draw
+    k mixes the state seed + (k + 1) * gamma (mod 2**64), exactly as the
+    sequential generator above advances it."""
+    with np.errstate(over="ignore"):
+        k = np.arange(1, count + 1, dtype=np.uint64)
+        z = np.uint64(seed & MASK64) + k * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
 def lattice(n_per_axis: int, origin: float, spacing: float, jitter: float, seed: int) -> np.ndarray:
-    """Jittered cubic lattice, x-major (z fastest), jitter U[-jitter, jitter)."""
+    """Jittered cubic lattice, x-major (z fastest), jitter U[-jitter, jitter):
+    coordinate a of particle (ix, iy, iz) is (origin + spacing*i_a) +
+    jitter*(2u - 1), u the next draw, three draws per particle in x, y, z
+    order (all in double precision, rounded once to float32)."""
+    n = n_per_axis ** 3
+    u = splitmix64_uniform(seed, 3 * n).reshape(n, 3)
+    i = np.arange(n_per_axis, dtype=np.float64)
+    idx = np.stack(np.meshgrid(i, i, i, indexing="ij"), axis=-1).reshape(n, 3)
+    pos = (origin + spacing * idx) + jitter * (2.0 * u - 1.0)
+    out = np.zeros((n, PARTICLE_FLOATS), dtype=np.float32)
+    out[:, 0:3] = pos.astype(np.float32)
+    return out
+
+
+def lattice_sequential(n_per_axis: int, origin: float, spacing: float, jitter: float,
+                       seed: int) -> np.ndarray:
+    """`lattice` written as the plain loop over the sequential generator (the
+    definition the vectorised version is tested against)."""
     rng = SplitMix64(seed)
     n = n_per_axis ** 3
     pos = np.empty((n, 3), dtype=np.float64)

@@ -7,7 +7,7 @@ wgsl_interp.py, dispatched in the order of MLSMPMSimulator.execute
 
 Run from the repository root (needs the reference checkout; the fixtures it
 writes are committed so that the tests never read the reference):
-    python tests/golden/make_golden.py [--reference /path/to/WebGPU-Ocean]
+    python tests/golden/make_golden.py --reference /path/to/WebGPU-Ocean
 
 Each fixture holds the inputs (particles in the 80-byte layout, init and real
 box) and, for substep 0, the grid / particles / posvel after every one of the
@@ -148,7 +148,10 @@ def wall_impact_particles() -> np.ndarray:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("WEBGPU_OCEAN_REFERENCE"),
+                    required="WEBGPU_OCEAN_REFERENCE" not in os.environ,
+                    help="checkout of matsuoka-601/WebGPU-Ocean (or set "
+                         "WEBGPU_OCEAN_REFERENCE)")
     ap.add_argument("--only", nargs="*", help="fixture names to (re)generate (default: all)")
     args = ap.parse_args()
     src_dir = os.path.join(args.reference, "mls-mpm")

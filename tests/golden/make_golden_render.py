@@ -27,7 +27,7 @@ What the graphics pipeline supplies is fixed as follows:
     reference's particle radius and field of view (main.ts:136-137).
 
 Run from the repository root (needs the reference checkout):
-    python tests/golden/make_golden_render.py [--reference /path/to/WebGPU-Ocean]
+    python tests/golden/make_golden_render.py --reference /path/to/WebGPU-Ocean
 """
 from __future__ import annotations
 
@@ -79,7 +79,10 @@ def run_pass(module, img, blur_dir, half_target):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("WEBGPU_OCEAN_REFERENCE"),
+                    required="WEBGPU_OCEAN_REFERENCE" not in os.environ,
+                    help="checkout of matsuoka-601/WebGPU-Ocean (or set "
+                         "WEBGPU_OCEAN_REFERENCE)")
     args = ap.parse_args()
     from oracle import oracle as O
     W.EXP_F32 = lambda x: np.float32(O.render_scalar("exp", float(x)))

@@ -26,7 +26,7 @@ of the reference:
 
 Run from the repository root (needs the reference checkout; the fixtures are
 committed so the tests never read the reference):
-    python tests/golden/make_golden_sph.py [--reference /path/to/WebGPU-Ocean]
+    python tests/golden/make_golden_sph.py --reference /path/to/WebGPU-Ocean
 """
 from __future__ import annotations
 
@@ -174,7 +174,10 @@ def cases():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("WEBGPU_OCEAN_REFERENCE"),
+                    required="WEBGPU_OCEAN_REFERENCE" not in os.environ,
+                    help="checkout of matsuoka-601/WebGPU-Ocean (or set "
+                         "WEBGPU_OCEAN_REFERENCE)")
     ap.add_argument("--only", nargs="*", help="fixture names to (re)generate (default: all)")
     args = ap.parse_args()
     src_dir = os.path.join(args.reference, "sph")

@@ -79,6 +79,24 @@ def test_lattice_scene_matches_restatement(pkg):
     assert np.all(np.abs(got[:, 0:3] - np.round((got[:, 0:3] - 3.0) / 0.5) * 0.5 - 3.0) <= 0.0501)
 
 
+def test_lattice_vectorised_equals_sequential_definition():
+    """oracle/scene.py draws the lattice's jitter with a vectorised SplitMix64;
+    it must equal the plain sequential loop draw for draw."""
+    from oracle import scene
+    for args in ((9, 3.0, 0.5, 0.05, 7), (16, 8.0, 0.5, 0.05, 3), (5, 4.0, 0.5, 0.05, 20240601)):
+        assert_bits_equal(scene.lattice(*args), scene.lattice_sequential(*args), f"lattice {args}")
+
+
+def test_benchmark_lattice_matches_restatement(pkg):
+    """The 1,000,000-particle benchmark scene (100^3 points from 4, spacing
+    0.5, jitter 0.05, seed 20240601): the library's builder and the oracle's
+    give the same bits, so the CPU reference arm never needs the library."""
+    from oracle import scene
+    got = pkg.scene_lattice(100, 4.0, 0.5, 0.05, 20240601)
+    want = scene.lattice(100, 4.0, 0.5, 0.05, 20240601)
+    assert_bits_equal(got, want, "1M lattice")
+
+
 def test_no_device_is_reported_not_faked(pkg):
     """Without a GPU, creating a simulator fails loudly (no CPU fallback)."""
     import torch

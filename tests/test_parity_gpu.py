@@ -260,6 +260,27 @@ def test_lattice_1m_128(cuda, pkg, oracle_mod, engine):
     sim.close()
 
 
+def test_benchmark_workload_200_frames(cuda, pkg, oracle_mod):
+    """The benchmarked configuration exactly: the 1,000,000-particle lattice
+    (100^3 points from 4, spacing 0.5, jitter 0.05, seed 20240601) on 128^3,
+    the sorted engine with CUDA graphs, for the configuration's full 200
+    frames (400 substeps); grid, particles and posvel bit-exact against the
+    oracle after frames 1, 5, 25, 100 and 200."""
+    from oracle import scene
+    box = [128.0, 128.0, 128.0]
+    parts = scene.lattice(100, 4.0, 0.5, 0.05, 20240601)
+    sim = make_sim(pkg, "sorted", max_particles=1_000_000, max_grid=(128, 128, 128))
+    sim.upload(parts, box)
+    ref = oracle_mod.OracleSim(parts, box)
+    checks = {1, 5, 25, 100, 200}
+    for frame in range(1, 201):
+        sim.execute()
+        ref.execute(2, NTHREADS)
+        if frame in checks:
+            assert_state_equal(sim, ref, f"benchmark workload frame {frame}")
+    sim.close()
+
+
 def test_packed_f32x2_matches_scalar_ieee(cuda, pkg):
     """The sorted engine pairs independent products in mul.rn.f32x2 and adds
     them with scalar add.rn.f32 (ptxas would contract a packed product that

@@ -53,6 +53,36 @@ def test_noalloc_watchdog_matches_check_health(cuda, pkg):
     sim.close()
 
 
+def test_noalloc_skips_padding_of_80_byte_records(cuda, pkg):
+    """WGSL struct stores leave the padding of the 80-byte record unspecified:
+    a NaN or Inf there is not a non-finite particle (mpm_check_health never
+    sees padding: the upload drops it).  Any other stride checks every float."""
+    torch = cuda
+    from oracle import scene
+    lib = pkg._lib.load()
+    parts = scene.lattice(10, 6.0, 0.5, 0.05, 23)
+    for j, rec in zip((3, 7, 11, 15, 19), (0, 17, 256, 511, 999)):
+        parts[rec, j] = np.nan if j % 2 else np.inf        # padding only
+    parts[5, 4] = np.nan                                   # one real state float
+    sim = pkg.MLSMPMSimulator(None, None, 1.2, maxParticles=len(parts), maxGrid=(32, 32, 32))
+    sim.upload(parts, [32.0, 32.0, 32.0])
+    want = sim.checkHealth()["nonfinite_particles"]
+    sim.close()
+    assert want == 1
+    recs = torch.from_numpy(parts).cuda()
+    out = torch.zeros(1, dtype=torch.int64, device="cuda")
+    stream = torch.cuda.current_stream()
+    for stride, n, expect in ((20, len(parts), want), (4, len(parts) * 5, 6)):
+        for call in range(2):
+            out.fill_(-1)
+            rc = lib.mpm_count_nonfinite_noalloc(ctypes.c_void_p(recs.data_ptr()), stride, n,
+                                                 ctypes.c_void_p(out.data_ptr()),
+                                                 ctypes.c_void_p(stream.cuda_stream))
+            assert rc == 0, lib.mpm_last_error()
+            torch.cuda.synchronize()
+            assert int(out.item()) == expect, f"stride {stride}, call {call}"
+
+
 def test_noalloc_rejects_oversized_calls(cuda, pkg):
     torch = cuda
     lib = pkg._lib.load()

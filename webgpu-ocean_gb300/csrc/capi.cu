@@ -552,11 +552,28 @@ int mpm_download_posvel_async(mpm_sim* s, float* out, void* stream) {
     if (!out && s->n) return fail(MPM_E_INVALID, "null output");
     DeviceGuard g(s->device);
     if (!s->copy_stream) {
-        MPM_CUDA(cudaMalloc(&s->posvel_snap, sizeof(float4) * 2 * (size_t)(s->max_particles > 0 ? s->max_particles : 1)));
-        MPM_CUDA(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
-        MPM_CUDA(cudaEventCreateWithFlags(&s->snap_taken, cudaEventDisableTiming));
-        MPM_CUDA(cudaEventCreateWithFlags(&s->snap_copied, cudaEventDisableTiming));
-        MPM_CUDA(cudaEventRecord(s->snap_copied, s->copy_stream));
+        // Made into locals and committed together, so a failure part-way
+        // leaves the handle as it was (and frees what was made).
+        float4* snap = nullptr;
+        cudaStream_t cs = nullptr;
+        cudaEvent_t taken = nullptr, copied = nullptr;
+        cudaError_t e = cudaMalloc(&snap, sizeof(float4) * 2 *
+                                              (size_t)(s->max_particles > 0 ? s->max_particles : 1));
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&taken, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&copied, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(copied, cs);
+        if (e != cudaSuccess) {
+            if (copied) cudaEventDestroy(copied);
+            if (taken) cudaEventDestroy(taken);
+            if (cs) cudaStreamDestroy(cs);
+            cudaFree(snap);
+            return cuda_fail(e, "mpm_download_posvel_async set-up");
+        }
+        s->posvel_snap = snap;
+        s->copy_stream = cs;
+        s->snap_taken = taken;
+        s->snap_copied = copied;
     }
     if (!s->n) return MPM_OK;
     cudaStream_t st = static_cast<cudaStream_t>(stream);

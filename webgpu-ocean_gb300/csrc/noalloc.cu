@@ -11,9 +11,14 @@
 // count per thread block and a completion ticket) in a file-scope device
 // array that is part of the library image: every GPU that loads libmpm.so
 // holds those 512 KiB until the process exits.
+//
+// Which floats are checked: for the 80-byte particle record (stride 20) the
+// 16 state floats, as mpm_check_health does; the five padding floats (3, 7,
+// 11, 15, 19: the fourth float of each vec3f slot and of each column of C)
+// are skipped, because a WGSL struct store leaves them unspecified.  For any
+// other stride every float of a record is checked.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "../../include/mpm.h"
@@ -27,16 +32,12 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kMaxBlocks = 65536;  // records per call <= kMaxBlocks * kThreads
 constexpr long long kMaxRecords = (long long)kMaxBlocks * kThreads;
-constexpr int kMaxDevices = 64;
 
 // [0]: completion ticket, zero between calls; [1 + b]: count of block b.
 static __device__ __align__(256) unsigned long long g_scratch[1 + kMaxBlocks];
 
-// Device address of g_scratch per device ordinal, looked up once per device
-// with that device current (in host code the symbol's name is only a host
-// stand-in, not a device address).
-std::mutex g_mu;
-unsigned long long* g_scratch_ptr[kMaxDevices] = {};
+// g_scratch is zero when the module loads into a context, and the last block
+// of every call sets the ticket back to zero, so no call has to clear it.
 
 __global__ void __launch_bounds__(kThreads)
     k_count_nonfinite_noalloc(const float* __restrict__ rec, int stride, int n,
@@ -51,7 +52,9 @@ __global__ void __launch_bounds__(kThreads)
     bool bad = false;
     if (i < n) {
         const float* r = rec + i * (long long)stride;
-        for (int j = 0; j < stride; ++j) bad |= !isfinite(r[j]);
+        const bool padded = stride == 20;  // the reference's 80-byte particle record
+        for (int j = 0; j < stride; ++j)
+            if (!padded || (j & 3) != 3) bad |= !isfinite(r[j]);
     }
     const unsigned m = __ballot_sync(0xffffffffu, bad);
     if ((threadIdx.x & 31u) == 0 && m) atomicAdd(&s_count, (unsigned)__popc(m));
@@ -84,23 +87,19 @@ int fail(int code, const std::string& msg) {
     return code;
 }
 
-// Once per device: the device address of g_scratch, and its ticket zeroed.
+// The device address of g_scratch in the current device's context.  In host
+// code the array's name is only a host-side stand-in, not a device address.
+// The lookup runs on every call (it allocates nothing), so a context that
+// was reset or replaced on the same device never leaves a stale address.
 int scratch_for_current_device(unsigned long long** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail(MPM_E_NO_DEVICE, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return fail(MPM_E_INVALID, "device ordinal out of range");
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_scratch);
-        if (e != cudaSuccess)
-            return fail(MPM_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        e = cudaMemset(p, 0, sizeof(unsigned long long));
-        if (e != cudaSuccess) return fail(MPM_E_CUDA, std::string("cudaMemset: ") + cudaGetErrorString(e));
-        g_scratch_ptr[dev] = static_cast<unsigned long long*>(p);
-    }
-    *out = g_scratch_ptr[dev];
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_scratch);
+    if (e != cudaSuccess)
+        return fail(MPM_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    *out = static_cast<unsigned long long*>(p);
     return MPM_OK;
 }
 
