@@ -58,15 +58,15 @@ int64_t orc64_grid_count(const orc64_params* p) {
            (int64_t)ceil(p->init_box[2]);
 }
 
-/* Runs `substeps` substeps on state (n x 15 doubles) in place.  Returns the
- * number of stencil accesses outside the grid, or -1 on allocation failure. */
-int64_t orc64_run(double* state, int64_t n, const orc64_params* p, int substeps) {
+/* One substep on state (n x 15 doubles) in place; the grid g (grid_count x 4
+ * doubles, caller-owned) is left as updateGrid leaves it: per touched cell
+ * the velocity (or, where the mass is not positive, the raw momentum) and
+ * the mass.  Adds the number of stencil accesses outside the grid to *bad. */
+void orc64_substep(double* state, int64_t n, const orc64_params* p, double* g, int64_t* bad_out) {
     const int64_t gc = orc64_grid_count(p);
     const int32_t Y = d2i_sat(p->init_box[1]), Z = d2i_sat(p->init_box[2]);
-    double* g = (double*)malloc(sizeof(double) * 4 * (size_t)(gc > 0 ? gc : 1));
-    if (!g) return -1;
     int64_t bad = 0;
-    for (int sub = 0; sub < substeps; ++sub) {
+    {
         memset(g, 0, sizeof(double) * 4 * (size_t)gc);
         /* p2g_1 */
         for (int64_t i = 0; i < n; ++i) {
@@ -186,6 +186,17 @@ int64_t orc64_run(double* state, int64_t n, const orc64_params* p, int substeps)
             }
         }
     }
+    *bad_out += bad;
+}
+
+/* Runs `substeps` substeps on state (n x 15 doubles) in place.  Returns the
+ * number of stencil accesses outside the grid, or -1 on allocation failure. */
+int64_t orc64_run(double* state, int64_t n, const orc64_params* p, int substeps) {
+    const int64_t gc = orc64_grid_count(p);
+    double* g = (double*)malloc(sizeof(double) * 4 * (size_t)(gc > 0 ? gc : 1));
+    if (!g) return -1;
+    int64_t bad = 0;
+    for (int sub = 0; sub < substeps; ++sub) orc64_substep(state, n, p, g, &bad);
     free(g);
     return bad;
 }

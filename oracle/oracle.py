@@ -23,6 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "build")
 LIB_PATH = os.path.join(BUILD_DIR, "libmpm_oracle.so")
 SOURCES = [os.path.join(HERE, "mpm_oracle.c"), os.path.join(HERE, "mpm_oracle64.c"),
+           os.path.join(HERE, "mpm_adjoint64.c"),
            os.path.join(HERE, "render_oracle.c"), os.path.join(HERE, "sph_oracle.c")]
 
 # -ffp-contract=off: every float op rounds separately, as the WGSL restatement
@@ -238,6 +239,35 @@ def run64(state: np.ndarray, params: Params64, substeps: int) -> np.ndarray:
     if L.orc64_run(st, len(st), ctypes.byref(params), int(substeps)) < 0:
         raise MemoryError("orc64_run")
     return st
+
+
+def backward64(state0: np.ndarray, params: Params64, substeps: int, seeds: dict,
+               every: int = 20):
+    """FP64 tape adjoint on the CPU (mpm_adjoint64.c): gradient of a loss whose
+    adjoint seeds are `seeds` = {substep t: (n, 15) adjoint of the state
+    after t substeps}.  Returns (grad (n, 15) w.r.t. state0, [dL/d
+    stiffness, dL/d dynamic viscosity])."""
+    L = lib()
+    f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+    if not getattr(L, "_orc64_bwd_ready", False):
+        L.orc64_backward.argtypes = [f64p, ctypes.c_int64, ctypes.POINTER(Params64), ctypes.c_int,
+                                     ctypes.c_int, np.ctypeslib.ndpointer(np.int32),
+                                     f64p, ctypes.c_int, f64p, f64p]
+        L.orc64_backward.restype = ctypes.c_int
+        L._orc64_bwd_ready = True
+    st = np.ascontiguousarray(state0, dtype=np.float64)
+    n = len(st)
+    ts = sorted(int(t) for t in seeds)
+    vals = np.ascontiguousarray(np.stack([np.asarray(seeds[t], np.float64).reshape(n, 15)
+                                          for t in ts]) if ts else np.zeros((0, n, 15)))
+    grad = np.zeros((n, 15), np.float64)
+    pgrad = np.zeros(2, np.float64)
+    rc = L.orc64_backward(st, n, ctypes.byref(params), int(substeps), int(every),
+                          np.array(ts, np.int32), vals.reshape(-1) if vals.size else
+                          np.zeros(1), len(ts), grad, pgrad)
+    if rc != 0:
+        raise MemoryError("orc64_backward")
+    return grad, pgrad
 
 
 # ---------------------------------------------------------------------------
