@@ -389,6 +389,14 @@ int mpm_renderer_set_envmap(mpm_renderer* renderer, int face_size, const float* 
  * posvel_device = 32-byte records (mpm_posvel_device_ptr), asynchronous. */
 int mpm_renderer_execute(mpm_renderer* renderer, const void* posvel_device, int num_particles,
                          const mpm_render_uniforms* uniforms, void* stream);
+/* FluidRenderer.execute with sphereRenderFl true (fluidRender.ts:481-485,
+ * render/sphere.wgsl): every particle's billboard drawn as a lit sphere
+ * coloured by its speed, depth test 'less', over the clear colour
+ * (0.8, 0.8, 0.8, 1).  MPM_RENDER_COLOR / _COLOR8 then hold the image and
+ * MPM_RENDER_DEPTH the winning fragment depth (1 where none). */
+int mpm_renderer_execute_spheres(mpm_renderer* renderer, const void* posvel_device,
+                                 int num_particles, const mpm_render_uniforms* uniforms,
+                                 void* stream);
 /* Copies one of the MPM_RENDER_* images to host memory (synchronizes). */
 int mpm_renderer_download(mpm_renderer* renderer, int what, void* out);
 void* mpm_renderer_color_device_ptr(mpm_renderer* renderer);

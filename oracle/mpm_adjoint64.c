@@ -50,6 +50,23 @@ typedef struct orc64_params {
 
 int64_t orc64_grid_count(const orc64_params* p);
 void orc64_substep(double* state, int64_t n, const orc64_params* p, double* g, int64_t* bad);
+void orc32_substep(float* state, int64_t n, const orc64_params* p, float* g, int64_t* bad);
+
+
+/* One forward substep of the tape: in FP64, or (f32 != 0) in f32 through the
+ * float buffers sf (n x 15) and gf (grid), the result widened to double. */
+static void tape_substep(double* state, int64_t n, const orc64_params* p, double* g, int64_t* bad,
+                         int f32, float* sf, float* gf) {
+    if (!f32) {
+        orc64_substep(state, n, p, g, bad);
+        return;
+    }
+    const int64_t gc = orc64_grid_count(p);
+    for (int64_t q = 0; q < 15 * n; ++q) sf[q] = (float)state[q];
+    orc32_substep(sf, n, p, gf, bad);
+    for (int64_t q = 0; q < 15 * n; ++q) state[q] = (double)sf[q];
+    for (int64_t q = 0; q < 4 * gc; ++q) g[q] = (double)gf[q];
+}
 
 static int32_t sat_i32(double x) {
     if (x != x) return 0;
@@ -297,9 +314,23 @@ void orc64_substep_adjoint(const double* S, const double* G, const double* Aout,
  * state.  Outputs: grad (n x 15, dL/d state0) and pgrad[2] (dL/d stiffness,
  * dL/d dynamic viscosity).  every: checkpoint interval.  Returns 0, or -1 on
  * allocation failure. */
+int orc64_backward_tape(const double* state0, int64_t n, const orc64_params* p, int T, int every,
+                        const int* seed_t, const double* seed_vals, int nseeds, double* grad,
+                        double* pgrad, int f32);
+
 int orc64_backward(const double* state0, int64_t n, const orc64_params* p, int T, int every,
                    const int* seed_t, const double* seed_vals, int nseeds, double* grad,
                    double* pgrad) {
+    return orc64_backward_tape(state0, n, p, T, every, seed_t, seed_vals, nseeds, grad, pgrad, 0);
+}
+
+/* orc64_backward with the tape (the trajectory and its grids) integrated in
+ * f32 when f32 != 0 (the state widened to double between substeps, exactly);
+ * the reverse pass itself stays FP64.  The difference from orc64_backward is
+ * what an f32 trajectory costs the gradient. */
+int orc64_backward_tape(const double* state0, int64_t n, const orc64_params* p, int T, int every,
+                        const int* seed_t, const double* seed_vals, int nseeds, double* grad,
+                        double* pgrad, int f32) {
     if (every < 1) every = 1;
     const int64_t gc = orc64_grid_count(p);
     const size_t sbytes = sizeof(double) * 15 * (size_t)n;
@@ -312,8 +343,11 @@ int orc64_backward(const double* state0, int64_t n, const orc64_params* p, int T
     double* a = (double*)malloc(sbytes + 1);
     double* a2 = (double*)malloc(sbytes + 1);
     double* gadj = (double*)malloc(gbytes);
-    if (!ckpt || !tape_s || !tape_g || !work || !a || !a2 || !gadj) {
+    float* sf = f32 ? (float*)malloc(sbytes / 2 + 1) : NULL;
+    float* gf = f32 ? (float*)malloc(gbytes / 2 + 1) : NULL;
+    if (!ckpt || !tape_s || !tape_g || !work || !a || !a2 || !gadj || (f32 && (!sf || !gf))) {
         free(ckpt); free(tape_s); free(tape_g); free(work); free(a); free(a2); free(gadj);
+        free(sf); free(gf);
         return -1;
     }
     int64_t bad = 0;
@@ -321,7 +355,7 @@ int orc64_backward(const double* state0, int64_t n, const orc64_params* p, int T
     memcpy(work, state0, sbytes);
     for (int t = 0; t < T; ++t) {
         if (t % every == 0) memcpy(ckpt + 15 * (size_t)n * (t / every), work, sbytes);
-        orc64_substep(work, n, p, gadj, &bad);
+        tape_substep(work, n, p, gadj, &bad, f32, sf, gf);
     }
     pgrad[0] = pgrad[1] = 0.0;
     memset(a, 0, sbytes);
@@ -336,7 +370,7 @@ int orc64_backward(const double* state0, int64_t n, const orc64_params* p, int T
         memcpy(work, ckpt + 15 * (size_t)n * seg, sbytes);
         for (int t = t0; t < t1; ++t) {
             memcpy(tape_s + 15 * (size_t)n * (t - t0), work, sbytes);
-            orc64_substep(work, n, p, tape_g + 4 * (size_t)gc * (t - t0), &bad);
+            tape_substep(work, n, p, tape_g + 4 * (size_t)gc * (t - t0), &bad, f32, sf, gf);
         }
         for (int t = t1 - 1; t >= t0; --t) {
             orc64_substep_adjoint(tape_s + 15 * (size_t)n * (t - t0),
@@ -351,5 +385,6 @@ int orc64_backward(const double* state0, int64_t n, const orc64_params* p, int T
     }
     memcpy(grad, a, sbytes);
     free(ckpt); free(tape_s); free(tape_g); free(work); free(a); free(a2); free(gadj);
+    free(sf); free(gf);
     return 0;
 }

@@ -189,6 +189,151 @@ void orc64_substep(double* state, int64_t n, const orc64_params* p, double* g, i
     *bad_out += bad;
 }
 
+static void weights32(const float* x, float ci[3], float w[3][3]) {
+    for (int a = 0; a < 3; ++a) {
+        ci[a] = floorf(x[a]);
+        const float d = x[a] - (ci[a] + 0.5f);
+        w[a][0] = 0.5f * (0.5f - d) * (0.5f - d);
+        w[a][1] = 0.75f - d * d;
+        w[a][2] = 0.5f * (0.5f + d) * (0.5f + d);
+    }
+}
+
+/* The same substep with every value and grid sum in f32 (state n x 15
+ * floats, grid grid_count x 4 floats): the continuous model integrated in
+ * single precision, as the library's f32 tape integrates it (there the
+ * grid sums arrive in atomic order). */
+/* One substep on state (n x 15 floats) in place; the grid g (grid_count x 4
+ * floats, caller-owned) is left as updateGrid leaves it: per touched cell
+ * the velocity (or, where the mass is not positive, the raw momentum) and
+ * the mass.  Adds the number of stencil accesses outside the grid to *bad. */
+void orc32_substep(float* state, int64_t n, const orc64_params* p, float* g, int64_t* bad_out) {
+    const int64_t gc = orc64_grid_count(p);
+    const int32_t Y = d2i_sat(p->init_box[1]), Z = d2i_sat(p->init_box[2]);
+    int64_t bad = 0;
+    {
+        memset(g, 0, sizeof(float) * 4 * (size_t)gc);
+        /* p2g_1 */
+        for (int64_t i = 0; i < n; ++i) {
+            const float* P = state + 15 * i;
+            float ci[3], w[3][3];
+            weights32(P, ci, w);
+            for (int gx = 0; gx < 3; ++gx)
+                for (int gy = 0; gy < 3; ++gy)
+                    for (int gz = 0; gz < 3; ++gz) {
+                        const float wt = w[0][gx] * w[1][gy] * w[2][gz];
+                        const float c[3] = {ci[0] + gx - 1.0f, ci[1] + gy - 1.0f, ci[2] + gz - 1.0f};
+                        float d[3];
+                        for (int a = 0; a < 3; ++a) d[a] = (c[a] + 0.5f) - P[a];
+                        const int32_t idx = flat64(c[0], c[1], c[2], Y, Z);
+                        if (idx < 0 || idx >= gc) { ++bad; continue; }
+                        float* cell = g + 4 * (int64_t)idx;
+                        for (int r = 0; r < 3; ++r) {
+                            const float q = P[6 + r] * d[0] + P[9 + r] * d[1] + P[12 + r] * d[2];
+                            cell[r] += wt * (P[3 + r] + q);
+                        }
+                        cell[3] += wt;
+                    }
+        }
+        /* p2g_2 */
+        for (int64_t i = 0; i < n; ++i) {
+            const float* P = state + 15 * i;
+            float ci[3], w[3][3];
+            weights32(P, ci, w);
+            float rho = 0.0f;
+            for (int gx = 0; gx < 3; ++gx)
+                for (int gy = 0; gy < 3; ++gy)
+                    for (int gz = 0; gz < 3; ++gz) {
+                        const float wt = w[0][gx] * w[1][gy] * w[2][gz];
+                        const int32_t idx = flat64(ci[0] + gx - 1.0f, ci[1] + gy - 1.0f,
+                                                   ci[2] + gz - 1.0f, Y, Z);
+                        if (idx < 0 || idx >= gc) { ++bad; continue; }
+                        rho += g[4 * (int64_t)idx + 3] * wt;
+                    }
+            const float V = 1.0f / rho;
+            const float rr = rho / (float)p->rest_density;
+            const float pterm = (float)p->stiffness * (rr * rr * rr * rr * rr - 1.0f);
+            const float pres = pterm > 0.0f ? pterm : 0.0f;
+            float T[3][3]; /* [row][col] */
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    const float strain = P[6 + 3 * b + a] + P[6 + 3 * a + b];
+                    const float sig = (a == b ? -pres : 0.0f) + (float)p->dynamic_viscosity * strain;
+                    T[a][b] = -V * 4.0f * sig * (float)p->dt;
+                }
+            for (int gx = 0; gx < 3; ++gx)
+                for (int gy = 0; gy < 3; ++gy)
+                    for (int gz = 0; gz < 3; ++gz) {
+                        const float wt = w[0][gx] * w[1][gy] * w[2][gz];
+                        const float c[3] = {ci[0] + gx - 1.0f, ci[1] + gy - 1.0f, ci[2] + gz - 1.0f};
+                        float d[3];
+                        for (int a = 0; a < 3; ++a) d[a] = (c[a] + 0.5f) - P[a];
+                        const int32_t idx = flat64(c[0], c[1], c[2], Y, Z);
+                        if (idx < 0 || idx >= gc) { ++bad; continue; }
+                        float* cell = g + 4 * (int64_t)idx;
+                        for (int r = 0; r < 3; ++r)
+                            cell[r] += wt * (T[r][0] * d[0] + T[r][1] * d[1] + T[r][2] * d[2]);
+                    }
+        }
+        /* updateGrid */
+        int32_t hi[3];
+        for (int a = 0; a < 3; ++a) hi[a] = d2i_sat(ceil(p->real_box[a]) - 3.0);
+        for (int64_t j = 0; j < gc; ++j) {
+            float* cell = g + 4 * j;
+            if (!(cell[3] > 0.0f)) continue;
+            const int32_t id = (int32_t)j;
+            const int32_t xyz[3] = {(id / Z) / Y, (id / Z) % Y, id % Z};
+            for (int a = 0; a < 3; ++a) {
+                float v = cell[a] / cell[3] + (float)p->gravity[a] * (float)p->dt;
+                if (xyz[a] < 2 || xyz[a] > hi[a]) v = 0.0f;
+                cell[a] = v;
+            }
+        }
+        /* g2p */
+        for (int64_t i = 0; i < n; ++i) {
+            float* P = state + 15 * i;
+            float ci[3], w[3][3];
+            weights32(P, ci, w);
+            float v[3] = {0.0f, 0.0f, 0.0f}, B[3][3] = {{0}}; /* B[c][r] */
+            for (int gx = 0; gx < 3; ++gx)
+                for (int gy = 0; gy < 3; ++gy)
+                    for (int gz = 0; gz < 3; ++gz) {
+                        const float wt = w[0][gx] * w[1][gy] * w[2][gz];
+                        const float c[3] = {ci[0] + gx - 1.0f, ci[1] + gy - 1.0f, ci[2] + gz - 1.0f};
+                        float d[3];
+                        for (int a = 0; a < 3; ++a) d[a] = (c[a] + 0.5f) - P[a];
+                        const int32_t idx = flat64(c[0], c[1], c[2], Y, Z);
+                        float gv[3] = {0.0f, 0.0f, 0.0f};
+                        if (idx < 0 || idx >= gc) ++bad;
+                        else for (int a = 0; a < 3; ++a) gv[a] = g[4 * (int64_t)idx + a];
+                        for (int r = 0; r < 3; ++r) {
+                            const float wv = gv[r] * wt;
+                            for (int cc = 0; cc < 3; ++cc) B[cc][r] += wv * d[cc];
+                            v[r] += wv;
+                        }
+                    }
+            for (int cc = 0; cc < 3; ++cc)
+                for (int r = 0; r < 3; ++r) P[6 + 3 * cc + r] = B[cc][r] * 4.0f;
+            for (int a = 0; a < 3; ++a) {
+                float x = P[a] + v[a] * (float)p->dt;
+                const float lo = 1.0f, hw = (float)p->real_box[a] - 2.0f;
+                x = x < lo ? lo : x;
+                x = x > hw ? hw : x;
+                P[a] = x;
+            }
+            for (int a = 0; a < 3; ++a) {
+                const float xn = P[a] + v[a] * (float)p->dt * 3.0f;
+                const float wmax = (float)p->real_box[a] - 4.0f;
+                float va = v[a];
+                if (xn < 3.0f) va += 0.3f * (3.0f - xn);
+                if (xn > wmax) va += 0.3f * (wmax - xn);
+                P[3 + a] = va;
+            }
+        }
+    }
+    *bad_out += bad;
+}
+
 /* Runs `substeps` substeps on state (n x 15 doubles) in place.  Returns the
  * number of stencil accesses outside the grid, or -1 on allocation failure. */
 int64_t orc64_run(double* state, int64_t n, const orc64_params* p, int substeps) {

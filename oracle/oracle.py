@@ -242,18 +242,20 @@ def run64(state: np.ndarray, params: Params64, substeps: int) -> np.ndarray:
 
 
 def backward64(state0: np.ndarray, params: Params64, substeps: int, seeds: dict,
-               every: int = 20):
+               every: int = 20, f32_tape: bool = False):
     """FP64 tape adjoint on the CPU (mpm_adjoint64.c): gradient of a loss whose
     adjoint seeds are `seeds` = {substep t: (n, 15) adjoint of the state
     after t substeps}.  Returns (grad (n, 15) w.r.t. state0, [dL/d
-    stiffness, dL/d dynamic viscosity])."""
+    stiffness, dL/d dynamic viscosity]).  f32_tape: the trajectory is
+    integrated in f32 (the reverse pass stays FP64)."""
     L = lib()
     f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
     if not getattr(L, "_orc64_bwd_ready", False):
-        L.orc64_backward.argtypes = [f64p, ctypes.c_int64, ctypes.POINTER(Params64), ctypes.c_int,
-                                     ctypes.c_int, np.ctypeslib.ndpointer(np.int32),
-                                     f64p, ctypes.c_int, f64p, f64p]
-        L.orc64_backward.restype = ctypes.c_int
+        L.orc64_backward_tape.argtypes = [f64p, ctypes.c_int64, ctypes.POINTER(Params64),
+                                          ctypes.c_int, ctypes.c_int,
+                                          np.ctypeslib.ndpointer(np.int32), f64p, ctypes.c_int,
+                                          f64p, f64p, ctypes.c_int]
+        L.orc64_backward_tape.restype = ctypes.c_int
         L._orc64_bwd_ready = True
     st = np.ascontiguousarray(state0, dtype=np.float64)
     n = len(st)
@@ -262,9 +264,9 @@ def backward64(state0: np.ndarray, params: Params64, substeps: int, seeds: dict,
                                           for t in ts]) if ts else np.zeros((0, n, 15)))
     grad = np.zeros((n, 15), np.float64)
     pgrad = np.zeros(2, np.float64)
-    rc = L.orc64_backward(st, n, ctypes.byref(params), int(substeps), int(every),
-                          np.array(ts, np.int32), vals.reshape(-1) if vals.size else
-                          np.zeros(1), len(ts), grad, pgrad)
+    rc = L.orc64_backward_tape(st, n, ctypes.byref(params), int(substeps), int(every),
+                               np.array(ts, np.int32), vals.reshape(-1) if vals.size else
+                               np.zeros(1), len(ts), grad, pgrad, int(bool(f32_tape)))
     if rc != 0:
         raise MemoryError("orc64_backward")
     return grad, pgrad
@@ -303,6 +305,11 @@ def _render_lib():
         L.ro_sample_cube.argtypes = [f32p, ctypes.c_int, ctypes.c_float, ctypes.c_float,
                                      ctypes.c_float, f32p]
         L.ro_sample_cube.restype = None
+        L.ro_splat.argtypes = [f32p, ctypes.c_int64, f32p, ctypes.c_int, ctypes.c_int, f32p, f32p]
+        L.ro_splat.restype = ctypes.c_int
+        L.ro_sphere.argtypes = [f32p, ctypes.c_int64, f32p, ctypes.c_int, ctypes.c_int, f32p, u8p,
+                                f32p]
+        L.ro_sphere.restype = ctypes.c_int
         L._ro_ready = True
     return L
 
@@ -324,6 +331,34 @@ def render(posvel: np.ndarray, uniforms_f32: np.ndarray, width: int, height: int
     if L.ro_render(pv, len(pv), u, width, height, dt, mf, ppc, e, e.shape[1], out["color"],
                    out["color8"], out["depth"], out["thickness"]) != 0:
         raise MemoryError("ro_render")
+    return out
+
+
+def splat(posvel: np.ndarray, uniforms_f32: np.ndarray, width: int, height: int) -> dict:
+    """The depth and thickness splats alone (before the filters): depth =
+    view-space z of the nearest fragment (0 where none), thickness rounded to
+    half."""
+    L = _render_lib()
+    pv = np.ascontiguousarray(posvel, dtype=np.float32).reshape(-1, 8)
+    u = np.ascontiguousarray(uniforms_f32, dtype=np.float32).reshape(68)
+    out = {"depth": np.zeros((height, width), np.float32),
+           "thickness": np.zeros((height, width), np.float32)}
+    if L.ro_splat(pv, len(pv), u, width, height, out["depth"], out["thickness"]) != 0:
+        raise MemoryError("ro_splat")
+    return out
+
+
+def sphere(posvel: np.ndarray, uniforms_f32: np.ndarray, width: int, height: int) -> dict:
+    """Sphere mode (render/sphere.wgsl): colour, its rgba8 store and the
+    winning fragment depth (1 where none)."""
+    L = _render_lib()
+    pv = np.ascontiguousarray(posvel, dtype=np.float32).reshape(-1, 8)
+    u = np.ascontiguousarray(uniforms_f32, dtype=np.float32).reshape(68)
+    out = {"color": np.zeros((height, width, 4), np.float32),
+           "color8": np.zeros((height, width, 4), np.uint8),
+           "depth": np.zeros((height, width), np.float32)}
+    if L.ro_sphere(pv, len(pv), u, width, height, out["color"], out["color8"], out["depth"]) != 0:
+        raise MemoryError("ro_sphere")
     return out
 
 

@@ -15,6 +15,7 @@
  * the shader math of
  *   depthMap.wgsl:34-79      billboard depth splat, 'less' depth test
  *   thicknessMap.wgsl:27-62  additive thickness splat
+ *   sphere.wgsl:37-110       sphere mode (ro_sphere)
  *   bilateral.wgsl:18-75     separable bilateral depth filter (4 x X, Y)
  *   gaussian.wgsl:14-42      separable gaussian thickness filter (X, Y)
  *   fluid.wgsl:19-98         shading
@@ -391,18 +392,16 @@ static void shade_pass(const float* d0, const float* t0, const ro_uniforms* u, c
         }
 }
 
-int ro_render(const float* posvel, int64_t n, const ro_uniforms* u, int W, int H,
-              float depth_threshold, float max_filter_size, float ppc, const float* env,
-              int env_size, float* color, uint8_t* color8, float* depth_out, float* thick_out) {
+/* The depth and thickness splats and the depth resolve (depthMap.wgsl,
+ * thicknessMap.wgsl): d0 = view-space z of the nearest fragment (0 where
+ * none), t0 = the additive thickness rounded to half. */
+static int splat(const float* posvel, int64_t n, const ro_uniforms* u, int W, int H, float* d0,
+                 float* t0) {
     const size_t np = (size_t)W * H;
     uint64_t* dkey = (uint64_t*)malloc(8 * np);
     int64_t* tacc = (int64_t*)calloc(np, 8);
-    float* d0 = (float*)malloc(4 * np);
-    float* d1 = (float*)malloc(4 * np);
-    float* t0 = (float*)malloc(4 * np);
-    float* t1 = (float*)malloc(4 * np);
-    if (!dkey || !tacc || !d0 || !d1 || !t0 || !t1) {
-        free(dkey); free(tacc); free(d0); free(d1); free(t0); free(t1);
+    if (!dkey || !tacc) {
+        free(dkey); free(tacc);
         return -1;
     }
     const uint64_t clear_key = ((uint64_t)0x3f800000u << 32) | 0xffffffffu;
@@ -437,6 +436,27 @@ int ro_render(const float* posvel, int64_t n, const ro_uniforms* u, int W, int H
         d0[p] = d;
         t0[p] = half_round((float)tacc[p] * 2.3283064365386963e-10f);
     }
+    free(dkey); free(tacc);
+    return 0;
+}
+
+int ro_splat(const float* posvel, int64_t n, const ro_uniforms* u, int W, int H, float* depth_out,
+             float* thick_out) {
+    return splat(posvel, n, u, W, H, depth_out, thick_out);
+}
+
+int ro_render(const float* posvel, int64_t n, const ro_uniforms* u, int W, int H,
+              float depth_threshold, float max_filter_size, float ppc, const float* env,
+              int env_size, float* color, uint8_t* color8, float* depth_out, float* thick_out) {
+    const size_t np = (size_t)W * H;
+    float* d0 = (float*)malloc(4 * np);
+    float* d1 = (float*)malloc(4 * np);
+    float* t0 = (float*)malloc(4 * np);
+    float* t1 = (float*)malloc(4 * np);
+    if (!d0 || !d1 || !t0 || !t1 || splat(posvel, n, u, W, H, d0, t0) != 0) {
+        free(d0); free(d1); free(t0); free(t1);
+        return -1;
+    }
     /* bilateral depth filter, 4 x (X, Y) */
     for (int it = 0; it < 8; ++it)
         bilateral_pass((it & 1) ? d1 : d0, (it & 1) ? d0 : d1, W, H, (it & 1) ? 0 : 1,
@@ -448,7 +468,86 @@ int ro_render(const float* posvel, int64_t n, const ro_uniforms* u, int W, int H
     shade_pass(d0, t0, u, env, env_size, W, H, color, color8);
     memcpy(depth_out, d0, 4 * np);
     memcpy(thick_out, t0, 4 * np);
-    free(dkey); free(tacc); free(d0); free(d1); free(t0); free(t1);
+    free(d0); free(d1); free(t0); free(t1);
+    return 0;
+}
+
+/* sphere.wgsl:67-90 value_to_color. */
+static v3 value_to_color(float value) {
+    const v3 col[5] = {mk(0.0f, 0.4f, 0.8f), mk(35.0f / 256.0f, 161.0f / 256.0f, 165.0f / 256.0f),
+                       mk(95.0f / 256.0f, 254.0f / 256.0f, 150.0f / 256.0f),
+                       mk(243.0f / 256.0f, 250.0f / 256.0f, 49.0f / 256.0f),
+                       mk(255.0f / 256.0f, 165.0f / 256.0f, 0.0f / 256.0f)};
+    int k;
+    float t;
+    if (0.0f <= value && value < 0.25f) { k = 0; t = value / 0.25f; }
+    else if (0.25f <= value && value < 0.50f) { k = 1; t = (value - 0.25f) / 0.25f; }
+    else if (0.50f <= value && value < 0.75f) { k = 2; t = (value - 0.50f) / 0.25f; }
+    else { k = 3; t = (value - 0.75f) / 0.25f; }
+    const float om = 1.0f - t;  /* mix(a, b, t) = a * (1 - t) + b * t */
+    return mk(col[k].x * om + col[k + 1].x * t, col[k].y * om + col[k + 1].y * t,
+              col[k].z * om + col[k + 1].z * t);
+}
+
+/* Sphere mode (render/sphere.wgsl, render/fluidRender.ts:481-485): each
+ * particle's billboard shaded as a lit sphere coloured by its speed, with
+ * the depth test 'less' (first-drawn fragment wins ties) over the clear
+ * colour (0.8, 0.8, 0.8, 1).  color: W*H*4 floats, color8 its rgba8unorm
+ * store, depth_out: the winning frag_depth (1 where none). */
+int ro_sphere(const float* posvel, int64_t n, const ro_uniforms* u, int W, int H, float* color,
+              uint8_t* color8, float* depth_out) {
+    const size_t np = (size_t)W * H;
+    uint64_t* dkey = (uint64_t*)malloc(8 * np);
+    if (!dkey) return -1;
+    const uint64_t clear_key = ((uint64_t)0x3f800000u << 32) | 0xffffffffu;
+    for (size_t p = 0; p < np; ++p) dkey[p] = clear_key;
+    for (int64_t i = 0; i < n; ++i) {
+        billboard_t b;
+        if (!billboard(posvel, i, u, W, H, &b)) continue;
+        for (int py = b.y0; py <= b.y1; ++py)
+            for (int px = b.x0; px <= b.x1; ++px) {
+                frag_t f;
+                if (!fragment(&b, px, py, u, &f)) continue;
+                const size_t p = (size_t)py * W + px;
+                if (f.depth < 1.0f) {
+                    const uint64_t key = ((uint64_t)bitsf(f.depth) << 32) | (uint32_t)i;
+                    if (key < dkey[p]) dkey[p] = key;
+                }
+            }
+    }
+    const float inv_len = 1.0f / sqrtf(3.0f);  /* normalize(vec3(1.0, 1.0, 1.0)) */
+    for (size_t p = 0; p < np; ++p) {
+        v3 col = mk(0.8f, 0.8f, 0.8f);
+        float depth = 1.0f;
+        if (dkey[p] != clear_key) {
+            const int64_t i = (int64_t)(dkey[p] & 0xffffffffu);
+            billboard_t b;
+            frag_t f;
+            if (billboard(posvel, i, u, W, H, &b) &&
+                fragment(&b, (int)(p % W), (int)(p / W), u, &f)) {
+                const float* pv = posvel + 8 * i;
+                const v3 v = mk(pv[4], pv[5], pv[6]);
+                const float speed = sqrtf(vdot(v, v));
+                const float cx = (float)(p % W) + 0.5f, cy = (float)(p / W) + 0.5f;
+                const float nx = ((cx - b.fxm) / (b.fxp - b.fxm)) * 2.0f - 1.0f;
+                const float ny = ((cy - b.fym) / (b.fyp - b.fym)) * 2.0f - 1.0f;
+                const float diffuse =
+                    wmax(0.0f, vdot(mk(nx, ny, f.nz), mk(inv_len, inv_len, inv_len)));
+                const v3 c = value_to_color(speed / 1.5f);
+                col = vscale(c, diffuse);
+                depth = f.depth;
+            }
+        }
+        const float cv[3] = {col.x, col.y, col.z};
+        for (int k = 0; k < 3; ++k) {
+            color[4 * p + k] = cv[k];
+            color8[4 * p + k] = cv[k] != cv[k] ? 0 : (uint8_t)rintf(wmin(wmax(cv[k], 0.0f), 1.0f) * 255.0f);
+        }
+        color[4 * p + 3] = 1.0f;
+        color8[4 * p + 3] = 255;
+        depth_out[p] = depth;
+    }
+    free(dkey);
     return 0;
 }
 

@@ -355,7 +355,7 @@ class Parser:
             self.expect(")")
             body = self.block()
             return ("for", init, cond, upd, body)
-        if t[1] in ("continue", "break"):
+        if t[1] in ("continue", "break", "discard"):
             self.next()
             self.expect(";")
             return (t[1],)
@@ -483,6 +483,14 @@ class BreakSignal(Exception):
     pass
 
 
+class DiscardSignal(Exception):
+    """A fragment invocation executed `discard`: its entry point returns the
+    DISCARDED marker instead of a value."""
+
+
+DISCARDED = "discarded"
+
+
 SWZ = {"x": 0, "y": 1, "z": 2, "w": 3, "r": 0, "g": 1, "b": 2, "a": 3}
 
 # exp(x) for f32 x; a fixture generator installs the project's restatement
@@ -574,6 +582,8 @@ class Module:
                 body(env)
             except ReturnSignal as r:
                 return r.value
+            except DiscardSignal:
+                return DISCARDED
             return None
 
         self.compiled[name] = (run, ret, params)
@@ -665,6 +675,10 @@ class Module:
         if k == "break":
             def run(env):
                 raise BreakSignal()
+            return run
+        if k == "discard":
+            def run(env):
+                raise DiscardSignal()
             return run
         if k == "return":
             if s[1] is None:
@@ -911,16 +925,30 @@ class Module:
                 "mat3x3f": mat(TF32), "f32": TF32, "i32": TI32, "u32": TU32}
         if name in ctor:
             return self.construct(ctor[name], args, scope)
+        if name in self.structs:
+            st = self.structs[name]
+            fields = [(f, self.coerce(*self.compile_expr(a, scope), ft))
+                      for (f, ft), a in zip(st.fields, args)]
+            return (lambda env: {f: _copy(ev(env)) for f, ev in fields}), st
         evs = [self.compile_expr(a, scope) for a in args]
-        if name == "vec3":
+        if name in ("vec2", "vec3", "vec4"):
             # element type inferred from the components; an abstract float
-            # vector concretises to vec3f, an abstract int one to vec3i
+            # vector concretises to an f32 vector, an abstract int one to i32
+            # (every abstract value these shaders build is exact in f32)
+            n = int(name[3])
             kinds = {scalar_of(t).kind for _, t in evs}
             if kinds & {"f32", "absfloat"}:
-                return self.construct(vec(TF32), args, scope)
+                return self.construct(vec(TF32, n), args, scope)
             if "u32" in kinds:
-                return self.construct(vec(TU32), args, scope)
-            return self.construct(vec(TI32), args, scope)
+                return self.construct(vec(TU32, n), args, scope)
+            return self.construct(vec(TI32, n), args, scope)
+        if name == "array":
+            # array(e0, e1, ...): the elements' (concretised) common type
+            et = evs[0][1]
+            if is_abstract(et) or (et.kind == "vec" and is_abstract(et.elem)):
+                et = self.concretize(et)
+            conv = [self.coerce(v, t, et) for v, t in evs]
+            return (lambda env: [c(env) for c in conv]), T("array", et, len(conv))
         if name == "abs":
             (v, t), = evs
             if t.kind == "vec":

@@ -159,3 +159,38 @@ def test_render_reads_the_simulator_buffer(cuda, pkg):
     assert (r.download("depth") != 0).any()
     r.close()
     sim.close()
+
+
+def test_sphere_mode_matches_restatement(cuda, pkg, oracle_mod):
+    """FluidRenderer.execute(..., sphereRenderFl=True) (render/sphere.wgsl)
+    against the restatement, which reproduces the reference's sphere shader
+    run through the WGSL interpreter (tests/golden/render_splats.npz): the
+    fixture's own scene and camera, then a simulated dam-break."""
+    import os
+    import torch
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "render_splats.npz"))
+    H, W = g["sphere_depth"].shape
+    u = pkg._lib.RenderUniforms.from_buffer_copy(g["uniforms"].astype(np.float32).tobytes())
+    r = pkg.FluidRenderer(W, H, RADIUS, FOV)
+    dev = torch.from_numpy(np.ascontiguousarray(g["posvel"], dtype=np.float32)).cuda()
+    r.execute(dev, len(g["posvel"]), u, sphereRenderFl=True)
+    same_bits(r.download("color"), g["sphere_color"], "sphere colour vs reference shader")
+    same_bits(r.download("depth"), g["sphere_depth"], "sphere depth vs reference shader")
+    r.close()
+    # a simulated scene at another size
+    sim = pkg.MLSMPMSimulator(None, None, 2 * RADIUS, maxParticles=20000, seed=4)
+    sim.reset(20000, [40.0, 30.0, 60.0])
+    for _ in range(20):
+        sim.execute()
+    sim.synchronize()
+    pv = sim.downloadPosvel()
+    W, H = 160, 96
+    u = pkg.camera_uniforms(W, H, 60.0, [20.0, 10.0, 30.0], FOV, 2 * RADIUS)
+    r = pkg.FluidRenderer(W, H, RADIUS, FOV)
+    r.execute(sim, sim.numParticles, u, sphereRenderFl=True)
+    want = oracle_mod.sphere(pv, uniforms_f32(u), W, H)
+    for k in ("color", "color8", "depth"):
+        same_bits(r.download(k), want[k], f"sphere {k}")
+    assert (want["depth"] < 1).mean() > 0.03
+    r.close()
+    sim.close()

@@ -154,3 +154,43 @@ fn fs(input: FragmentInput) -> @location(0) vec4f {
     out = run({"texture": img}, {"uv": (F32(0), F32(0)), "iuv": (F32(1.5), F32(1.5))})
     # x = 1 - 3 -> negative -> u32 0; x = 1 + 3 = 4 -> beyond the edge -> 3
     assert out[0] == img[1, 0] and out[1] == img[1, 3] and out[3] == 1.0
+
+
+def test_vertex_and_fragment_features():
+    """What the billboard shaders (render/depthMap.wgsl, thicknessMap.wgsl,
+    sphere.wgsl) need: an array value built by array(...), inferred vec2 /
+    vec4 constructors, struct constructors as return values, builtin vertex
+    inputs, a struct fragment input and output, and discard."""
+    src = """
+struct VOut { @builtin(position) position: vec4f, @location(0) uv: vec2f, }
+struct FIn { @location(0) uv: vec2f, }
+struct FOut { @location(0) color: vec4f, @builtin(frag_depth) depth: f32, }
+@vertex
+fn vs(@builtin(vertex_index) vi: u32, @builtin(instance_index) ii: u32) -> VOut {
+    var corners = array(vec2(0.5, 0.5), vec2(0.5, -0.5), vec2(-0.5, -0.5));
+    let c = corners[vi] * 2.0;
+    return VOut(vec4(c, f32(ii), 1.0), corners[vi] + 0.5);
+}
+@fragment
+fn fs(input: FIn) -> FOut {
+    var out: FOut;
+    let r2 = dot(input.uv, input.uv);
+    if (r2 > 1.0) {
+        discard;
+    }
+    out.depth = r2 * 0.5;
+    out.color = vec4(input.uv, r2, 1.);
+    return out;
+}
+"""
+    m = W.Module(src, {})
+    vs, _, _ = m.entry("vs")
+    fs, _, _ = m.entry("fs")
+    o = vs({}, 2, 7)
+    assert o["position"] == (F32(-1.0), F32(-1.0), F32(7.0), F32(1.0))
+    assert o["uv"] == (F32(0.0), F32(0.0))
+    assert fs({}, {"uv": (F32(1.0), F32(1.0))}) == W.DISCARDED
+    r = fs({}, {"uv": (F32(0.5), F32(0.25))})
+    r2 = F32(F32(F32(0.5) * F32(0.5)) + F32(F32(0.25) * F32(0.25)))
+    assert r["depth"] == F32(r2 * F32(0.5))
+    assert r["color"] == (F32(0.5), F32(0.25), r2, F32(1.0))

@@ -190,6 +190,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "mpm_renderer_destroy": (i32, [vp]),
         "mpm_renderer_set_envmap": (i32, [vp, i32, fp]),
         "mpm_renderer_execute": (i32, [vp, vp, i32, ctypes.POINTER(RenderUniforms), vp]),
+        "mpm_renderer_execute_spheres": (i32, [vp, vp, i32, ctypes.POINTER(RenderUniforms), vp]),
         "mpm_renderer_download": (i32, [vp, i32, vp]),
         "mpm_renderer_color_device_ptr": (vp, [vp]),
         "mpm_sph_create": (i32, [i32, f32, vp, ctypes.c_size_t, ctypes.POINTER(vp)]),

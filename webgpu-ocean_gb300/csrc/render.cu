@@ -14,6 +14,10 @@
 //                     [gaussian.wgsl:14-42]
 //   k_shade           normals, lighting, fresnel, transmittance, cube-map
 //                     reflection [fluid.wgsl:37-98]
+// and, for the sphere mode (sphereRenderFl, fluidRender.ts:481-485):
+//   k_sphere_splat    the depth test of every billboard [sphere.wgsl:37-64]
+//   k_sphere_shade    the winning particle's lit sphere, coloured by speed
+//                     [sphere.wgsl:67-110]
 //
 // Rasterisation, restated for these billboards: with a perspective matrix
 // without skew all four corners of a billboard share their clip w, so the
@@ -380,6 +384,85 @@ __global__ void k_shade(const float* __restrict__ depth_map, const float* __rest
     out8[p] = make_uchar4(u8(col.x), u8(col.y), u8(col.z), 255);
 }
 
+// Sphere mode (render/sphere.wgsl, fluidRender.ts:481-485): the depth test
+// alone, then each pixel shaded from the winning particle.
+__global__ void __launch_bounds__(128) k_sphere_splat(const float4* __restrict__ posvel, int n,
+                                                      Uni u, Consts c,
+                                                      unsigned long long* __restrict__ dkey) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Billboard b;
+    if (!billboard(posvel, i, u, c, b)) return;
+    for (int py = b.y0; py <= b.y1; ++py)
+        for (int px = b.x0; px <= b.x1; ++px) {
+            Frag f;
+            if (!fragment(b, px, py, u, f)) continue;
+            if (f.depth < 1.0f)
+                atomicMin(dkey + (size_t)py * c.W + px,
+                          ((unsigned long long)__float_as_uint(f.depth) << 32) | (unsigned)i);
+        }
+}
+
+// sphere.wgsl:67-90 value_to_color: mix(col_k, col_k+1, t) = a*(1-t) + b*t.
+__device__ __forceinline__ V3 value_to_color(float value) {
+    float a[3], bb[3], t;
+    if (0.0f <= value && value < 0.25f) {
+        a[0] = 0.0f; a[1] = 0.4f; a[2] = 0.8f;
+        bb[0] = 35.0f / 256.0f; bb[1] = 161.0f / 256.0f; bb[2] = 165.0f / 256.0f;
+        t = dvd(value, 0.25f);
+    } else if (0.25f <= value && value < 0.50f) {
+        a[0] = 35.0f / 256.0f; a[1] = 161.0f / 256.0f; a[2] = 165.0f / 256.0f;
+        bb[0] = 95.0f / 256.0f; bb[1] = 254.0f / 256.0f; bb[2] = 150.0f / 256.0f;
+        t = dvd(sub(value, 0.25f), 0.25f);
+    } else if (0.50f <= value && value < 0.75f) {
+        a[0] = 95.0f / 256.0f; a[1] = 254.0f / 256.0f; a[2] = 150.0f / 256.0f;
+        bb[0] = 243.0f / 256.0f; bb[1] = 250.0f / 256.0f; bb[2] = 49.0f / 256.0f;
+        t = dvd(sub(value, 0.50f), 0.25f);
+    } else {
+        a[0] = 243.0f / 256.0f; a[1] = 250.0f / 256.0f; a[2] = 49.0f / 256.0f;
+        bb[0] = 255.0f / 256.0f; bb[1] = 165.0f / 256.0f; bb[2] = 0.0f;
+        t = dvd(sub(value, 0.75f), 0.25f);
+    }
+    const float om = sub(1.0f, t);
+    return v3(add(mul(a[0], om), mul(bb[0], t)), add(mul(a[1], om), mul(bb[1], t)),
+              add(mul(a[2], om), mul(bb[2], t)));
+}
+
+__global__ void k_sphere_shade(const float4* __restrict__ posvel, Uni u, Consts c,
+                               const unsigned long long* __restrict__ dkey,
+                               float4* __restrict__ out, uchar4* __restrict__ out8,
+                               float* __restrict__ depth) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= c.W * c.H) return;
+    const unsigned long long key = dkey[p];
+    V3 col = v3(0.8f, 0.8f, 0.8f);  // the sphere pass's clear colour (fluidRender.ts:425)
+    float d = 1.0f;
+    if (key != kClearKey) {
+        Billboard b;
+        Frag f;
+        const int i = (int)(key & 0xffffffffull);
+        const int px = p % c.W, py = p / c.W;
+        if (billboard(posvel, i, u, c, b) && fragment(b, px, py, u, f)) {
+            const float4 v = posvel[2 * (size_t)i + 1];
+            const float speed = __fsqrt_rn(vdot(v3(v.x, v.y, v.z), v3(v.x, v.y, v.z)));
+            const float cx = add((float)px, 0.5f), cy = add((float)py, 0.5f);
+            const float nx = sub(mul(dvd(sub(cx, b.fxm), sub(b.fxp, b.fxm)), 2.0f), 1.0f);
+            const float ny = sub(mul(dvd(sub(cy, b.fym), sub(b.fyp, b.fym)), 2.0f), 1.0f);
+            const float inv_len = dvd(1.0f, __fsqrt_rn(3.0f));  // normalize(vec3(1, 1, 1))
+            const float diffuse = wmax(0.0f, vdot(v3(nx, ny, f.nz), v3(inv_len, inv_len, inv_len)));
+            col = vscale(value_to_color(dvd(speed, 1.5f)), diffuse);
+            d = f.depth;
+        }
+    }
+    out[p] = make_float4(col.x, col.y, col.z, 1.0f);
+    auto u8 = [](float x) -> unsigned char {
+        if (x != x) return 0;
+        return (unsigned char)rintf(mul(wmin(wmax(x, 0.0f), 1.0f), 255.0f));
+    };
+    out8[p] = make_uchar4(u8(col.x), u8(col.y), u8(col.z), 255);
+    depth[p] = d;
+}
+
 int fail(int code, const std::string& msg) {
     mpm::set_last_error(msg);
     return code;
@@ -560,6 +643,24 @@ int mpm_renderer_execute(mpm_renderer* r, const void* posvel, int n,
                                 r->color8);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "mpm_renderer_execute");
+    return MPM_OK;
+}
+
+int mpm_renderer_execute_spheres(mpm_renderer* r, const void* posvel, int n,
+                                 const mpm_render_uniforms* uniforms, void* stream) {
+    if (!r || !uniforms || n < 0 || (n > 0 && !posvel)) return fail(MPM_E_INVALID, "bad arguments");
+    Uni u;
+    std::memcpy(&u, uniforms, sizeof(Uni));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const Consts& c = r->c;
+    const int npix = c.W * c.H;
+    const int pb = (npix + 255) / 256;
+    const float4* pv = static_cast<const float4*>(posvel);
+    k_clear<<<pb, 256, 0, st>>>(r->dkey, r->tacc, npix);
+    if (n > 0) k_sphere_splat<<<(n + 127) / 128, 128, 0, st>>>(pv, n, u, c, r->dkey);
+    k_sphere_shade<<<pb, 256, 0, st>>>(pv, u, c, r->dkey, r->color, r->color8, r->depth[0]);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "mpm_renderer_execute_spheres");
     return MPM_OK;
 }
 

@@ -88,18 +88,22 @@ class FluidRenderer:
                "setEnvmap")
 
     def execute(self, posvel, numParticles: int, uniforms: L.RenderUniforms,
-                commandEncoder=None) -> None:
-        """posvel: a device pointer (int), a simulator (its posvel buffer) or a
-        CUDA tensor of 32-byte records."""
+                commandEncoder=None, sphereRenderFl: bool = False) -> None:
+        """FluidRenderer.execute (render/fluidRender.ts:292-488).  posvel: a
+        device pointer (int), a simulator (its posvel buffer) or a CUDA tensor
+        of 32-byte records.  sphereRenderFl: draw every particle as a lit
+        sphere coloured by its speed (render/sphere.wgsl) instead of the
+        fluid surface."""
         if hasattr(posvel, "posvelDevicePtr"):
             ptr = posvel.posvelDevicePtr()
         elif hasattr(posvel, "data_ptr"):
             ptr = int(posvel.data_ptr())
         else:
             ptr = int(posvel)
-        _check(self._lib.mpm_renderer_execute(self._handle, ctypes.c_void_p(ptr), int(numParticles),
-                                              ctypes.byref(uniforms),
-                                              _stream_handle(commandEncoder)), "execute")
+        fn = (self._lib.mpm_renderer_execute_spheres if sphereRenderFl
+              else self._lib.mpm_renderer_execute)
+        _check(fn(self._handle, ctypes.c_void_p(ptr), int(numParticles), ctypes.byref(uniforms),
+                  _stream_handle(commandEncoder)), "execute")
 
     def download(self, what: str = "color") -> np.ndarray:
         h, w = self.height, self.width
