@@ -115,7 +115,10 @@ def test_adjoint_differentiable_config(cuda, pkg, oracle_mod):
     T = 200
     L, grad, pgrad = run_gradient(pkg, recs, box, T, 20)
     assert np.isfinite(grad).all() and np.isfinite(pgrad).all()
-    check_against_fd(oracle_mod, recs, box, T, grad, pgrad, (1e-4, 3e-5, 1e-5), 1e-3, ndir=1)
+    # four state-space directions (two in velocity, one each in position and
+    # C) plus both parameters; the median over eps is the reference, and the
+    # report carries each eps's value (eps = 1e-4 first)
+    check_against_fd(oracle_mod, recs, box, T, grad, pgrad, (1e-4, 3e-5, 1e-5), 1e-3, ndir=4)
 
 
 def test_fixed_point_tape_short_horizon(cuda, pkg, oracle_mod):
@@ -351,3 +354,44 @@ def test_contiguous_seed_block_abi(cuda, pkg):
     assert rc == 0
     np.testing.assert_allclose(grad, g_list, rtol=1e-4, atol=1e-5 * float(np.abs(g_list).max()))
     np.testing.assert_allclose(pgrad, p_list, rtol=1e-4)
+
+
+@pytest.mark.parametrize("T,every", [(1, 1), (12, 5), (40, 10)])
+def test_backward_matches_cpu_tape_adjoint(cuda, pkg, oracle_mod, T, every):
+    """The library's backward on the FP64 tape against the independent FP64
+    tape adjoint on the CPU (oracle/mpm_adjoint64.c): the same trajectory,
+    the same seeds (random adjoints of every state component at the final
+    substep and of the velocities at an intermediate one), the reverse pass
+    restated by hand in double precision.  T = 1 compares one substep's
+    adjoint (p2g_1, p2g_2, updateGrid and g2p backward) term for term;
+    longer runs add checkpointing and recompute.  The GPU's adjoint
+    arithmetic is f32, so the tolerance is relative to the gradient's
+    scale."""
+    from oracle import scene as scene_mod
+    recs = lattice_with_velocity(scene_mod, 16, 8.0)
+    recs[:, 8:11] = np.random.default_rng(3).normal(0.0, 0.05, (len(recs), 3)).astype(np.float32)
+    box = [32.0, 32.0, 32.0]
+    n = len(recs)
+    rng = np.random.default_rng(11)
+    seed_T = np.zeros((n, 20), np.float32)
+    for sl in (slice(0, 3), slice(4, 7), slice(8, 11), slice(12, 15), slice(16, 19)):
+        seed_T[:, sl] = rng.normal(0.0, 1e-3, (n, 3)).astype(np.float32)
+    mid = T // 2
+    seed_m = np.zeros((n, 20), np.float32)
+    seed_m[:, 4:7] = rng.normal(0.0, 1e-3, (n, 3)).astype(np.float32)
+    seeds = {T: seed_T} if mid in (0, T) else {T: seed_T, mid: seed_m}
+    adj = pkg.MLSMPMAdjoint([pkg.scene_desc(n, box)], T, every, tape="fp64")
+    adj.forward(recs, T)
+    g, pg = adj.backward(seeds)
+    adj.close()
+    st0 = oracle_mod.records_to_state64(recs)
+    p = oracle_mod.Params64.make(box)
+    cs = {t: oracle_mod.records_to_state64(v) for t, v in seeds.items()}
+    want, pwant = oracle_mod.backward64(st0, p, T, cs, every=every)
+    got = oracle_mod.records_to_state64(g)
+    for name, sl in (("x", slice(0, 3)), ("v", slice(3, 6)), ("C", slice(6, 15))):
+        scale = np.abs(want[:, sl]).max()
+        err = np.abs(got[:, sl] - want[:, sl]).max() / scale
+        assert err < 2e-4, f"{name}: max error {err:.2e} of the gradient's scale {scale:.3e}"
+    for j, name in enumerate(("stiffness", "viscosity")):
+        assert abs(pg[0, j] - pwant[j]) <= 2e-4 * abs(pwant[j]) + 1e-12, (name, pg[0, j], pwant[j])
