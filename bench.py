@@ -50,7 +50,7 @@ sys.path.insert(0, REPO)
 METRIC = "MLS-MPM particle-substeps/s at 1M (bit-exact grid)"
 UNIT = "particle-substeps/s"
 SUBSTEPS = 2                  # per execute(), mls-mpm/mls-mpm.ts:247
-AUTOTUNE_SUBSTEPS = 8         # timed per (task size, lane-table threshold) candidate
+AUTOTUNE_SUBSTEPS = 8         # timed per (block size, task size, lane-table threshold) candidate
 N_PER_AXIS = 100              # 100^3 = 1,000,000 particles
 ORIGIN, SPACING, JITTER, SEED = 4.0, 0.5, 0.05, 20240601
 BOX = [128.0, 128.0, 128.0]
@@ -368,8 +368,9 @@ def measure_batched(pkg, torch, stream, repeats: int = 3, autotune: bool = True)
     descs, recs = pkg.batch_scenes(BATCH_SCENES, seed=BATCH_SEED)
     S, K = len(descs), BATCH_SUBSTEPS
     batch = pkg.MLSMPMBatch(descs, recs, graph=True)
-    tuned = {"task_size": batch.autotune(4) if autotune else batch.taskSize,
-             "lane_table_min": batch.laneTableMin}
+    if autotune:
+        batch.autotune(4)
+    tuned = batch.tuning()
     batch.step(K, stream)  # captures the graph and warms up
     stream.synchronize()
     l0 = batch.launchCount()
@@ -816,11 +817,13 @@ def run_ours(args) -> None:
     # start from (the autotuner restores it), then the same start again so
     # the graphs of the chosen configuration are captured before timing
     if args.no_autotune:
-        tuned = {"task_size": sim.taskSize, "lane_table_min": sim.laneTableMin,
-                 "autotune": "off (engine defaults)"}
+        tuned = {**sim.tuning(), "autotune": "off (engine defaults)"}
     else:
-        tuned = {"task_size": sim.autotune(AUTOTUNE_SUBSTEPS), "lane_table_min": sim.laneTableMin,
-                 "autotune": f"{AUTOTUNE_SUBSTEPS} substeps after the warm-up steps"}
+        sim.autotune(AUTOTUNE_SUBSTEPS)
+        tuned = {**sim.tuning(),
+                 "autotune": f"{AUTOTUNE_SUBSTEPS} substeps after the warm-up steps, over "
+                             "task-kernel block sizes {128, 256, 512} x task sizes {64 ... 1024} "
+                             "x lane-table thresholds {32, 128, 512, off}"}
         sim.upload(parts, BOX)
         for _ in range(args.warmup):
             sim.execute(stream)
@@ -1081,8 +1084,8 @@ def main():
     ap.add_argument("--quick", action="store_true",
                     help="time the device-resident steps only (for profiler captures)")
     ap.add_argument("--no-autotune", action="store_true",
-                    help="keep the engine's default task size and lane-table threshold (the "
-                         "configuration of the committed ncu captures)")
+                    help="keep the engine's default block size, task size and lane-table "
+                         "threshold (the configuration of the committed ncu captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

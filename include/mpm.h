@@ -227,12 +227,20 @@ int mpm_get_task_size(const mpm_sim* sim);
  * depend on it. */
 int mpm_set_lane_table_min(mpm_sim* sim, int min_particles);
 int mpm_get_lane_table_min(const mpm_sim* sim);
-/* Autotuner: times `substeps` substeps for each task size in {64, 128, 256,
- * 512, 1024} and each lane-table threshold in {32, 128, 512, off} from the
- * current state (each pair once untimed first, so its CUDA graphs are
- * captured outside the timing), keeps the fastest pair and restores the
- * state (particles, posvel, counters and grid are as before the call).
- * Writes the task size to *chosen_task_size when non-null (the threshold:
+/* Sorted engine: threads per block of its two task kernels (p2g_2; g2p with
+ * the next p2g_1), the generalisation of the reference's
+ * @workgroup_size(64) (mls-mpm/p2g_1.wgsl:24): 128, 256 (the default) or
+ * 512; 0 restores the default.  A task is processed in chunks of this many
+ * particles.  Results do not depend on it. */
+int mpm_set_task_threads(mpm_sim* sim, int threads);
+int mpm_get_task_threads(const mpm_sim* sim);
+/* Autotuner: times `substeps` substeps for each task-kernel block size in
+ * {128, 256, 512}, each task size in {64, 128, 256, 512, 1024} and each
+ * lane-table threshold in {32, 128, 512, off} from the current state (each
+ * triple once untimed first, so its CUDA graphs are captured outside the
+ * timing), keeps the fastest triple and restores the state (particles,
+ * posvel, counters and grid are as before the call).  Writes the task size
+ * to *chosen_task_size when non-null (the others: mpm_get_task_threads,
  * mpm_get_lane_table_min).  Synchronizes. */
 int mpm_autotune(mpm_sim* sim, int substeps, int* chosen_task_size);
 
@@ -276,6 +284,8 @@ int mpm_batch_set_task_size(mpm_batch* batch, int task_size); /* see mpm_set_tas
 int mpm_batch_get_task_size(const mpm_batch* batch);
 int mpm_batch_set_lane_table_min(mpm_batch* batch, int min_particles); /* see mpm_set_lane_table_min */
 int mpm_batch_get_lane_table_min(const mpm_batch* batch);
+int mpm_batch_set_task_threads(mpm_batch* batch, int threads); /* see mpm_set_task_threads */
+int mpm_batch_get_task_threads(const mpm_batch* batch);
 /* See mpm_autotune: the batch's particles and posvel are as before the call;
  * mpm_batch_download_grid returns zeros until the next step. */
 int mpm_batch_autotune(mpm_batch* batch, int substeps, int* chosen_task_size);

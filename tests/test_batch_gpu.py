@@ -162,13 +162,15 @@ def test_batch_task_size_and_autotune(cuda, pkg, oracle_mod):
     descs, recs = mixed_scenes(pkg, scene_mod)
     offs = np.concatenate([[0], np.cumsum([d.num_particles for d in descs])])
     results = []
-    for cap in (64, 1024):
+    for cap, threads in ((64, 256), (1024, 256), (128, 128), (512, 512)):
         batch = pkg.MLSMPMBatch(descs, recs)
         batch.setTaskSize(cap)
+        batch.taskThreads = threads
         batch.step(6)
         results.append(batch.downloadParticles())
         batch.close()
-    assert_bits_equal(results[0], results[1], "task sizes 64 vs 1024")
+    for r, what in zip(results[1:], ("task size 1024", "128 threads", "512 threads")):
+        assert_bits_equal(results[0], r, f"task size 64 vs {what}")
     batch = pkg.MLSMPMBatch(descs, recs)
     batch.step(2)
     before = batch.downloadParticles()

@@ -355,6 +355,58 @@ def test_lane_table_threshold_does_not_change_results(cuda, pkg, oracle_mod):
     sim.close()
 
 
+@pytest.mark.parametrize("threads", [128, 256, 512])
+def test_task_threads_do_not_change_results(cuda, pkg, oracle_mod, threads):
+    """The task kernels at 128, 256 or 512 threads per block, with the
+    smallest and the default task sizes and the lane table always or never:
+    same bits as the oracle (the reference's UI scene and the 64k lattice)."""
+    from oracle import scene
+    cases = [([40.0, 30.0, 60.0], None), ([64.0, 64.0, 64.0], scene.lattice(40, 3.0, 0.5, 0.05, 8))]
+    for box, parts in cases:
+        for cap, lane in ((64, 1), (0, 1 << 30)):
+            sim = make_sim(pkg, "sorted")
+            if parts is None:
+                sim.reset(70000, box)
+            else:
+                sim.upload(parts, box)
+            sim.taskThreads = threads
+            sim.taskSize = cap
+            sim.laneTableMin = lane
+            assert sim.taskThreads == threads
+            ref = oracle_mod.OracleSim(sim.downloadParticles(), box)
+            for _ in range(4):
+                sim.execute()
+                ref.execute(2, NTHREADS)
+            assert_state_equal(sim, ref, f"{threads} threads, task size {cap}, lane table {lane}")
+            sim.close()
+    sim = make_sim(pkg, "sorted")
+    sim.taskThreads = 0
+    assert sim.taskThreads == 256
+    with pytest.raises(Exception):
+        sim.taskThreads = 192
+    sim.close()
+
+
+def test_autotune_cache_file(cuda, pkg, tmp_path):
+    """autotune(cache=...) times once per workload key and reapplies the
+    stored choice afterwards."""
+    import json
+    box = [40.0, 30.0, 60.0]
+    path = str(tmp_path / "tuning.json")
+    sim = make_sim(pkg, "sorted")
+    sim.reset(70000, box)
+    sim.autotune(2, cache=path)
+    choice = sim.tuning()
+    table = json.load(open(path))
+    assert list(table.values()) == [choice]
+    sim2 = make_sim(pkg, "sorted")
+    sim2.reset(70000, box)
+    sim2.autotune(2, cache=path)
+    assert sim2.tuning() == choice
+    sim.close()
+    sim2.close()
+
+
 def test_autotune_keeps_the_state(cuda, pkg, oracle_mod):
     box = [40.0, 30.0, 60.0]
     sim = make_sim(pkg, "sorted")
@@ -367,6 +419,7 @@ def test_autotune_keeps_the_state(cuda, pkg, oracle_mod):
     chosen = sim.autotune(4)
     assert chosen in (64, 128, 256, 512, 1024) and sim.taskSize == chosen
     assert sim.laneTableMin in (32, 128, 512, 1 << 30)
+    assert sim.taskThreads in (128, 256, 512)
     assert_bits_equal(sim.downloadParticles(), before[0], "particles after autotune")
     assert_bits_equal(sim.downloadGrid(), before[1], "grid after autotune")
     assert_bits_equal(sim.downloadPosvel(), before[2], "posvel after autotune")

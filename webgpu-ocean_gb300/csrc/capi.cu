@@ -478,6 +478,16 @@ int mpm_get_lane_table_min(const mpm_sim* s) {
     return s ? sorted_lane_table_min(s->sorted) : MPM_E_INVALID;
 }
 
+int mpm_set_task_threads(mpm_sim* s, int threads) {
+    if (int rc = check_sim(s)) return rc;
+    if (sorted_set_threads(s->sorted, threads) != 0) return fail(MPM_E_INVALID, sorted_error());
+    return MPM_OK;
+}
+
+int mpm_get_task_threads(const mpm_sim* s) {
+    return s ? sorted_threads(s->sorted) : MPM_E_INVALID;
+}
+
 
 int mpm_autotune(mpm_sim* s, int substeps, int* chosen_task_size) {
     if (int rc = check_sim(s)) return rc;

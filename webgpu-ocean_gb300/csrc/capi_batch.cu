@@ -209,6 +209,16 @@ int mpm_batch_get_lane_table_min(const mpm_batch* b) {
     return b && b->sorted ? sorted_lane_table_min(b->sorted) : MPM_E_INVALID;
 }
 
+int mpm_batch_set_task_threads(mpm_batch* b, int threads) {
+    if (int rc = check_batch(b)) return rc;
+    if (sorted_set_threads(b->sorted, threads) != 0) return fail(MPM_E_INVALID, sorted_error());
+    return MPM_OK;
+}
+
+int mpm_batch_get_task_threads(const mpm_batch* b) {
+    return b && b->sorted ? sorted_threads(b->sorted) : MPM_E_INVALID;
+}
+
 int mpm_batch_autotune(mpm_batch* b, int substeps, int* chosen_task_size) {
     if (int rc = check_batch(b)) return rc;
     if (substeps < 1) return fail(MPM_E_INVALID, "substeps must be positive");

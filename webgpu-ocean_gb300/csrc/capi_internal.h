@@ -64,15 +64,16 @@ long long grid_count_of(const float b[3]);
 // (capi_batch.cu).
 int scene_consts(const mpm_scene_desc& d, SimConsts& k);
 
-// Times `substeps` sorted-engine substeps for each pair of task size and
-// lane-table threshold from the same saved state and keeps the fastest.
-// Each candidate first runs once untimed, so that the CUDA graphs the timed
-// run replays are captured outside it.  The state after the call is the
-// state before it (particles, posvel, counters, grid).
+// Times `substeps` sorted-engine substeps for each triple of task-kernel
+// block size, task size and lane-table threshold from the same saved state
+// and keeps the fastest.  Each candidate first runs once untimed, so that
+// the CUDA graphs the timed run replays are captured outside it.  The state
+// after the call is the state before it (particles, posvel, counters, grid).
 template <class StepFn>
 int tune_engine(SortedEngine* e, ParticleStore& ps, int n, float4* posvel,
                 unsigned long long* counters, int substeps, cudaStream_t st, StepFn step,
-                int* chosen, int* chosen_lane, double* ms_out) {
+                int* chosen, int* chosen_lane, double* ms_out, int* chosen_threads = nullptr) {
+    static const int kThreads[] = {128, 256, 512};
     static const int kCaps[] = {64, 128, 256, 512, 1024};
     static const int kLanes[] = {32, 128, 512, 1 << 30};  // 1 << 30: no lane table
     Particles save{};
@@ -119,12 +120,14 @@ int tune_engine(SortedEngine* e, ParticleStore& ps, int n, float4* posvel,
         sorted_invalidate(e);
         return cudaGetLastError();
     };
-    int best = 0, best_lane = 0;
+    int best = 0, best_lane = 0, best_threads = 0;
     double best_ms = 0.0;
+    for (int th : kThreads)
     for (int cap : kCaps) {
         for (int lane : kLanes) {
             if (err != cudaSuccess) break;
-            if (sorted_set_task_cap(e, cap) != 0 || sorted_set_lane_table_min(e, lane) != 0)
+            if (sorted_set_threads(e, th) != 0 || sorted_set_task_cap(e, cap) != 0 ||
+                sorted_set_lane_table_min(e, lane) != 0)
                 continue;
             if ((err = restore()) != cudaSuccess) break;
             if (step(1) != 0 || step(substeps) != 0) { err = cudaErrorLaunchFailure; break; }
@@ -139,6 +142,7 @@ int tune_engine(SortedEngine* e, ParticleStore& ps, int n, float4* posvel,
             if (!best || ms < best_ms) {
                 best = cap;
                 best_lane = lane;
+                best_threads = th;
                 best_ms = ms;
             }
         }
@@ -151,11 +155,13 @@ int tune_engine(SortedEngine* e, ParticleStore& ps, int n, float4* posvel,
     cleanup();
     if (err != cudaSuccess) return cuda_fail(err, "autotune");
     if (best) {
+        sorted_set_threads(e, best_threads);
         sorted_set_task_cap(e, best);
         sorted_set_lane_table_min(e, best_lane);
     }
     if (chosen) *chosen = best;
     if (chosen_lane) *chosen_lane = best_lane;
+    if (chosen_threads) *chosen_threads = best_threads;
     if (ms_out) *ms_out = best_ms;
     return MPM_OK;
 }

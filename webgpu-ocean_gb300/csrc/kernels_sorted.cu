@@ -51,12 +51,14 @@ namespace mpm {
 
 namespace {
 
-// Particles per chunk == threads per CTA of the task kernels.  Bricks at the
-// free surface hold few particles, so smaller chunks leave fewer lanes idle.
-#ifndef MPM_TASK_THREADS
-#define MPM_TASK_THREADS 256
-#endif
-constexpr int kTask = MPM_TASK_THREADS;
+// Particles per chunk == threads per CTA of the task kernels (TH below):
+// 128, 256 (default) or 512, chosen per engine (sorted_set_threads) or by
+// the autotuner.  Bricks at the free surface hold few particles, so smaller
+// chunks leave fewer lanes idle; larger CTAs share one arena among more
+// particles in flight.  Every variant asks for 1024 resident threads per SM
+// (64 registers per thread).
+constexpr int kTask = 256;
+constexpr int kThreadVariants[3] = {128, 256, 512};
 // Arena strides: with x-stride = 16 and y-stride = 12 (mod 32) the 64 cells
 // of a brick fall into 32 bank classes of exactly two cells each
 // (class = (16*x + 12*y + z) mod 32 for brick-relative x, y, z).  When the
@@ -78,15 +80,10 @@ constexpr int kScanThreads = 1024;
 constexpr int kMinTaskCap = 64;
 constexpr int kMaxTaskCap = 1 << 30;
 
-// Minimum resident CTAs per SM requested from the register allocator.
-#ifndef MPM_G2P_MIN_BLOCKS
-#define MPM_G2P_MIN_BLOCKS (1024 / MPM_TASK_THREADS)
-#endif
-// k_p2g2 at 4 CTAs/SM (64 registers, some spilled to L1) measured ~5 %
-// faster than at 3 on the 1M dam-break, early and late in the run.
-#ifndef MPM_P2G2_MIN_BLOCKS
-#define MPM_P2G2_MIN_BLOCKS (1024 / MPM_TASK_THREADS)
-#endif
+// Minimum resident CTAs per SM requested from the register allocator: 1024
+// threads per SM.  k_p2g2 at 4 CTAs of 256 (64 registers, some spilled to
+// L1) measured ~5 % faster than at 3 on the 1M dam-break, early and late in
+// the run.
 // Default for Dev::lane_min: tasks with fewer particles skip the bank-class
 // lane table (its barriers and position loads cost more than the bank
 // conflicts it saves when a brick holds a few dozen particles) and keep the
@@ -342,13 +339,14 @@ struct LaneTable {
 // order, and the unfilled lanes are the tail of the last row.  The table is
 // written to order[first .. first + n) (g2p reuses it) and to lt.slot.
 // Every thread calls it (it contains barriers).
+template <int TH>
 __device__ __forceinline__ void build_lane_table(const Particles& P, const Geo& g, const Dev& d,
                                                  const Task& task, int tbx, int tby, int tbz,
                                                  LaneTable& lt) {
     const int n = task.count;
     if (threadIdx.x < 33) lt.cnt[threadIdx.x] = 0;
     __syncthreads();
-    for (int j = threadIdx.x; j < n; j += kTask) {
+    for (int j = threadIdx.x; j < n; j += TH) {
         const uint32_t slot = d.order[task.first + j];
         const float4 a = P.p0[slot];
         const float x[3] = {a.x, a.y, a.z};
@@ -388,7 +386,7 @@ __device__ __forceinline__ void build_lane_table(const Particles& P, const Geo& 
         }
     }
     __syncthreads();
-    for (int j = threadIdx.x; j < n; j += kTask) {
+    for (int j = threadIdx.x; j < n; j += TH) {
         const uint32_t key = lt.key[j];
         const int cls = (int)(key & 63u), r = (int)(key >> 6);
         int pos;
@@ -416,21 +414,21 @@ __device__ __forceinline__ void build_lane_table(const Particles& P, const Geo& 
 // (decoded into the other buffer after the compute), and task i-1's momentum
 // arena is flushed (each thread reads, flushes and zeroes its own slots).
 // ---------------------------------------------------------------------------
-template <bool BATCH>
-__global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
+template <bool BATCH, int TH>
+__global__ void __launch_bounds__(TH, 1024 / TH)
     k_p2g2(Particles P, Scene one, Dev d, int cur, unsigned long long* oob) {
     __shared__ float s_mass[2][kNA];
     __shared__ int s_q[2][3][kNA];
     __shared__ int s_task[2];
     __shared__ LaneTable s_lt;
-    constexpr int kPer = (kNA + kTask - 1) / kTask;  // arena slots per thread
+    constexpr int kPer = (kNA + TH - 1) / TH;  // arena slots per thread
 
     clear_dirty(d, cur ^ 1);
 
     int4* __restrict__ grid_all = d.grid[cur];
     unsigned bad = 0;
     const int ntasks = (int)__ldcg(d.ntasks);
-    for (int i = threadIdx.x; i < 2 * 3 * kNA; i += kTask) (&s_q[0][0][0])[i] = 0;
+    for (int i = threadIdx.x; i < 2 * 3 * kNA; i += TH) (&s_q[0][0][0])[i] = 0;
     if (threadIdx.x == 0) {
         s_task[0] = claim_task(d, kCtrP2G2);
         s_task[1] = claim_task(d, kCtrP2G2);
@@ -460,7 +458,7 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
         const int4* grid = grid_all + (size_t)brick_base<BATCH>(ts) * 64;
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
-            const int li = (int)threadIdx.x + q * kTask;
+            const int li = (int)threadIdx.x + q * TH;
             int x, y, z;
             if (li < kNA && arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z) &&
                 cell_exists(ts.g, x, y, z))
@@ -470,7 +468,7 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
     auto store_mass = [&](int buf, const int m[kPer], float fm) {
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
-            const int li = (int)threadIdx.x + q * kTask;
+            const int li = (int)threadIdx.x + q * TH;
             if (li < kNA) s_mass[buf][li] = dec(m[q], fm);
         }
     };
@@ -479,7 +477,7 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
         int ox, oy, oz;
         if (!origin(ts.g, tk, ox, oy, oz)) return;
         int4* grid = grid_all + (size_t)brick_base<BATCH>(ts) * 64;
-        for (int li = threadIdx.x; li < kNA; li += kTask) {
+        for (int li = threadIdx.x; li < kNA; li += TH) {
             const int q0 = s_q[buf][0][li], q1 = s_q[buf][1][li], q2 = s_q[buf][2][li];
             if ((q0 | q1 | q2) == 0) continue;
             s_q[buf][0][li] = 0;
@@ -528,8 +526,8 @@ __global__ void __launch_bounds__(kTask, MPM_P2G2_MIN_BLOCKS)
         if (task.brick >= 0) brick_coords(g, task.brick, tbx, tby, tbz);
         const bool table = task.brick >= 0 && task.count <= kMaxSort &&
                            task.count >= d.lane_min;  // uniform
-        if (table) build_lane_table(P, g, d, task, tbx, tby, tbz, s_lt);
-        for (int j = threadIdx.x; j < task.count; j += kTask) {
+        if (table) build_lane_table<TH>(P, g, d, task, tbx, tby, tbz, s_lt);
+        for (int j = threadIdx.x; j < task.count; j += TH) {
             const int slot = table ? (int)s_lt.slot[j] : (int)d.order[task.first + j];
             PState s;
             unpack_xC(P.p0[slot], P.p1[slot], P.p2[slot], s);
@@ -633,8 +631,8 @@ __global__ void __launch_bounds__(256) k_update(Scene one, Dev d, int cur) {
 // reads, flushes and zeroes its own slots); the bricks task i-1's stencils
 // reached are registered as dirty right after the barrier.
 // ---------------------------------------------------------------------------
-template <bool BATCH, bool DO_G2P, bool POSVEL>
-__global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
+template <bool BATCH, bool DO_G2P, bool POSVEL, int TH>
+__global__ void __launch_bounds__(TH, 1024 / TH)
     k_g2p_p2g1(Particles Pin, Particles Pout, const uint32_t* __restrict__ id_in,
                uint32_t* __restrict__ id_out, float4* __restrict__ posvel, Scene one, Dev d,
                int src, int dst, unsigned long long* oob) {
@@ -648,7 +646,7 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
     const int ctr = DO_G2P ? kCtrG2P : kCtrP2G1;
     unsigned bad = 0;
     const int ntasks = (int)__ldcg(d.ntasks);
-    for (int i = threadIdx.x; i < 2 * 4 * kNB; i += kTask) (&s_a[0][0][0])[i] = 0;
+    for (int i = threadIdx.x; i < 2 * 4 * kNB; i += TH) (&s_a[0][0][0])[i] = 0;
     if (threadIdx.x < 54) (&s_touch[0][0])[threadIdx.x] = 0;
     if (threadIdx.x == 0) {
         s_task[0] = claim_task(d, ctr);
@@ -668,7 +666,7 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
         ox = 4 * ox - 1;
         oy = 4 * oy - 1;
         oz = 4 * oz - 1;
-        for (int li = threadIdx.x; li < kNA; li += kTask) {
+        for (int li = threadIdx.x; li < kNA; li += TH) {
             int x, y, z;
             if (arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z) && cell_exists(ts.g, x, y, z))
                 cp_async16(&s_v[buf][li], gvsrc + brick_addr(ts.g, x, y, z));
@@ -681,7 +679,7 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
     auto flush = [&](int buf, const Scene& ts, int tbx, int tby, int tbz) {
         int4* gdst = gdst_all + (size_t)brick_base<BATCH>(ts) * 64;
         const int ox = 4 * tbx - 2, oy = 4 * tby - 2, oz = 4 * tbz - 2;
-        for (int li = threadIdx.x; li < kNB; li += kTask) {
+        for (int li = threadIdx.x; li < kNB; li += TH) {
             const int q0 = s_a[buf][0][li], q1 = s_a[buf][1][li], q2 = s_a[buf][2][li],
                       q3 = s_a[buf][3][li];
             if ((q0 | q1 | q2 | q3) == 0) continue;
@@ -737,7 +735,7 @@ __global__ void __launch_bounds__(kTask, MPM_G2P_MIN_BLOCKS)
         int4* __restrict__ gdst = gdst_all + (size_t)bb * 64;
         int tbx = 0, tby = 0, tbz = 0;
         if (task.brick >= 0) brick_coords(g, task.brick, tbx, tby, tbz);
-        for (int base = 0; base < task.count; base += kTask) {
+        for (int base = 0; base < task.count; base += TH) {
             const bool active = base + (int)threadIdx.x < task.count;
             const int jo = task.first + base + (active ? (int)threadIdx.x : 0);  // bin order
             const int slot = active ? (int)d.order[jo] : 0;
@@ -1073,7 +1071,12 @@ struct SortedEngine {
     int last = 0;         // grid read by the last substep's g2p
     bool primed = false;
     bool has_grid = false;
-    int blocks_p2g2 = 0, blocks_g2p = 0, blocks_update = 0;
+    int blocks_update = 0;
+    int blocks_p2g2_v[3] = {0, 0, 0}, blocks_g2p_v[3] = {0, 0, 0};  // per kThreadVariants
+    int threads = kTask;         // CTA size of the task kernels
+    int variant() const { return threads == 128 ? 0 : (threads == 512 ? 2 : 1); }
+    int blocks_p2g2() const { return blocks_p2g2_v[variant()]; }
+    int blocks_g2p() const { return blocks_g2p_v[variant()]; }
     int task_cap = kMaxSort;     // most particles per task (see kMinTaskCap)
     bool task_cap_auto = true;   // task_cap follows the particle count
     int ncells_linear = 0;       // batch: cells of all scenes' reference-layout grids
@@ -1185,7 +1188,7 @@ int ensure_grid_state(SortedEngine* e, long long bricks, long long bins) {
 // Default task size: enough tasks for every resident CTA of the task
 // kernels, bins left whole when they already are.
 int auto_task_cap(const SortedEngine* e, long long n) {
-    const long long per = e->blocks_g2p > 0 ? n / e->blocks_g2p : kMaxSort;
+    const long long per = e->blocks_g2p() > 0 ? n / e->blocks_g2p() : kMaxSort;
     return (int)std::min<long long>(kMaxSort, std::max<long long>(kMinTaskCap, per));
 }
 
@@ -1214,11 +1217,16 @@ int sorted_create(SortedEngine** out, int max_particles) {
     if (r == cudaSuccess) r = cudaMalloc(&e->d.ntasks, 4);
     if (r == cudaSuccess) r = cudaMalloc(&e->d.task_next, 4 * 3);
     if (r == cudaSuccess) {
-        e->blocks_p2g2 = occupancy_blocks((const void*)k_p2g2<false>, kTask);
-        e->blocks_g2p = occupancy_blocks((const void*)k_g2p_p2g1<false, true, false>, kTask);
+        e->blocks_p2g2_v[0] = occupancy_blocks((const void*)k_p2g2<false, 128>, 128);
+        e->blocks_p2g2_v[1] = occupancy_blocks((const void*)k_p2g2<false, 256>, 256);
+        e->blocks_p2g2_v[2] = occupancy_blocks((const void*)k_p2g2<false, 512>, 512);
+        e->blocks_g2p_v[0] = occupancy_blocks((const void*)k_g2p_p2g1<false, true, false, 128>, 128);
+        e->blocks_g2p_v[1] = occupancy_blocks((const void*)k_g2p_p2g1<false, true, false, 256>, 256);
+        e->blocks_g2p_v[2] = occupancy_blocks((const void*)k_g2p_p2g1<false, true, false, 512>, 512);
         e->blocks_update = occupancy_blocks((const void*)k_update<false>, 256);
-        if (e->blocks_p2g2 <= 0 || e->blocks_g2p <= 0 || e->blocks_update <= 0)
-            r = cudaErrorInvalidValue;
+        for (int v = 0; v < 3; ++v)
+            if (e->blocks_p2g2_v[v] <= 0 || e->blocks_g2p_v[v] <= 0) r = cudaErrorInvalidValue;
+        if (e->blocks_update <= 0) r = cudaErrorInvalidValue;
     }
     if (r != cudaSuccess) {
         g_err = std::string("sorted_create: ") + cudaGetErrorString(r);
@@ -1357,6 +1365,26 @@ int sorted_set_lane_table_min(SortedEngine* e, int min_particles) {
 
 int sorted_lane_table_min(const SortedEngine* e) { return e->d.lane_min; }
 
+int sorted_set_threads(SortedEngine* e, int threads) {
+    if (threads == 0) threads = kTask;
+    if (threads != 128 && threads != 256 && threads != 512) {
+        g_err = "task-kernel block size must be 128, 256 or 512 (0: default 256)";
+        return -1;
+    }
+    if (threads == e->threads) return 0;
+    drop_graphs(e);  // the captured launches carry the CTA size
+    e->threads = threads;
+    long long n = e->one.k.n;
+    if (e->batch) {
+        n = 0;
+        for (const Scene& sc : e->scenes) n += sc.k.n;
+    }
+    apply_task_cap(e, n);  // the automatic task size follows the resident CTAs
+    return 0;
+}
+
+int sorted_threads(const SortedEngine* e) { return e->threads; }
+
 int sorted_set_scene_consts(SortedEngine* e, int scene, const SimConsts& k, cudaStream_t st) {
     if (!e->configured || !e->batch || scene < 0 || scene >= (int)e->scenes.size()) {
         g_err = "no such scene in the batch";
@@ -1389,6 +1417,51 @@ bool sorted_has_grid(const SortedEngine* e) { return e && e->has_grid; }
 
 namespace {
 
+// The task kernels at the engine's CTA size.
+template <bool BATCH, int TH>
+void launch_p2g2_th(SortedEngine* e, const Particles& P, const Scene& one, int cur,
+                    unsigned long long* oob, cudaStream_t st) {
+    k_p2g2<BATCH, TH><<<e->blocks_p2g2(), TH, 0, st>>>(P, one, e->d, cur, oob);
+}
+
+template <bool BATCH>
+void launch_p2g2(SortedEngine* e, const Particles& P, const Scene& one, int cur,
+                 unsigned long long* oob, cudaStream_t st) {
+    switch (e->threads) {
+        case 128: launch_p2g2_th<BATCH, 128>(e, P, one, cur, oob, st); break;
+        case 512: launch_p2g2_th<BATCH, 512>(e, P, one, cur, oob, st); break;
+        default: launch_p2g2_th<BATCH, 256>(e, P, one, cur, oob, st); break;
+    }
+}
+
+template <bool BATCH, bool DO_G2P, bool POSVEL, int TH>
+void launch_g2p_th(SortedEngine* e, const Particles& Pin, const Particles& Pout,
+                   const uint32_t* id_in, uint32_t* id_out, float4* posvel, const Scene& one,
+                   int src, int dst, unsigned long long* oob, cudaStream_t st) {
+    k_g2p_p2g1<BATCH, DO_G2P, POSVEL, TH><<<e->blocks_g2p(), TH, 0, st>>>(
+        Pin, Pout, id_in, id_out, posvel, one, e->d, src, dst, oob);
+}
+
+template <bool BATCH, bool DO_G2P, bool POSVEL>
+void launch_g2p(SortedEngine* e, const Particles& Pin, const Particles& Pout,
+                const uint32_t* id_in, uint32_t* id_out, float4* posvel, const Scene& one,
+                int src, int dst, unsigned long long* oob, cudaStream_t st) {
+    switch (e->threads) {
+        case 128:
+            launch_g2p_th<BATCH, DO_G2P, POSVEL, 128>(e, Pin, Pout, id_in, id_out, posvel, one,
+                                                      src, dst, oob, st);
+            break;
+        case 512:
+            launch_g2p_th<BATCH, DO_G2P, POSVEL, 512>(e, Pin, Pout, id_in, id_out, posvel, one,
+                                                      src, dst, oob, st);
+            break;
+        default:
+            launch_g2p_th<BATCH, DO_G2P, POSVEL, 256>(e, Pin, Pout, id_in, id_out, posvel, one,
+                                                      src, dst, oob, st);
+            break;
+    }
+}
+
 // Issues the kernels of `substeps` substeps and advances the engine state.
 template <bool BATCH>
 int enqueue_substeps(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned long long* oob,
@@ -1397,19 +1470,16 @@ int enqueue_substeps(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigne
     for (int s = 0; s < substeps; ++s) {
         const int cur = e->cur, nxt = cur ^ 1;
         const int pin = ps->cur, pout = pin ^ 1;
-        LAUNCH(KID_SORTED_P2G_2,
-               (k_p2g2<BATCH><<<e->blocks_p2g2, kTask, 0, st>>>(ps->P[pin], one, e->d, cur, oob)));
+        LAUNCH(KID_SORTED_P2G_2, (launch_p2g2<BATCH>(e, ps->P[pin], one, cur, oob, st)));
         LAUNCH(KID_UPDATE_GRID, (k_update<BATCH><<<e->blocks_update, 256, 0, st>>>(one, e->d, cur)));
         if (s == substeps - 1)
             LAUNCH(KID_SORTED_G2P_P2G_1,
-                   (k_g2p_p2g1<BATCH, true, true><<<e->blocks_g2p, kTask, 0, st>>>(
-                       ps->P[pin], ps->P[pout], ps->id[pin], ps->id[pout], posvel, one, e->d, cur,
-                       nxt, oob)));
+                   (launch_g2p<BATCH, true, true>(e, ps->P[pin], ps->P[pout], ps->id[pin],
+                                                  ps->id[pout], posvel, one, cur, nxt, oob, st)));
         else
             LAUNCH(KID_SORTED_G2P_P2G_1,
-                   (k_g2p_p2g1<BATCH, true, false><<<e->blocks_g2p, kTask, 0, st>>>(
-                       ps->P[pin], ps->P[pout], ps->id[pin], ps->id[pout], posvel, one, e->d, cur,
-                       nxt, oob)));
+                   (launch_g2p<BATCH, true, false>(e, ps->P[pin], ps->P[pout], ps->id[pin],
+                                                   ps->id[pout], posvel, one, cur, nxt, oob, st)));
         LAUNCH(KID_SCAN, (k_scan<<<(nbins + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(e->d, nbins)));
         LAUNCH(KID_SCATTER, (k_scatter<<<(max(n, nbins) + 255) / 256, 256, 0, st>>>(e->d, n, nbins)));
         e->last = cur;
@@ -1441,8 +1511,8 @@ int prime(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned long long
     LAUNCH(KID_SCATTER, (k_scatter<<<(max(n, nbins) + 255) / 256, 256, 0, st>>>(e->d, n, nbins)));
     e->cur = 0;
     LAUNCH(KID_SORTED_P2G_1,
-           (k_g2p_p2g1<BATCH, false, false><<<e->blocks_g2p, kTask, 0, st>>>(
-               P, P, ps->id[ps->cur], ps->id[ps->cur], posvel, one, e->d, e->cur, e->cur, oob)));
+           (launch_g2p<BATCH, false, false>(e, P, P, ps->id[ps->cur], ps->id[ps->cur], posvel,
+                                            one, e->cur, e->cur, oob, st)));
     SE_CUDA(cudaGetLastError());
     e->primed = true;
     return 0;

@@ -40,6 +40,11 @@ int sorted_task_cap(const SortedEngine* e);
 int sorted_set_lane_table_min(SortedEngine* e, int min_particles);
 int sorted_lane_table_min(const SortedEngine* e);
 
+// Threads per CTA of the two task kernels (p2g_2; g2p + p2g_1): 128, 256 or
+// 512 (0: the default, 256).  Results do not depend on it.
+int sorted_set_threads(SortedEngine* e, int threads);
+int sorted_threads(const SortedEngine* e);
+
 // Forgets the carried-over state (the next step re-bins and redoes p2g_1).
 void sorted_invalidate(SortedEngine* e);
 

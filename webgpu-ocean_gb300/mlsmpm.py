@@ -78,6 +78,28 @@ def default_params() -> L.Params:
     return p
 
 
+def _cached_tuning(path, key: str, run, apply) -> dict:
+    """The tuning choice for `key`: from the JSON file at `path` when it holds
+    one (applied with apply(choice)), else run() -> choice, stored there."""
+    import json
+    import os
+    table = {}
+    if path and os.path.exists(path):
+        with open(path) as f:
+            table = json.load(f)
+        if key in table:
+            apply(table[key])
+            return table[key]
+    choice = run()
+    if path:
+        table[key] = choice
+        tmp = f"{path}.tmp{os.getpid()}"
+        with open(tmp, "w") as f:
+            json.dump(table, f, indent=1, sort_keys=True)
+        os.replace(tmp, path)
+    return choice
+
+
 class MLSMPMSimulator:
     max_x_grids = 64  # mls-mpm/mls-mpm.ts:13-15
     max_y_grids = 64
@@ -250,12 +272,43 @@ class MLSMPMSimulator:
         _check(self._lib.mpm_set_lane_table_min(self._handle, int(min_particles)),
                "laneTableMin")
 
-    def autotune(self, substeps: int = 8) -> int:
-        """Picks the fastest task size and lane-table threshold for the
-        current scene (returns the task size); state unchanged."""
-        out = ctypes.c_int(0)
-        _check(self._lib.mpm_autotune(self._handle, int(substeps), ctypes.byref(out)), "autotune")
-        return int(out.value)
+    @property
+    def taskThreads(self) -> int:
+        """Threads per block of the sorted engine's task kernels (128, 256,
+        512; 0 to set: the default)."""
+        return _check(self._lib.mpm_get_task_threads(self._handle), "taskThreads")
+
+    @taskThreads.setter
+    def taskThreads(self, threads: int) -> None:
+        _check(self._lib.mpm_set_task_threads(self._handle, int(threads)), "taskThreads")
+
+    def tuning(self) -> dict:
+        """The engine's tunable configuration."""
+        return {"task_threads": self.taskThreads, "task_size": self.taskSize,
+                "lane_table_min": self.laneTableMin}
+
+    def autotune(self, substeps: int = 8, cache: str | None = None,
+                 key: str | None = None) -> int:
+        """Picks the fastest task-kernel block size, task size and lane-table
+        threshold for the current scene (returns the task size); state
+        unchanged.  cache: a JSON file of earlier choices by workload key
+        (default key: particle count and grid size); a hit applies the
+        stored choice without timing anything, a miss times and stores."""
+        key = key or f"MLSMPMSimulator/n={self.numParticles}/cells={self.gridCount}"
+
+        def run():
+            out = ctypes.c_int(0)
+            _check(self._lib.mpm_autotune(self._handle, int(substeps), ctypes.byref(out)),
+                   "autotune")
+            return self.tuning()
+
+        choice = _cached_tuning(cache, key, run, self._apply_tuning)
+        return int(choice["task_size"])
+
+    def _apply_tuning(self, choice: dict) -> None:
+        self.taskThreads = choice["task_threads"]
+        self.taskSize = choice["task_size"]
+        self.laneTableMin = choice["lane_table_min"]
 
     def checkHealth(self) -> dict:
         h = L.Health()
@@ -493,12 +546,37 @@ class MLSMPMBatch:
         _check(self._lib.mpm_batch_set_lane_table_min(self._handle, int(min_particles)),
                "laneTableMin")
 
-    def autotune(self, substeps: int = 4) -> int:
-        """Task size and lane-table threshold, as MLSMPMSimulator.autotune."""
-        out = ctypes.c_int(0)
-        _check(self._lib.mpm_batch_autotune(self._handle, int(substeps), ctypes.byref(out)),
-               "autotune")
-        return int(out.value)
+    @property
+    def taskThreads(self) -> int:
+        """See MLSMPMSimulator.taskThreads."""
+        return _check(self._lib.mpm_batch_get_task_threads(self._handle), "taskThreads")
+
+    @taskThreads.setter
+    def taskThreads(self, threads: int) -> None:
+        _check(self._lib.mpm_batch_set_task_threads(self._handle, int(threads)), "taskThreads")
+
+    def tuning(self) -> dict:
+        return {"task_threads": self.taskThreads, "task_size": self.taskSize,
+                "lane_table_min": self.laneTableMin}
+
+    def autotune(self, substeps: int = 4, cache: str | None = None,
+                 key: str | None = None) -> int:
+        """Block size, task size and lane-table threshold, as
+        MLSMPMSimulator.autotune (default key: scene and particle counts)."""
+        key = key or f"MLSMPMBatch/scenes={self.numScenes}/n={self.numParticles}"
+
+        def run():
+            out = ctypes.c_int(0)
+            _check(self._lib.mpm_batch_autotune(self._handle, int(substeps), ctypes.byref(out)),
+                   "autotune")
+            return self.tuning()
+
+        def apply(choice):
+            self.taskThreads = choice["task_threads"]
+            self.taskSize = choice["task_size"]
+            self.laneTableMin = choice["lane_table_min"]
+
+        return int(_cached_tuning(cache, key, run, apply)["task_size"])
 
     def downloadParticles(self) -> np.ndarray:
         out = np.zeros((self.numParticles, 20), dtype=np.float32)
