@@ -387,6 +387,83 @@ def test_task_threads_do_not_change_results(cuda, pkg, oracle_mod, threads):
     sim.close()
 
 
+def _quirk_scene():
+    """A lattice with particles past every wall, fast, NaN and saturating
+    ones (the global path and the padding bricks around the grid)."""
+    from oracle import scene
+    parts = scene.lattice(10, 6.0, 0.5, 0.05, 5)
+    parts[0, 0:3] = [0.2, 12.0, 12.0]
+    parts[1, 0:3] = [12.0, 0.3, 12.0]
+    parts[2, 0:3] = [12.0, 12.0, 23.7]
+    parts[3, 0:3] = [30.0, 30.0, 30.0]
+    parts[4, 4:7] = [50.0, -40.0, 30.0]
+    parts[5, 8] = np.nan
+    parts[6, 8:11] = [1e30, -1e30, 1e30]
+    return parts
+
+
+@pytest.mark.parametrize("depth", [4, 8])
+def test_bin_depth_does_not_change_results(cuda, pkg, oracle_mod, depth):
+    """Bins of one brick (4 cells along z) or of two bricks stacked along z
+    (8), at every block size, with the smallest and the default task sizes
+    and the lane table always or never: same bits as the oracle on the
+    reference's UI scene (60 cells along z: an odd brick count), the 64k
+    lattice, a box of odd sizes and particles past every wall."""
+    from oracle import scene
+    cases = [([40.0, 30.0, 60.0], None, 70000),
+             ([64.0, 64.0, 64.0], scene.lattice(40, 3.0, 0.5, 0.05, 8), None),
+             ([37.0, 23.0, 29.0], None, 20000),
+             ([24.0, 24.0, 24.0], _quirk_scene(), None)]
+    for box, parts, n in cases:
+        for threads, cap, lane in ((256, 0, 128), (128, 64, 1), (512, 0, 1 << 30)):
+            sim = make_sim(pkg, "sorted")
+            if parts is None:
+                sim.reset(n, box)
+            else:
+                sim.upload(parts, box)
+            sim.binDepth = depth
+            sim.taskThreads = threads
+            sim.taskSize = cap
+            sim.laneTableMin = lane
+            assert sim.binDepth == depth
+            ref = oracle_mod.OracleSim(sim.downloadParticles(), box)
+            for _ in range(4):
+                sim.execute()
+                ref.execute(2, NTHREADS)
+            what = f"box {box}, bin depth {depth}, {threads} threads, task size {cap}, lane {lane}"
+            assert_bits_equal(sim.downloadGrid(), ref.cells, what + " grid")
+            p = sim.downloadParticles()
+            finite = np.isfinite(ref.particles)
+            assert np.array_equal(np.isfinite(p), finite), what
+            assert_bits_equal(p[finite], ref.particles[finite], what + " particles")
+            sim.close()
+
+
+def test_bin_depth_switch_mid_run(cuda, pkg, oracle_mod):
+    """Switching the bin depth between frames re-bins the particles: the run
+    continues bit for bit, and the grid of the last frame stays readable."""
+    box = [40.0, 30.0, 60.0]
+    sim = make_sim(pkg, "sorted")
+    sim.reset(70000, box)
+    ref = oracle_mod.OracleSim(sim.downloadParticles(), box)
+    ran = False
+    for depth in (4, 8, 4, 8):
+        sim.binDepth = depth
+        if ran:
+            assert_bits_equal(sim.downloadGrid(), ref.cells, f"grid after switching to {depth}")
+        for _ in range(2):
+            sim.execute()
+            ref.execute(2, NTHREADS)
+        ran = True
+        assert_state_equal(sim, ref, f"bin depth {depth}")
+    sim.binDepth = 0
+    assert sim.binDepth == 4
+    for bad in (2, 6, 16, -4):
+        with pytest.raises(Exception):
+            sim.binDepth = bad
+    sim.close()
+
+
 def test_autotune_cache_file(cuda, pkg, tmp_path):
     """autotune(cache=...) times once per workload key and reapplies the
     stored choice afterwards."""
@@ -420,6 +497,7 @@ def test_autotune_keeps_the_state(cuda, pkg, oracle_mod):
     assert chosen in (64, 128, 256, 512, 1024) and sim.taskSize == chosen
     assert sim.laneTableMin in (32, 128, 512, 1 << 30)
     assert sim.taskThreads in (128, 256, 512)
+    assert sim.binDepth in (4, 8)
     assert_bits_equal(sim.downloadParticles(), before[0], "particles after autotune")
     assert_bits_equal(sim.downloadGrid(), before[1], "grid after autotune")
     assert_bits_equal(sim.downloadPosvel(), before[2], "posvel after autotune")

@@ -488,6 +488,17 @@ int mpm_get_task_threads(const mpm_sim* s) {
     return s ? sorted_threads(s->sorted) : MPM_E_INVALID;
 }
 
+int mpm_set_bin_depth(mpm_sim* s, int depth) {
+    if (int rc = check_sim(s)) return rc;
+    DeviceGuard g(s->device);
+    if (sorted_set_bin_depth(s->sorted, depth) != 0) return fail(MPM_E_INVALID, sorted_error());
+    return MPM_OK;
+}
+
+int mpm_get_bin_depth(const mpm_sim* s) {
+    return s ? sorted_bin_depth(s->sorted) : MPM_E_INVALID;
+}
+
 
 int mpm_autotune(mpm_sim* s, int substeps, int* chosen_task_size) {
     if (int rc = check_sim(s)) return rc;

@@ -5,23 +5,31 @@
 // of mpm_math.cuh, and the grid is an i32 sum, so the order in which
 // contributions arrive does not matter.  What changes is where the work runs:
 //
-//  * The grid is stored brick-major: 4x4x4-cell bricks of 1 KB, contiguous.
-//  * Particles are counting-sorted by the brick of their base cell every
+//  * The grid is stored brick-major: 4x4x4-cell bricks of 1 KB, contiguous,
+//    with one brick of zero padding around the grid (two above it along z
+//    when needed), so that every arena slot of every task addresses a stored
+//    cell: padding and cells outside the reference grid are never written
+//    and read as zero.
+//  * Particles are counting-sorted by the bin of their base cell every
 //    substep, and kept physically in that order: g2p writes each particle to
 //    its position in the bin order of the other particle buffer (an id array
-//    rides along), so the next substep reads nearly contiguous memory.
-//  * A task is one brick's particles; CTAs claim tasks from an atomic work
+//    rides along), so the next substep reads nearly contiguous memory.  A bin
+//    is one brick (4x4x4 cells) or two bricks stacked along z (4x4x8 cells),
+//    chosen per engine (sorted_set_bin_depth) or by the autotuner.
+//  * A task is one bin's particles; CTAs claim tasks from an atomic work
 //    counter and walk a task in chunks of one particle per thread.  In tasks
 //    of at least Dev::lane_min particles (a runtime parameter, autotuned),
-//    p2g_2 first reorders the brick's particles into a lane table that puts
+//    p2g_2 first reorders the bin's particles into a lane table that puts
 //    particles of 32 different shared-memory bank classes in the 32 lanes of
 //    a warp (build_lane_table); g2p reuses that order.  The CTA keeps the
 //    cells the task's stencils reach (its "arena") in shared memory: the
-//    brick plus a one-cell halo (6^3 cells) for p2g_2 and g2p, plus a
-//    two-cell halo (8^3) for the next substep's p2g_1, whose particles have
-//    moved.  Gathers read the arena; scatters are shared-memory i32 atomics,
-//    flushed once per task with one red.global.add per touched cell and
-//    component.  Arena offsets are compile-time constants.
+//    bin plus a one-cell halo (6x6x6 or 6x6x10 cells) for p2g_2 and g2p, plus
+//    a two-cell halo (8x8x8 or 8x8x12) for the next substep's p2g_1, whose
+//    particles have moved.  Gathers read the arena; scatters are shared-memory
+//    i32 atomics, flushed once per task with one red.global.add per touched
+//    cell and component.  Each thread owns fixed arena slots and keeps their
+//    offsets (relative to the task's corner brick) in registers, so a task's
+//    arena load and flush cost one add per slot.
 //  * Per substep:
 //      k_p2g2        p2g_2; also clears the other grid's dirty bricks
 //      k_update      updateGrid over the bricks that hold contributions
@@ -73,6 +81,9 @@ constexpr int kSYA = 12, kSXA = 80, kNA = kA * kSXA;
 constexpr int kB = 8;            // next-p2g_1 arena edge: brick + 2-cell halo
 constexpr int kSYB = 12, kSXB = 112, kNB = kB * kSXB;
 constexpr int kMaxSort = 1024;   // tasks with more particles keep the bin order
+// p2g_1 dirty-brick flags per task: the 3 x 3 x 4 stored bricks around a bin
+// (a 4x4x8 bin's 8x8x12 arena reaches four bricks along z)
+constexpr int kTouch = 36;
 constexpr int kScanThreads = 1024;
 // A bin holding more than `task_cap` particles is split into tasks of at
 // most task_cap particles (same brick, separate arena flushes), so that small
@@ -103,19 +114,27 @@ struct Geo {
     int Y, Z, YZ;      // flat-index strides: i32(init.y), i32(init.z)
     int grid_count;
     int Xi;            // cells along x reachable by an in-range flat index
-    int BX, BY, BZ;    // bricks per axis
-    int nbricks;       // BX*BY*BZ; bin id nbricks collects irregular particles
+    int BX, BY, BZ;    // bricks per axis covering the grid
+    int PY, PZ;        // stored bricks along y and z (the grid's plus padding)
+    int nbricks;       // stored bricks: (BX + 2) * PY * PZ
+    int zs;            // log2 of a bin's cells along z: 2 (4x4x4) or 3 (4x4x8)
+    int NZ;            // bins along z
+    int nbins;         // BX * BY * NZ; bin id nbins collects irregular particles
 };
 
-// A task: particles [first, first + count) of the bin order, all in `brick`
+// A task: particles [first, first + count) of the bin order, all in `bin`
 // (scene-local; -1: the scene's bin of irregular particles) of `scene`.
+// (x0, y0, z0) is the bin's first cell; abase the int4 offset (scene-local)
+// of the stored brick (x0/4 - 1, y0/4 - 1, z0/4 - 1), from which the arena
+// slot offsets count.
 struct __align__(16) Task {
     int first;
     int count;
-    int brick;
+    int bin;
     int scene;
+    int x0, y0, z0;
+    int abase;
 };
-
 // One scene of a batch: its geometry and constants, and where its bricks,
 // bins and particles start in the concatenated arrays.  A scene's bins are
 // its bricks followed by its irregular bin.
@@ -137,8 +156,8 @@ struct Dev {
     uint32_t* ticket;    // [1]
     uint32_t* bin_of;
     uint32_t* rank_of;
-    uint32_t* bin_count;  // [nbricks + 1]
-    uint32_t* bin_start;  // [nbricks + 2]
+    uint32_t* bin_count;  // [bins + 1]
+    uint32_t* bin_start;  // [bins + 2]
     uint32_t* order;
     Task* tasks;
     uint32_t* ntasks;
@@ -158,7 +177,7 @@ __device__ __forceinline__ const Scene& scene_ref(const Dev& d, const Scene& one
     if constexpr (BATCH) return d.scenes[s];
     else return one;
 }
-// First global brick / bin of a scene (0 for a single scene).
+// First stored brick / bin of a scene (0 for a single scene).
 template <bool BATCH>
 __device__ __forceinline__ int brick_base(const Scene& s) {
     if constexpr (BATCH) return s.bbase;
@@ -178,8 +197,10 @@ __device__ __forceinline__ int claim_task(const Dev& d, int ctr) {
     return (int)atomicAdd(d.task_next + ctr, 1u);
 }
 
+// Stored brick of cell (x, y, z); cells down to -4 and up to the padding's
+// end along each axis have one.
 __device__ __forceinline__ int brick_of(const Geo& g, int x, int y, int z) {
-    return ((x >> 2) * g.BY + (y >> 2)) * g.BZ + (z >> 2);
+    return (((x >> 2) + 1) * g.PY + (y >> 2) + 1) * g.PZ + (z >> 2) + 1;
 }
 
 __device__ __forceinline__ int brick_addr(const Geo& g, int x, int y, int z) {
@@ -199,13 +220,6 @@ __device__ __forceinline__ bool in_grid(const Geo& g, int idx) {
     return (unsigned)idx < (unsigned)g.grid_count;
 }
 
-// A cell that exists in the reference grid: per-axis in range and its flat
-// index below grid_count.
-__device__ __forceinline__ bool cell_exists(const Geo& g, int x, int y, int z) {
-    if (x < 0 || y < 0 || z < 0 || x >= g.Xi || y >= g.Y || z >= g.Z) return false;
-    return (x * g.Y + y) * g.Z + z < g.grid_count;
-}
-
 // A particle is regular when all 27 stencil cells are in-range cells whose
 // flat index equals their geometric position (no aliasing).
 __device__ __forceinline__ bool regular_base(const Geo& g, int bx, int by, int bz) {
@@ -221,12 +235,17 @@ __device__ __forceinline__ void base_cell(const float x[3], int& bx, int& by, in
     bz = f2i_sat(floorf(x[2]));
 }
 
+// Stored brick index -> brick coordinates of the grid (padding: -1 or past
+// the end).
 __device__ __forceinline__ void brick_coords(const Geo& g, int brick, int& x, int& y, int& z) {
-    const int byz = g.BY * g.BZ;
-    x = brick / byz;
-    const int r = brick - x * byz;
-    y = r / g.BZ;
-    z = r - y * g.BZ;
+    const int pyz = g.PY * g.PZ;
+    x = brick / pyz;
+    const int r = brick - x * pyz;
+    y = r / g.PZ;
+    z = r - y * g.PZ;
+    x -= 1;
+    y -= 1;
+    z -= 1;
 }
 
 __device__ __forceinline__ void mark_brick(const Dev& d, int gi, uint32_t b) {
@@ -255,7 +274,8 @@ __device__ __forceinline__ void count_bin(const Dev& d, bool active, int slot, u
 
 __device__ __forceinline__ uint32_t bin_key(const Geo& g, uint32_t base, bool reg, int bx, int by,
                                            int bz) {
-    return base + (reg ? (uint32_t)brick_of(g, bx, by, bz) : (uint32_t)g.nbricks);
+    return base + (reg ? (uint32_t)(((bx >> 2) * g.BY + (by >> 2)) * g.NZ + (bz >> g.zs))
+                       : (uint32_t)g.nbins);
 }
 
 // Clears the dirty bricks of grid gi (warp per brick, grid-stride over the
@@ -287,20 +307,29 @@ __device__ __forceinline__ void clear_dirty(const Dev& d, int gi) {
     }
 }
 
-// Arena slot li (strides SX, SY, 1) at origin o -> grid coordinates; false
-// for padding slots.
-template <int E, int SX, int SY>
-__device__ __forceinline__ bool arena_cell(int li, int ox, int oy, int oz, int& x, int& y, int& z) {
+// int4 offset of arena slot li, counted from the stored brick (x0/4 - 1,
+// y0/4 - 1, z0/4 - 1) of a task's bin at (x0, y0, z0).  The arena spans E
+// cells along x and y and ez along z from (x0 - H, y0 - H, z0 - H) with
+// strides (SX, SY, 1); slots past its extent (padding) and past N give -1.
+template <int E, int SX, int SY, int H, int N>
+__device__ __forceinline__ int slot_offset(const Geo& g, int li, int ez) {
     const int ax = li / SX;
     const int r = li - ax * SX;
     const int ay = r / SY;
     const int az = r - ay * SY;
-    x = ox + ax;
-    y = oy + ay;
-    z = oz + az;
-    return ay < E && az < E;
+    if (li >= N || ay >= E || az >= ez) return -1;
+    const int tx = ax + 4 - H, ty = ay + 4 - H, tz = az + 4 - H;
+    return (((tx >> 2) * g.PY + (ty >> 2)) * g.PZ + (tz >> 2)) * 64 + ((tx & 3) << 4) +
+           ((ty & 3) << 2) + (tz & 3);
 }
 
+// The offsets of this thread's slots li = threadIdx.x + q * TH.
+template <int E, int SX, int SY, int H, int N, int TH, int PER>
+__device__ __forceinline__ void slot_offsets(const Geo& g, int ez, int (&off)[PER]) {
+#pragma unroll
+    for (int q = 0; q < PER; ++q)
+        off[q] = slot_offset<E, SX, SY, H, N>(g, (int)threadIdx.x + q * TH, ez);
+}
 
 // Global-path mass source (flat indices, as the reference's shaders address).
 struct GlobalMass {
@@ -332,7 +361,7 @@ struct LaneTable {
     int valid[32], core[32], empty_pre[33], over_pre[33];
 };
 
-// Orders a brick's n particles into a table of ceil(n/32) rows of 32 lanes
+// Orders a bin's n particles into a table of ceil(n/32) rows of 32 lanes
 // in which lane k of a row holds, where possible, a particle of bank class k
 // (its base cell's class); particles of over-full classes (and particles
 // outside the arena) fill the lanes that under-full classes leave empty, in
@@ -341,8 +370,7 @@ struct LaneTable {
 // Every thread calls it (it contains barriers).
 template <int TH>
 __device__ __forceinline__ void build_lane_table(const Particles& P, const Geo& g, const Dev& d,
-                                                 const Task& task, int tbx, int tby, int tbz,
-                                                 LaneTable& lt) {
+                                                 const Task& task, LaneTable& lt) {
     const int n = task.count;
     if (threadIdx.x < 33) lt.cnt[threadIdx.x] = 0;
     __syncthreads();
@@ -352,9 +380,9 @@ __device__ __forceinline__ void build_lane_table(const Particles& P, const Geo& 
         const float x[3] = {a.x, a.y, a.z};
         int bx, by, bz;
         base_cell(x, bx, by, bz);
-        const int ax = bx - 4 * tbx, ay = by - 4 * tby, az = bz - 4 * tbz;
+        const int ax = bx - task.x0, ay = by - task.y0, az = bz - task.z0;
         const bool in = regular_base(g, bx, by, bz) && (unsigned)ax <= 3u && (unsigned)ay <= 3u &&
-                        (unsigned)az <= 3u;
+                        (unsigned)az < (1u << g.zs);
         const int cls = in ? ((16 * ax + 12 * ay + az) & 31) : 32;
         const int r = atomicAdd(&lt.cnt[cls], 1);
         lt.tmp[j] = slot;
@@ -433,17 +461,21 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         s_task[0] = claim_task(d, kCtrP2G2);
         s_task[1] = claim_task(d, kCtrP2G2);
     }
+
+    // offsets of this thread's arena slots for the geometry of scene
+    // off_scene (recomputed when a batch's task belongs to another scene)
+    int off[kPer];
+    int off_scene = 0;
+    slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPer>(one.g, (1 << one.g.zs) + 2, off);
+    auto offsets_for = [&](int scene) {
+        if (BATCH && scene != off_scene) {
+            const Geo& tg = scene_ref<BATCH>(d, one, scene).g;
+            slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPer>(tg, (1 << tg.zs) + 2, off);
+            off_scene = scene;
+        }
+    };
     __syncthreads();
 
-    // arena origin (brick - 1 cell) of a task, or false for an irregular bin
-    auto origin = [&](const Geo& tg, const Task& tk, int& ox, int& oy, int& oz) -> bool {
-        if (tk.brick < 0) return false;
-        brick_coords(tg, tk.brick, ox, oy, oz);
-        ox = 4 * ox - 1;
-        oy = 4 * oy - 1;
-        oz = 4 * oz - 1;
-        return true;
-    };
     // raw mass words of this thread's arena slots for a task, and its FM
     auto load_mass = [&](int t, int m[kPer], float& fm) {
 #pragma unroll
@@ -453,17 +485,13 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         const Task tk = d.tasks[t];
         const Scene& ts = scene_ref<BATCH>(d, one, tk.scene);
         fm = ts.k.fm;
-        int ox, oy, oz;
-        if (!origin(ts.g, tk, ox, oy, oz)) return;
-        const int4* grid = grid_all + (size_t)brick_base<BATCH>(ts) * 64;
+        if (tk.bin < 0) return;
+        offsets_for(tk.scene);
+        const int* grid = reinterpret_cast<const int*>(
+            grid_all + (size_t)brick_base<BATCH>(ts) * 64 + tk.abase);
 #pragma unroll
-        for (int q = 0; q < kPer; ++q) {
-            const int li = (int)threadIdx.x + q * TH;
-            int x, y, z;
-            if (li < kNA && arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z) &&
-                cell_exists(ts.g, x, y, z))
-                m[q] = __ldcg(reinterpret_cast<const int*>(grid + brick_addr(ts.g, x, y, z)) + 3);
-        }
+        for (int q = 0; q < kPer; ++q)
+            if (off[q] >= 0) m[q] = __ldcg(grid + 4 * off[q] + 3);
     };
     auto store_mass = [&](int buf, const int m[kPer], float fm) {
 #pragma unroll
@@ -473,20 +501,21 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         }
     };
     auto flush = [&](int buf, const Task& tk) {
+        if (tk.bin < 0) return;
+        offsets_for(tk.scene);
         const Scene& ts = scene_ref<BATCH>(d, one, tk.scene);
-        int ox, oy, oz;
-        if (!origin(ts.g, tk, ox, oy, oz)) return;
-        int4* grid = grid_all + (size_t)brick_base<BATCH>(ts) * 64;
-        for (int li = threadIdx.x; li < kNA; li += TH) {
+        int* grid = reinterpret_cast<int*>(grid_all + (size_t)brick_base<BATCH>(ts) * 64 + tk.abase);
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const int li = (int)threadIdx.x + q * TH;
+            if (li >= kNA) continue;
             const int q0 = s_q[buf][0][li], q1 = s_q[buf][1][li], q2 = s_q[buf][2][li];
             if ((q0 | q1 | q2) == 0) continue;
             s_q[buf][0][li] = 0;
             s_q[buf][1][li] = 0;
             s_q[buf][2][li] = 0;
-            int x, y, z;
-            if (!arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z)) continue;
-            if (!cell_exists(ts.g, x, y, z)) continue;  // unreachable for regular particles
-            int* c = reinterpret_cast<int*>(grid + brick_addr(ts.g, x, y, z));
+            if (off[q] < 0) continue;  // unreachable: stencils stay inside the arena
+            int* c = grid + 4 * off[q];
             if (q0) atomicAdd(c + 0, q0);
             if (q1) atomicAdd(c + 1, q1);
             if (q2) atomicAdd(c + 2, q2);
@@ -501,7 +530,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         store_mass(0, m, fm);
     }
     Task prev;
-    prev.brick = -1;
+    prev.bin = -1;
     prev.count = 0;
     prev.scene = 0;
     bool have_prev = false;
@@ -522,22 +551,21 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         const SimConsts& k = sc.k;
         const int bb = brick_base<BATCH>(sc);
         int4* __restrict__ grid = grid_all + (size_t)bb * 64;
-        int tbx = 0, tby = 0, tbz = 0;
-        if (task.brick >= 0) brick_coords(g, task.brick, tbx, tby, tbz);
-        const bool table = task.brick >= 0 && task.count <= kMaxSort &&
+        const bool table = task.bin >= 0 && task.count <= kMaxSort &&
                            task.count >= d.lane_min;  // uniform
-        if (table) build_lane_table<TH>(P, g, d, task, tbx, tby, tbz, s_lt);
+        if (table) build_lane_table<TH>(P, g, d, task, s_lt);
+        const unsigned zext = 1u << g.zs;
         for (int j = threadIdx.x; j < task.count; j += TH) {
             const int slot = table ? (int)s_lt.slot[j] : (int)d.order[task.first + j];
             PState s;
             unpack_xC(P.p0[slot], P.p1[slot], P.p2[slot], s);
             int bx, by, bz;
             base_cell(s.x, bx, by, bz);
-            const int ax = bx - 4 * tbx, ay = by - 4 * tby, az = bz - 4 * tbz;
-            const bool in_arena = task.brick >= 0 && regular_base(g, bx, by, bz) &&
-                                  (unsigned)ax <= 3u && (unsigned)ay <= 3u && (unsigned)az <= 3u;
+            const int ax = bx - task.x0, ay = by - task.y0, az = bz - task.z0;
+            const bool in_arena = task.bin >= 0 && regular_base(g, bx, by, bz) &&
+                                  (unsigned)ax <= 3u && (unsigned)ay <= 3u && (unsigned)az < zext;
             if (in_arena) {
-                // stencil corner (base - 1) relative to the arena origin (brick - 1)
+                // stencil corner (base - 1) relative to the arena origin (bin - 1)
                 const int li0 = ax * kSXA + ay * kSYA + az;
                 auto mass = [&](int gx, int gy, int gz) -> float {
                     return s_mass[buf][li0 + gx * kSXA + gy * kSYA + gz];
@@ -638,8 +666,10 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
                int src, int dst, unsigned long long* oob) {
     __shared__ __align__(16) float4 s_v[DO_G2P ? 2 : 1][DO_G2P ? kNA : 1];
     __shared__ int s_a[2][4][kNB];
-    __shared__ int s_touch[2][27];
+    __shared__ int s_touch[2][kTouch];
     __shared__ int s_task[2];
+    constexpr int kPerA = DO_G2P ? (kNA + TH - 1) / TH : 1;  // g2p arena slots per thread
+    constexpr int kPerB = (kNB + TH - 1) / TH;                // p2g_1 arena slots per thread
 
     const float4* __restrict__ gv_all = d.gv[src];
     int4* __restrict__ gdst_all = d.grid[dst];
@@ -647,39 +677,49 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     unsigned bad = 0;
     const int ntasks = (int)__ldcg(d.ntasks);
     for (int i = threadIdx.x; i < 2 * 4 * kNB; i += TH) (&s_a[0][0][0])[i] = 0;
-    if (threadIdx.x < 54) (&s_touch[0][0])[threadIdx.x] = 0;
+    if (threadIdx.x < 2 * kTouch) (&s_touch[0][0])[threadIdx.x] = 0;
     if (threadIdx.x == 0) {
         s_task[0] = claim_task(d, ctr);
         s_task[1] = claim_task(d, ctr);
     }
+
+    // offsets of this thread's g2p arena slots for the geometry of scene
+    // off_scene (recomputed when a batch's task belongs to another); the
+    // flush computes those of its touched p2g_1 slots
+    int offA[kPerA];
+    int off_scene = 0;
+    if (DO_G2P) slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPerA>(one.g, (1 << one.g.zs) + 2, offA);
+    auto offsets_for = [&](int scene) {
+        if (BATCH && DO_G2P && scene != off_scene) {
+            const Geo& tg = scene_ref<BATCH>(d, one, scene).g;
+            slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPerA>(tg, (1 << tg.zs) + 2, offA);
+            off_scene = scene;
+        }
+    };
     __syncthreads();
 
     // g2p arena of task t (velocities decoded by k_update) into s_v[buf]
     auto prefetch = [&](int t, int buf) {
         if (!DO_G2P || t >= ntasks) return;
         const Task tk = d.tasks[t];
-        if (tk.brick < 0) return;
+        if (tk.bin < 0) return;
+        offsets_for(tk.scene);
         const Scene& ts = scene_ref<BATCH>(d, one, tk.scene);
-        const float4* gvsrc = gv_all + (size_t)brick_base<BATCH>(ts) * 64;
-        int ox, oy, oz;
-        brick_coords(ts.g, tk.brick, ox, oy, oz);
-        ox = 4 * ox - 1;
-        oy = 4 * oy - 1;
-        oz = 4 * oz - 1;
-        for (int li = threadIdx.x; li < kNA; li += TH) {
-            int x, y, z;
-            if (arena_cell<kA, kSXA, kSYA>(li, ox, oy, oz, x, y, z) && cell_exists(ts.g, x, y, z))
-                cp_async16(&s_v[buf][li], gvsrc + brick_addr(ts.g, x, y, z));
-            else
-                s_v[buf][li] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        }
+        const float4* gvsrc = gv_all + (size_t)brick_base<BATCH>(ts) * 64 + tk.abase;
+#pragma unroll
+        for (int q = 0; q < kPerA; ++q)
+            if (offA[q] >= 0) cp_async16(&s_v[buf][(int)threadIdx.x + q * TH], gvsrc + offA[q]);
         cp_async_commit();
     };
-    // flush the p2g_1 arena of a task of scene ts with brick coordinates tb
-    auto flush = [&](int buf, const Scene& ts, int tbx, int tby, int tbz) {
-        int4* gdst = gdst_all + (size_t)brick_base<BATCH>(ts) * 64;
-        const int ox = 4 * tbx - 2, oy = 4 * tby - 2, oz = 4 * tbz - 2;
-        for (int li = threadIdx.x; li < kNB; li += TH) {
+    // flush the p2g_1 arena of task tk
+    auto flush = [&](int buf, const Task& tk) {
+        const Scene& ts = scene_ref<BATCH>(d, one, tk.scene);
+        int* gdst = reinterpret_cast<int*>(gdst_all + (size_t)brick_base<BATCH>(ts) * 64 + tk.abase);
+        const int ez = (1 << ts.g.zs) + 4;
+#pragma unroll
+        for (int q = 0; q < kPerB; ++q) {
+            const int li = (int)threadIdx.x + q * TH;
+            if (li >= kNB) continue;
             const int q0 = s_a[buf][0][li], q1 = s_a[buf][1][li], q2 = s_a[buf][2][li],
                       q3 = s_a[buf][3][li];
             if ((q0 | q1 | q2 | q3) == 0) continue;
@@ -687,32 +727,34 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
             s_a[buf][1][li] = 0;
             s_a[buf][2][li] = 0;
             s_a[buf][3][li] = 0;
-            int x, y, z;
-            if (!arena_cell<kB, kSXB, kSYB>(li, ox, oy, oz, x, y, z)) continue;
-            if (!cell_exists(ts.g, x, y, z)) continue;  // unreachable for regular particles
-            int* c = reinterpret_cast<int*>(gdst + brick_addr(ts.g, x, y, z));
+            const int o = slot_offset<kB, kSXB, kSYB, 2, kNB>(ts.g, li, ez);
+            if (o < 0) continue;  // unreachable: stencils stay inside the arena
+            int* c = gdst + 4 * o;
             if (q0) atomicAdd(c + 0, q0);
             if (q1) atomicAdd(c + 1, q1);
             if (q2) atomicAdd(c + 2, q2);
             if (q3) atomicAdd(c + 3, q3);
         }
     };
-    // register the bricks (3x3x3 around tb) flagged in s_touch[buf]
-    auto mark = [&](int buf, const Scene& ts, int tbx, int tby, int tbz) {
-        if (threadIdx.x < 27 && s_touch[buf][threadIdx.x]) {
+    // register the stored bricks flagged in s_touch[buf]: flag
+    // (kx * 3 + ky) * 4 + kz is brick (x0/4 - 1 + kx, y0/4 - 1 + ky, z0/4 - 1 + kz)
+    auto mark = [&](int buf, const Task& tk) {
+        if (threadIdx.x < kTouch && s_touch[buf][threadIdx.x]) {
             const int i = threadIdx.x;
-            const int nbx = tbx + i / 9 - 1, nby = tby + (i / 3) % 3 - 1, nbz = tbz + i % 3 - 1;
-            mark_brick(d, dst,
-                       (uint32_t)(brick_base<BATCH>(ts) + (nbx * ts.g.BY + nby) * ts.g.BZ + nbz));
+            const Scene& ts = scene_ref<BATCH>(d, one, tk.scene);
+            const int kx = (i >> 2) / 3, ky = (i >> 2) - 3 * kx, kz = i & 3;
+            const int off = (kx * ts.g.PY + ky) * ts.g.PZ + kz;
+            mark_brick(d, dst, (uint32_t)(brick_base<BATCH>(ts) + (tk.abase >> 6) + off));
             s_touch[buf][i] = 0;
         }
     };
 
     int t = s_task[0];
     prefetch(t, 0);
-    bool have_prev = false, prev_arena = false;
-    int pbx = 0, pby = 0, pbz = 0;  // brick of the previous task
-    int pscene = 0;                 // and its scene
+    bool have_prev = false;
+    Task prev;
+    prev.bin = -1;
+    prev.scene = 0;
     int it = 0;
     while (t < ntasks) {
         const int buf = it & 1;
@@ -720,10 +762,9 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         __syncthreads();  // s_v[buf] arrived; task it-1 computed everywhere
         const int t_next = s_task[buf ^ 1];
         if (threadIdx.x == 0) s_task[buf] = claim_task(d, ctr);
-        if (have_prev && prev_arena) mark(buf ^ 1, scene_ref<BATCH>(d, one, pscene), pbx, pby, pbz);
+        if (have_prev && prev.bin >= 0) mark(buf ^ 1, prev);
         prefetch(t_next, buf ^ 1);
-        if (have_prev && prev_arena)
-            flush(buf ^ 1, scene_ref<BATCH>(d, one, pscene), pbx, pby, pbz);
+        if (have_prev && prev.bin >= 0) flush(buf ^ 1, prev);
 
         const Task task = d.tasks[t];
         const Scene& sc = scene_ref<BATCH>(d, one, task.scene);
@@ -733,8 +774,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         const uint32_t binb = bin_base<BATCH>(sc);
         const float4* __restrict__ gvsrc = gv_all + (size_t)bb * 64;
         int4* __restrict__ gdst = gdst_all + (size_t)bb * 64;
-        int tbx = 0, tby = 0, tbz = 0;
-        if (task.brick >= 0) brick_coords(g, task.brick, tbx, tby, tbz);
+        const unsigned zext = 1u << g.zs;
         for (int base = 0; base < task.count; base += TH) {
             const bool active = base + (int)threadIdx.x < task.count;
             const int jo = task.first + base + (active ? (int)threadIdx.x : 0);  // bin order
@@ -746,10 +786,10 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
                     s.x[0] = a.x; s.x[1] = a.y; s.x[2] = a.z;
                     int bx, by, bz;
                     base_cell(s.x, bx, by, bz);
-                    const int ax = bx - 4 * tbx, ay = by - 4 * tby, az = bz - 4 * tbz;
-                    const bool in_arena = task.brick >= 0 && regular_base(g, bx, by, bz) &&
+                    const int ax = bx - task.x0, ay = by - task.y0, az = bz - task.z0;
+                    const bool in_arena = task.bin >= 0 && regular_base(g, bx, by, bz) &&
                                           (unsigned)ax <= 3u && (unsigned)ay <= 3u &&
-                                          (unsigned)az <= 3u;
+                                          (unsigned)az < zext;
                     if (in_arena) {
                         const int li0 = ax * kSXA + ay * kSYA + az;
                         const float4* sv = s_v[DO_G2P ? buf : 0];
@@ -789,17 +829,16 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
                 load_particle(Pin, slot, s);
             }
 
-            // p2g_1 of the (new) state into grid dst, arena = brick + 2-cell halo.
+            // p2g_1 of the (new) state into grid dst, arena = bin + 2-cell halo.
             int bx = 0, by = 0, bz = 0;
             bool reg = false;
             if (active) {
                 base_cell(s.x, bx, by, bz);
                 reg = regular_base(g, bx, by, bz);
-                const int ax = bx + 1 - 4 * tbx, ay = by + 1 - 4 * tby, az = bz + 1 - 4 * tbz;
-                const bool in_arena = task.brick >= 0 && reg &&
-                                      (unsigned)ax <= (unsigned)(kB - 3) &&
+                const int ax = bx + 1 - task.x0, ay = by + 1 - task.y0, az = bz + 1 - task.z0;
+                const bool in_arena = task.bin >= 0 && reg && (unsigned)ax <= (unsigned)(kB - 3) &&
                                       (unsigned)ay <= (unsigned)(kB - 3) &&
-                                      (unsigned)az <= (unsigned)(kB - 3);
+                                      (unsigned)az <= zext + 1u;
                 if (in_arena) {
                     const int li0 = ax * kSXB + ay * kSYB + az;
                     auto sink = [&](int gx, int gy, int gz, int m, int vx, int vy, int vz) {
@@ -816,14 +855,16 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
                                       [&](int, int gx, int gy, int gz, int m, int vx, int vy,
                                           int vz) { sink(gx, gy, gz, m, vx, vy, vz); });
                     }
-                    // bricks the stencil (base-1 .. base+1) reaches, relative to the task's
-                    const int x0 = ((bx - 1) >> 2) - tbx, x1 = ((bx + 1) >> 2) - tbx;
-                    const int y0 = ((by - 1) >> 2) - tby, y1 = ((by + 1) >> 2) - tby;
-                    const int z0 = ((bz - 1) >> 2) - tbz, z1 = ((bz + 1) >> 2) - tbz;
+                    // bricks the stencil (base-1 .. base+1) reaches, from the bin's corner brick
+                    const int cx = (task.x0 >> 2) - 1, cy = (task.y0 >> 2) - 1,
+                              cz = (task.z0 >> 2) - 1;
+                    const int x0 = ((bx - 1) >> 2) - cx, x1 = ((bx + 1) >> 2) - cx;
+                    const int y0 = ((by - 1) >> 2) - cy, y1 = ((by + 1) >> 2) - cy;
+                    const int z0 = ((bz - 1) >> 2) - cz, z1 = ((bz + 1) >> 2) - cz;
                     for (int xx = x0; xx <= x1; ++xx)
                         for (int yy = y0; yy <= y1; ++yy)
                             for (int zz = z0; zz <= z1; ++zz)
-                                s_touch[buf][((xx + 1) * 3 + (yy + 1)) * 3 + (zz + 1)] = 1;
+                                s_touch[buf][(xx * 3 + yy) * 4 + zz] = 1;
                 } else {
                     p2g1_particle(s, k,
                                   [&](int idx, int, int, int, int m, int vx, int vy, int vz) {
@@ -841,18 +882,14 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
             if (DO_G2P) count_bin(d, active, jo, bin_key(g, binb, reg, bx, by, bz));
         }
         have_prev = true;
-        prev_arena = task.brick >= 0;
-        pbx = tbx;
-        pby = tby;
-        pbz = tbz;
-        pscene = task.scene;
+        prev = task;
         t = t_next;
         ++it;
     }
     __syncthreads();
-    if (have_prev && prev_arena) {
-        mark((it - 1) & 1, scene_ref<BATCH>(d, one, pscene), pbx, pby, pbz);
-        flush((it - 1) & 1, scene_ref<BATCH>(d, one, pscene), pbx, pby, pbz);
+    if (have_prev && prev.bin >= 0) {
+        mark((it - 1) & 1, prev);
+        flush((it - 1) & 1, prev);
     }
     if (bad) atomicAdd(oob, (unsigned long long)bad);
 }
@@ -886,7 +923,8 @@ __global__ void __launch_bounds__(kTask) k_bin(Particles P, Scene one, Dev d, in
 }
 
 // Exclusive scan of the bin counts -> bin_start and the task list (one task
-// per non-empty bin).  CTA c scans bins [c*1024, (c+1)*1024); it finds its
+// per non-empty bin, or several when it holds more than task_cap particles;
+// one_g is a single scene's geometry, batches read theirs from the table).  CTA c scans bins [c*1024, (c+1)*1024); it finds its
 // starting offsets by reducing all earlier counts itself (a few KB to a few
 // hundred KB from L2), so no CTA waits on another.  The counts are zeroed
 // by k_scatter, which runs next.
@@ -926,7 +964,7 @@ __device__ __forceinline__ uint32_t tasks_of(uint32_t c, uint32_t cap) {
     return (c + cap - 1u) / cap;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, int nbins) {
+__global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, Geo one_g, int nbins) {
     __shared__ uint32_t s_a[32], s_b[32];
     const int base = blockIdx.x * kScanThreads;
     const uint32_t cap = (uint32_t)d.task_cap;
@@ -957,14 +995,21 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, int nbins) {
         d.bin_start[bin] = start;
         if (c) {
             Task tk;
-            if (d.bin_scene) {
-                const int sc = (int)__ldg(d.bin_scene + bin);
-                const int local = bin - d.scenes[sc].binbase;
-                tk.brick = local == d.scenes[sc].g.nbricks ? -1 : local;
-                tk.scene = sc;
-            } else {
-                tk.brick = bin == nbins - 1 ? -1 : bin;
-                tk.scene = 0;
+            tk.scene = d.bin_scene ? (int)__ldg(d.bin_scene + bin) : 0;
+            const Geo& g = d.bin_scene ? d.scenes[tk.scene].g : one_g;
+            const int local = d.bin_scene ? bin - d.scenes[tk.scene].binbase : bin;
+            tk.bin = local == g.nbins ? -1 : local;
+            tk.x0 = tk.y0 = tk.z0 = tk.abase = 0;
+            if (tk.bin >= 0) {
+                const int byz = g.BY * g.NZ;
+                const int bx = local / byz;
+                const int r = local - bx * byz;
+                const int by = r / g.NZ;
+                const int bz = (r - by * g.NZ) << (g.zs - 2);  // in bricks
+                tk.x0 = 4 * bx;
+                tk.y0 = 4 * by;
+                tk.z0 = 4 * bz;
+                tk.abase = ((bx * g.PY + by) * g.PZ + bz) * 64;
             }
             for (uint32_t q = 0; q < nt; ++q) {
                 tk.first = (int)(start + q * cap);
@@ -1080,6 +1125,7 @@ struct SortedEngine {
     int task_cap = kMaxSort;     // most particles per task (see kMinTaskCap)
     bool task_cap_auto = true;   // task_cap follows the particle count
     int ncells_linear = 0;       // batch: cells of all scenes' reference-layout grids
+    int zs = 2;                  // log2 of a bin's cells along z (Geo::zs)
     std::vector<GraphEntry> graphs;
 };
 
@@ -1142,8 +1188,17 @@ int occupancy_blocks(const void* fn, int threads) {
     return nsm * per;
 }
 
-// Brick geometry of one scene; false for a degenerate box.
-bool make_geo(const SimConsts& k, Geo& g) {
+// Bins along z and in all for a bin depth of 1 << zs cells.
+void set_bins(Geo& g, int zs) {
+    g.zs = zs;
+    const int per = 1 << (zs - 2);  // bricks per bin along z
+    g.NZ = (g.BZ + per - 1) / per;
+    g.nbins = g.BX * g.BY * g.NZ;
+}
+
+// Brick geometry of one scene; false for a degenerate box or one too large
+// for i32 cell addresses.
+bool make_geo(const SimConsts& k, int zs, Geo& g) {
     if (k.Y <= 0 || k.Z <= 0 || k.grid_count <= 0) return false;
     g = Geo{};
     g.Y = k.Y;
@@ -1156,11 +1211,19 @@ bool make_geo(const SimConsts& k, Geo& g) {
     g.BX = (g.Xi + 3) / 4;
     g.BY = (g.Y + 3) / 4;
     g.BZ = (g.Z + 3) / 4;
-    const long long nb = (long long)g.BX * g.BY * g.BZ;
+    // padding: one brick on each side, along z up to an even brick count
+    // plus one more, so that a 4x4x8 bin's arena ends inside it
+    g.PY = g.BY + 2;
+    g.PZ = ((g.BZ + 1) & ~1) + 2;
+    const long long nb = (long long)(g.BX + 2) * g.PY * g.PZ;
     if (nb * 64 > INT_MAX) return false;
     g.nbricks = (int)nb;
+    set_bins(g, zs);
     return true;
 }
+
+// Bins of a scene at the finest bin depth (the bin arrays' size).
+long long max_bins(const Geo& g) { return (long long)g.BX * g.BY * g.BZ + 1; }
 
 // Grids, dirty lists, bin arrays and the task list for `bricks` bricks and
 // `bins` bins (kept when large enough).
@@ -1256,7 +1319,7 @@ int sorted_configure(SortedEngine* e, const SimConsts& k) {
     e->primed = false;
     e->has_grid = false;
     Geo g;
-    if (!make_geo(k, g)) return -1;
+    if (!make_geo(k, e->zs, g)) return -1;
     // Captured graphs hold the scene by value: they stay valid across a
     // reconfiguration with the same constants and geometry (a re-upload of
     // the same scene) and are dropped otherwise.
@@ -1264,13 +1327,13 @@ int sorted_configure(SortedEngine* e, const SimConsts& k) {
     one.g = g;
     one.k = k;
     if (e->batch || std::memcmp(&one, &e->one, sizeof(Scene)) != 0) drop_graphs(e);
-    if (ensure_grid_state(e, g.nbricks, (long long)g.nbricks + 1)) return -1;
+    if (ensure_grid_state(e, g.nbricks, max_bins(g))) return -1;
     free_tables(e);
     e->batch = false;
     e->scenes.clear();
     e->one = one;
     e->nbricks = g.nbricks;
-    e->nbins = g.nbricks + 1;
+    e->nbins = g.nbins + 1;
     apply_task_cap(e, k.n);
     e->configured = true;
     return 0;
@@ -1285,9 +1348,9 @@ int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes) {
         return -1;
     }
     std::vector<Scene> hs((size_t)nscenes);
-    long long bricks = 0, bins = 0, parts = 0, lcells = 0;
+    long long bricks = 0, bins = 0, bins_alloc = 0, parts = 0, lcells = 0;
     for (int s = 0; s < nscenes; ++s) {
-        if (!make_geo(ks[s], hs[s].g)) {
+        if (!make_geo(ks[s], e->zs, hs[s].g)) {
             g_err = "scene " + std::to_string(s) + " has a degenerate box";
             return -1;
         }
@@ -1297,7 +1360,8 @@ int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes) {
         hs[s].lbase = (int)lcells;
         hs[s].k = ks[s];
         bricks += hs[s].g.nbricks;
-        bins += (long long)hs[s].g.nbricks + 1;
+        bins += (long long)hs[s].g.nbins + 1;
+        bins_alloc += max_bins(hs[s].g);
         parts += ks[s].n;
         lcells += ks[s].grid_count;
         if (bricks * 64 > INT_MAX || parts > e->max_particles || lcells > INT_MAX) {
@@ -1306,16 +1370,16 @@ int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes) {
         }
     }
     drop_graphs(e);
-    if (ensure_grid_state(e, bricks, bins)) return -1;
+    if (ensure_grid_state(e, bricks, bins_alloc)) return -1;
     free_tables(e);
     std::vector<uint32_t> brick_scene((size_t)bricks), bin_scene((size_t)bins);
     for (int s = 0; s < nscenes; ++s) {
         for (int b = 0; b < hs[s].g.nbricks; ++b) brick_scene[(size_t)hs[s].bbase + b] = (uint32_t)s;
-        for (int b = 0; b <= hs[s].g.nbricks; ++b) bin_scene[(size_t)hs[s].binbase + b] = (uint32_t)s;
+        for (int b = 0; b <= hs[s].g.nbins; ++b) bin_scene[(size_t)hs[s].binbase + b] = (uint32_t)s;
     }
     SE_CUDA(cudaMalloc(&e->scenes_d, sizeof(Scene) * (size_t)nscenes));
     SE_CUDA(cudaMalloc(&e->brick_scene_d, 4 * (size_t)bricks));
-    SE_CUDA(cudaMalloc(&e->bin_scene_d, 4 * (size_t)bins));
+    SE_CUDA(cudaMalloc(&e->bin_scene_d, 4 * (size_t)bins_alloc));
     SE_CUDA(cudaMemcpy(e->scenes_d, hs.data(), sizeof(Scene) * (size_t)nscenes, cudaMemcpyHostToDevice));
     SE_CUDA(cudaMemcpy(e->brick_scene_d, brick_scene.data(), 4 * (size_t)bricks, cudaMemcpyHostToDevice));
     SE_CUDA(cudaMemcpy(e->bin_scene_d, bin_scene.data(), 4 * (size_t)bins, cudaMemcpyHostToDevice));
@@ -1384,6 +1448,46 @@ int sorted_set_threads(SortedEngine* e, int threads) {
 }
 
 int sorted_threads(const SortedEngine* e) { return e->threads; }
+
+int sorted_set_bin_depth(SortedEngine* e, int depth) {
+    if (depth == 0) depth = 4;
+    if (depth != 4 && depth != 8) {
+        g_err = "bin depth must be 4 or 8 cells (0: default 4)";
+        return -1;
+    }
+    const int zs = depth == 8 ? 3 : 2;
+    if (zs == e->zs) return 0;
+    e->zs = zs;
+    if (!e->configured) return 0;
+    drop_graphs(e);
+    e->primed = false;  // the particles are binned again before the next substep
+    if (!e->batch) {
+        set_bins(e->one.g, zs);
+        e->nbins = e->one.g.nbins + 1;
+        return 0;
+    }
+    // the scene table and the bin -> scene map change; no launch may read
+    // them meanwhile
+    SE_CUDA(cudaDeviceSynchronize());
+    long long bins = 0;
+    for (Scene& sc : e->scenes) {
+        set_bins(sc.g, zs);
+        sc.binbase = (int)bins;
+        bins += (long long)sc.g.nbins + 1;
+    }
+    std::vector<uint32_t> bin_scene((size_t)bins);
+    for (size_t s = 0; s < e->scenes.size(); ++s)
+        for (int b = 0; b <= e->scenes[s].g.nbins; ++b)
+            bin_scene[(size_t)e->scenes[s].binbase + b] = (uint32_t)s;
+    SE_CUDA(cudaMemcpy(e->scenes_d, e->scenes.data(), sizeof(Scene) * e->scenes.size(),
+                       cudaMemcpyHostToDevice));
+    SE_CUDA(cudaMemcpy(e->bin_scene_d, bin_scene.data(), 4 * (size_t)bins, cudaMemcpyHostToDevice));
+    e->one = e->scenes[0];
+    e->nbins = (int)bins;
+    return 0;
+}
+
+int sorted_bin_depth(const SortedEngine* e) { return 1 << e->zs; }
 
 int sorted_set_scene_consts(SortedEngine* e, int scene, const SimConsts& k, cudaStream_t st) {
     if (!e->configured || !e->batch || scene < 0 || scene >= (int)e->scenes.size()) {
@@ -1480,7 +1584,7 @@ int enqueue_substeps(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigne
             LAUNCH(KID_SORTED_G2P_P2G_1,
                    (launch_g2p<BATCH, true, false>(e, ps->P[pin], ps->P[pout], ps->id[pin],
                                                    ps->id[pout], posvel, one, cur, nxt, oob, st)));
-        LAUNCH(KID_SCAN, (k_scan<<<(nbins + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(e->d, nbins)));
+        LAUNCH(KID_SCAN, (k_scan<<<(nbins + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(e->d, one.g, nbins)));
         LAUNCH(KID_SCATTER, (k_scatter<<<(max(n, nbins) + 255) / 256, 256, 0, st>>>(e->d, n, nbins)));
         e->last = cur;
         e->cur = nxt;
@@ -1507,7 +1611,7 @@ int prime(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned long long
     SE_CUDA(cudaMemsetAsync(e->d.bin_count, 0, 4 * (size_t)nbins, st));
     const Particles& P = ps->P[ps->cur];
     LAUNCH(KID_BIN, (k_bin<BATCH><<<(n + kTask - 1) / kTask, kTask, 0, st>>>(P, one, e->d, n)));
-    LAUNCH(KID_SCAN, (k_scan<<<(nbins + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(e->d, nbins)));
+    LAUNCH(KID_SCAN, (k_scan<<<(nbins + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(e->d, one.g, nbins)));
     LAUNCH(KID_SCATTER, (k_scatter<<<(max(n, nbins) + 255) / 256, 256, 0, st>>>(e->d, n, nbins)));
     e->cur = 0;
     LAUNCH(KID_SORTED_P2G_1,

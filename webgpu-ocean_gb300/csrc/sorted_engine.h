@@ -45,6 +45,13 @@ int sorted_lane_table_min(const SortedEngine* e);
 int sorted_set_threads(SortedEngine* e, int threads);
 int sorted_threads(const SortedEngine* e);
 
+// Cells along z of a sort bin (a task's particles): 4 (one 4x4x4 brick) or
+// 8 (two bricks stacked along z; half the tasks for the same arenas' shared
+// memory), 0: the default, 4.  A change re-bins the particles before the
+// next substep.  Results do not depend on it.
+int sorted_set_bin_depth(SortedEngine* e, int depth);
+int sorted_bin_depth(const SortedEngine* e);
+
 // Forgets the carried-over state (the next step re-bins and redoes p2g_1).
 void sorted_invalidate(SortedEngine* e);
 

@@ -282,16 +282,26 @@ class MLSMPMSimulator:
     def taskThreads(self, threads: int) -> None:
         _check(self._lib.mpm_set_task_threads(self._handle, int(threads)), "taskThreads")
 
+    @property
+    def binDepth(self) -> int:
+        """Cells along z of the sorted engine's bins (4: one 4x4x4 brick per
+        task, 8: two bricks stacked along z; 0 to set: the default, 4)."""
+        return _check(self._lib.mpm_get_bin_depth(self._handle), "binDepth")
+
+    @binDepth.setter
+    def binDepth(self, depth: int) -> None:
+        _check(self._lib.mpm_set_bin_depth(self._handle, int(depth)), "binDepth")
+
     def tuning(self) -> dict:
         """The engine's tunable configuration."""
-        return {"task_threads": self.taskThreads, "task_size": self.taskSize,
-                "lane_table_min": self.laneTableMin}
+        return {"bin_depth": self.binDepth, "task_threads": self.taskThreads,
+                "task_size": self.taskSize, "lane_table_min": self.laneTableMin}
 
     def autotune(self, substeps: int = 8, cache: str | None = None,
                  key: str | None = None) -> int:
-        """Picks the fastest task-kernel block size, task size and lane-table
-        threshold for the current scene (returns the task size); state
-        unchanged.  cache: a JSON file of earlier choices by workload key
+        """Picks the fastest bin depth, task-kernel block size, task size and
+        lane-table threshold for the current scene (returns the task size);
+        state unchanged.  cache: a JSON file of earlier choices by workload key
         (default key: particle count and grid size); a hit applies the
         stored choice without timing anything, a miss times and stores."""
         key = key or f"MLSMPMSimulator/n={self.numParticles}/cells={self.gridCount}"
@@ -306,6 +316,7 @@ class MLSMPMSimulator:
         return int(choice["task_size"])
 
     def _apply_tuning(self, choice: dict) -> None:
+        self.binDepth = choice.get("bin_depth", 4)
         self.taskThreads = choice["task_threads"]
         self.taskSize = choice["task_size"]
         self.laneTableMin = choice["lane_table_min"]
@@ -555,13 +566,22 @@ class MLSMPMBatch:
     def taskThreads(self, threads: int) -> None:
         _check(self._lib.mpm_batch_set_task_threads(self._handle, int(threads)), "taskThreads")
 
+    @property
+    def binDepth(self) -> int:
+        """See MLSMPMSimulator.binDepth."""
+        return _check(self._lib.mpm_batch_get_bin_depth(self._handle), "binDepth")
+
+    @binDepth.setter
+    def binDepth(self, depth: int) -> None:
+        _check(self._lib.mpm_batch_set_bin_depth(self._handle, int(depth)), "binDepth")
+
     def tuning(self) -> dict:
-        return {"task_threads": self.taskThreads, "task_size": self.taskSize,
-                "lane_table_min": self.laneTableMin}
+        return {"bin_depth": self.binDepth, "task_threads": self.taskThreads,
+                "task_size": self.taskSize, "lane_table_min": self.laneTableMin}
 
     def autotune(self, substeps: int = 4, cache: str | None = None,
                  key: str | None = None) -> int:
-        """Block size, task size and lane-table threshold, as
+        """Bin depth, block size, task size and lane-table threshold, as
         MLSMPMSimulator.autotune (default key: scene and particle counts)."""
         key = key or f"MLSMPMBatch/scenes={self.numScenes}/n={self.numParticles}"
 
@@ -572,6 +592,7 @@ class MLSMPMBatch:
             return self.tuning()
 
         def apply(choice):
+            self.binDepth = choice.get("bin_depth", 4)
             self.taskThreads = choice["task_threads"]
             self.taskSize = choice["task_size"]
             self.laneTableMin = choice["lane_table_min"]
