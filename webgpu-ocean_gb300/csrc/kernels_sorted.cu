@@ -159,8 +159,8 @@ struct Dev {
     uint32_t* bin_count;  // [bins + 1]
     uint32_t* bin_start;  // [bins + 2]
     uint32_t* order;
-    Task* tasks;
-    uint32_t* ntasks;
+    Task* tasks;          // [task_slots]: multi-chunk tasks from the front, the others from the back
+    uint32_t* ntasks;     // [2]: all tasks, multi-chunk tasks
     uint32_t* task_next;  // [3] work counters: p2g_2, g2p+p2g_1, first p2g_1
     // Batches only (null for one scene):
     const Scene* scenes;
@@ -168,6 +168,9 @@ struct Dev {
     const uint32_t* bin_scene;    // global bin -> scene
     int nscenes;
     int task_cap;                 // most particles per task
+    int cap_shift;                // log2(task_cap) when it is a power of two, else -1
+    int chunk;                    // particles per chunk: the task kernels' block size
+    int task_slots;               // entries of `tasks`
     int lane_min;                 // tasks of at least this many particles use the lane table
 };
 
@@ -195,6 +198,13 @@ enum { kCtrP2G2 = 0, kCtrG2P = 1, kCtrP2G1 = 2 };
 // ahead, through a two-slot shared buffer (see the loops below).
 __device__ __forceinline__ int claim_task(const Dev& d, int ctr) {
     return (int)atomicAdd(d.task_next + ctr, 1u);
+}
+
+// Entry of claimed task t: the multi-chunk tasks (nbig of them, stored from
+// the front) are handed out first and the single-chunk ones (stored from the
+// back) last, so that the launch ends on short tasks.
+__device__ __forceinline__ int task_slot(const Dev& d, int nbig, int t) {
+    return t < nbig ? t : d.task_slots - 1 - (t - nbig);
 }
 
 // Stored brick of cell (x, y, z); cells down to -4 and up to the padding's
@@ -456,6 +466,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     int4* __restrict__ grid_all = d.grid[cur];
     unsigned bad = 0;
     const int ntasks = (int)__ldcg(d.ntasks);
+    const int nbig = (int)__ldcg(d.ntasks + 1);
     for (int i = threadIdx.x; i < 2 * 3 * kNA; i += TH) (&s_q[0][0][0])[i] = 0;
     if (threadIdx.x == 0) {
         s_task[0] = claim_task(d, kCtrP2G2);
@@ -482,7 +493,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         for (int q = 0; q < kPer; ++q) m[q] = 0;
         fm = one.k.fm;
         if (t >= ntasks) return;
-        const Task tk = d.tasks[t];
+        const Task tk = d.tasks[task_slot(d, nbig, t)];
         const Scene& ts = scene_ref<BATCH>(d, one, tk.scene);
         fm = ts.k.fm;
         if (tk.bin < 0) return;
@@ -545,7 +556,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         load_mass(t_next, m_next, fm_next);
         if (have_prev) flush(buf ^ 1, prev);
 
-        const Task task = d.tasks[t];
+        const Task task = d.tasks[task_slot(d, nbig, t)];
         const Scene& sc = scene_ref<BATCH>(d, one, task.scene);
         const Geo& g = sc.g;
         const SimConsts& k = sc.k;
@@ -676,6 +687,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     const int ctr = DO_G2P ? kCtrG2P : kCtrP2G1;
     unsigned bad = 0;
     const int ntasks = (int)__ldcg(d.ntasks);
+    const int nbig = (int)__ldcg(d.ntasks + 1);
     for (int i = threadIdx.x; i < 2 * 4 * kNB; i += TH) (&s_a[0][0][0])[i] = 0;
     if (threadIdx.x < 2 * kTouch) (&s_touch[0][0])[threadIdx.x] = 0;
     if (threadIdx.x == 0) {
@@ -701,7 +713,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     // g2p arena of task t (velocities decoded by k_update) into s_v[buf]
     auto prefetch = [&](int t, int buf) {
         if (!DO_G2P || t >= ntasks) return;
-        const Task tk = d.tasks[t];
+        const Task tk = d.tasks[task_slot(d, nbig, t)];
         if (tk.bin < 0) return;
         offsets_for(tk.scene);
         const Scene& ts = scene_ref<BATCH>(d, one, tk.scene);
@@ -766,7 +778,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         prefetch(t_next, buf ^ 1);
         if (have_prev && prev.bin >= 0) flush(buf ^ 1, prev);
 
-        const Task task = d.tasks[t];
+        const Task task = d.tasks[task_slot(d, nbig, t)];
         const Scene& sc = scene_ref<BATCH>(d, one, task.scene);
         const Geo& g = sc.g;
         const SimConsts& k = sc.k;
@@ -922,76 +934,108 @@ __global__ void __launch_bounds__(kTask) k_bin(Particles P, Scene one, Dev d, in
     count_bin(d, active, active ? i : 0, bin_key(sc.g, bin_base<BATCH>(sc), reg, bx, by, bz));
 }
 
-// Exclusive scan of the bin counts -> bin_start and the task list (one task
+// Exclusive scan of the bin counts -> bin_start and the task list: one task
 // per non-empty bin, or several when it holds more than task_cap particles;
-// one_g is a single scene's geometry, batches read theirs from the table).  CTA c scans bins [c*1024, (c+1)*1024); it finds its
-// starting offsets by reducing all earlier counts itself (a few KB to a few
-// hundred KB from L2), so no CTA waits on another.  The counts are zeroed
-// by k_scatter, which runs next.
-__device__ __forceinline__ void block_scan2(uint32_t& a, uint32_t& b, uint32_t* s_a, uint32_t* s_b,
-                                            uint32_t& tot_a, uint32_t& tot_b) {
+// tasks of more than one chunk are stored from the front of the list, the
+// others from the back (task_slot).  one_g is a single scene's geometry;
+// batches read theirs from the table.  CTA c scans bins [c*1024,
+// (c+1)*1024); it finds its starting offsets by reducing all earlier counts
+// itself (a few KB to a few hundred KB from L2), so no CTA waits on another.
+// The counts are zeroed by k_scatter, which runs next.
+
+// Block-wide exclusive scan of N values per thread, in place; tot gets the
+// block's totals.  s: 32 * N words of shared scratch.
+template <int N>
+__device__ __forceinline__ void block_scan(uint32_t (&v)[N], uint32_t (&tot)[N], uint32_t* s) {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    uint32_t ia = a, ib = b;
+    uint32_t inc[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) inc[k] = v[k];
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t ya = __shfl_up_sync(0xffffffffu, ia, o);
-        const uint32_t yb = __shfl_up_sync(0xffffffffu, ib, o);
-        if ((int)lane >= o) { ia += ya; ib += yb; }
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc[k], o);
+            if ((int)lane >= o) inc[k] += y;
+        }
     }
-    if (lane == 31) { s_a[warp] = ia; s_b[warp] = ib; }
+    if (lane == 31) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) s[k * 32 + warp] = inc[k];
+    }
     __syncthreads();
     if (warp == 0) {
-        uint32_t wa = s_a[lane], wb = s_b[lane];
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t ya = __shfl_up_sync(0xffffffffu, wa, o);
-            const uint32_t yb = __shfl_up_sync(0xffffffffu, wb, o);
-            if ((int)lane >= o) { wa += ya; wb += yb; }
+        for (int k = 0; k < N; ++k) {
+            uint32_t w = s[k * 32 + lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if ((int)lane >= o) w += y;
+            }
+            s[k * 32 + lane] = w;
         }
-        s_a[lane] = wa;
-        s_b[lane] = wb;
     }
     __syncthreads();
-    tot_a = s_a[31];
-    tot_b = s_b[31];
-    const uint32_t ea = ia - a + (warp ? s_a[warp - 1] : 0u);
-    const uint32_t eb = ib - b + (warp ? s_b[warp - 1] : 0u);
-    a = ea;
-    b = eb;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        tot[k] = s[k * 32 + 31];
+        v[k] = inc[k] - v[k] + (warp ? s[k * 32 + warp - 1] : 0u);
+    }
 }
 
-__device__ __forceinline__ uint32_t tasks_of(uint32_t c, uint32_t cap) {
-    return (c + cap - 1u) / cap;
+// Full tasks (task_cap particles) of a bin of c particles, and the rest.
+__device__ __forceinline__ void bin_split(const Dev& d, uint32_t c, uint32_t& full, uint32_t& rem) {
+    const uint32_t cap = (uint32_t)d.task_cap;
+    full = d.cap_shift >= 0 ? c >> d.cap_shift : c / cap;
+    rem = c - full * cap;
+}
+
+// Tasks of a bin of c particles: those of more than one chunk, and the others.
+__device__ __forceinline__ void bin_tasks(const Dev& d, uint32_t c, uint32_t& big, uint32_t& small) {
+    uint32_t full, rem;
+    bin_split(d, c, full, rem);
+    const uint32_t th = (uint32_t)d.chunk;
+    const bool cap_big = (uint32_t)d.task_cap > th;
+    big = (cap_big ? full : 0u) + (rem > th ? 1u : 0u);
+    small = (cap_big ? 0u : full) + (rem != 0u && rem <= th ? 1u : 0u);
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, Geo one_g, int nbins) {
-    __shared__ uint32_t s_a[32], s_b[32];
+    __shared__ uint32_t s_scan[3 * 32];
     const int base = blockIdx.x * kScanThreads;
-    const uint32_t cap = (uint32_t)d.task_cap;
-    // counts of all bins before this CTA's range (particles, tasks)
-    uint32_t pre_p = 0, pre_t = 0;
+    // counts of all bins before this CTA's range (particles, big and small tasks)
+    uint32_t pre[3] = {0u, 0u, 0u};
     {
         const uint4* c4 = reinterpret_cast<const uint4*>(d.bin_count);
         const int n4 = base / 4;  // base is a multiple of 1024
         for (int i = threadIdx.x; i < n4; i += kScanThreads) {
             const uint4 q = __ldcg(c4 + i);
-            pre_p += q.x + q.y + q.z + q.w;
-            pre_t += tasks_of(q.x, cap) + tasks_of(q.y, cap) + tasks_of(q.z, cap) +
-                     tasks_of(q.w, cap);
+            const uint32_t cs[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                uint32_t bg, sm;
+                bin_tasks(d, cs[j], bg, sm);
+                pre[0] += cs[j];
+                pre[1] += bg;
+                pre[2] += sm;
+            }
         }
-        uint32_t tp, tt;
-        block_scan2(pre_p, pre_t, s_a, s_b, tp, tt);
-        pre_p = tp;
-        pre_t = tt;
+        uint32_t tot[3];
+        block_scan<3>(pre, tot, s_scan);
+        pre[0] = tot[0];
+        pre[1] = tot[1];
+        pre[2] = tot[2];
     }
-    __syncthreads();  // s_a/s_b reused below
+    __syncthreads();  // s_scan reused below
     const int bin = base + (int)threadIdx.x;
     const uint32_t c = bin < nbins ? __ldcg(d.bin_count + bin) : 0u;
-    const uint32_t nt = tasks_of(c, cap);
-    uint32_t ep = c, et = nt, tot_p, tot_t;
-    block_scan2(ep, et, s_a, s_b, tot_p, tot_t);
+    uint32_t v[3], tot[3];
+    v[0] = c;
+    bin_tasks(d, c, v[1], v[2]);
+    block_scan<3>(v, tot, s_scan);
     if (bin < nbins) {
-        const uint32_t start = pre_p + ep;
+        const uint32_t start = pre[0] + v[0];
         d.bin_start[bin] = start;
         if (c) {
             Task tk;
@@ -1011,16 +1055,22 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, Geo one_g, int nbi
                 tk.z0 = 4 * bz;
                 tk.abase = ((bx * g.PY + by) * g.PZ + bz) * 64;
             }
-            for (uint32_t q = 0; q < nt; ++q) {
+            uint32_t full, rem;
+            bin_split(d, c, full, rem);
+            const uint32_t cap = (uint32_t)d.task_cap;
+            uint32_t jb = pre[1] + v[1], js = pre[2] + v[2];
+            for (uint32_t q = 0; q < full + (rem ? 1u : 0u); ++q) {
                 tk.first = (int)(start + q * cap);
-                tk.count = (int)min(cap, c - q * cap);
-                d.tasks[pre_t + et + q] = tk;
+                tk.count = (int)(q < full ? cap : rem);
+                const int slot = tk.count > d.chunk ? (int)jb++ : d.task_slots - 1 - (int)js++;
+                d.tasks[slot] = tk;
             }
         }
     }
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
-        d.bin_start[nbins] = pre_p + tot_p;
-        *d.ntasks = pre_t + tot_t;
+        d.bin_start[nbins] = pre[0] + tot[0];
+        d.ntasks[0] = pre[1] + tot[1] + pre[2] + tot[2];
+        d.ntasks[1] = pre[1] + tot[1];
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) d.task_next[0] = d.task_next[1] = d.task_next[2] = 0u;
 }
@@ -1245,6 +1295,7 @@ int ensure_grid_state(SortedEngine* e, long long bricks, long long bins) {
     e->grid_cells_alloc = cells;
     e->bricks_alloc = (int)bricks;
     e->max_tasks = (int)max_tasks;
+    e->d.task_slots = (int)max_tasks;
     return 0;
 }
 
@@ -1260,6 +1311,11 @@ void apply_task_cap(SortedEngine* e, long long n) {
     if (cap != e->d.task_cap) drop_graphs(e);
     e->task_cap = cap;
     e->d.task_cap = cap;
+    e->d.cap_shift = -1;
+    if ((cap & (cap - 1)) == 0)
+        for (int sh = 0; sh < 31; ++sh)
+            if ((1 << sh) == cap) e->d.cap_shift = sh;
+    e->d.chunk = e->threads;
 }
 
 }  // namespace
@@ -1270,6 +1326,8 @@ int sorted_create(SortedEngine** out, int max_particles) {
     e->max_particles = max_particles;
     e->d.nscenes = 1;
     e->d.task_cap = kMaxSort;
+    e->d.cap_shift = 10;
+    e->d.chunk = kTask;
     e->d.lane_min = MPM_LANE_TABLE_MIN;
     const size_t np = (size_t)(max_particles > 0 ? max_particles : 1);
     cudaError_t r = cudaMalloc(&e->d.bin_of, 4 * np);
@@ -1277,7 +1335,7 @@ int sorted_create(SortedEngine** out, int max_particles) {
     if (r == cudaSuccess) r = cudaMalloc(&e->d.order, 4 * np);
     if (r == cudaSuccess) r = cudaMalloc(&e->d.dirty_n, 4 * 2);
     if (r == cudaSuccess) r = cudaMalloc(&e->d.ticket, 4);
-    if (r == cudaSuccess) r = cudaMalloc(&e->d.ntasks, 4);
+    if (r == cudaSuccess) r = cudaMalloc(&e->d.ntasks, 4 * 2);
     if (r == cudaSuccess) r = cudaMalloc(&e->d.task_next, 4 * 3);
     if (r == cudaSuccess) {
         e->blocks_p2g2_v[0] = occupancy_blocks((const void*)k_p2g2<false, 128>, 128);
