@@ -822,8 +822,9 @@ def run_ours(args) -> None:
         sim.autotune(AUTOTUNE_SUBSTEPS)
         tuned = {**sim.tuning(),
                  "autotune": f"{AUTOTUNE_SUBSTEPS} substeps after the warm-up steps, over "
-                             "task-kernel block sizes {128, 256, 512} x task sizes {64 ... 1024} "
-                             "x lane-table thresholds {32, 128, 512, off}"}
+                             "z-pair thresholds {0, 256, 512, all} x task-kernel block sizes "
+                             "{128, 256, 512} x task sizes {128 ... 1024} x lane-table "
+                             "thresholds {32, 128, 512, off}"}
         sim.upload(parts, BOX)
         for _ in range(args.warmup):
             sim.execute(stream)

@@ -234,22 +234,24 @@ int mpm_get_lane_table_min(const mpm_sim* sim);
  * particles.  Results do not depend on it. */
 int mpm_set_task_threads(mpm_sim* sim, int threads);
 int mpm_get_task_threads(const mpm_sim* sim);
-/* Sorted engine: cells along z of a sort bin, the unit of a task: 4 (one
- * 4x4x4-cell brick, the default) or 8 (two bricks stacked along z: half the
- * tasks, each with the same shared-memory arenas, which pays when bricks
- * hold few particles); 0 restores the default.  A change re-bins the
- * particles before the next substep.  Results do not depend on it. */
-int mpm_set_bin_depth(mpm_sim* sim, int depth);
-int mpm_get_bin_depth(const mpm_sim* sim);
-/* Autotuner: times `substeps` substeps for each bin depth in {4, 8}, each
- * task-kernel block size in {128, 256, 512}, each task size in {64, 128,
- * 256, 512, 1024} and each lane-table threshold in {32, 128, 512, off} from
- * the current state (each combination once untimed first, so its CUDA
- * graphs are captured outside the timing), keeps the fastest and restores
- * the state (particles, posvel, counters and grid are as before the call).
- * Writes the task size to *chosen_task_size when non-null (the others:
- * mpm_get_bin_depth, mpm_get_task_threads, mpm_get_lane_table_min).
- * Synchronizes. */
+/* Sorted engine: the sort bins are 4x4x4-cell bricks; the bins of two bricks
+ * stacked along z (an aligned pair) whose particles together number at most
+ * `max_particles` (and at most the task size) form one task of 4x4x8 cells
+ * with arenas four cells deeper, so that sparse bricks share a task's fixed
+ * costs.  0 never pairs; 2^30 pairs every pair whose two bins hold
+ * particles (4x4x8-cell bins throughout); INT_MAX restores the default,
+ * 512.  Results do not depend on it. */
+int mpm_set_bin_pairing(mpm_sim* sim, int max_particles);
+int mpm_get_bin_pairing(const mpm_sim* sim);
+/* Autotuner: times `substeps` substeps for each z-pair threshold in {0,
+ * 256, 512, 2^30}, each task-kernel block size in {128, 256, 512}, each task
+ * size in {128, 256, 512, 1024} and each lane-table threshold in {32, 128,
+ * 512, off} from the current state (each combination once untimed first, so
+ * its CUDA graphs are captured outside the timing), keeps the fastest and
+ * restores the state (particles, posvel, counters and grid are as before
+ * the call).  Writes the task size to *chosen_task_size when non-null (the
+ * others: mpm_get_bin_pairing, mpm_get_task_threads,
+ * mpm_get_lane_table_min).  Synchronizes. */
 int mpm_autotune(mpm_sim* sim, int substeps, int* chosen_task_size);
 
 /* Batches: many independent scenes that advance together, one launch per
@@ -294,8 +296,8 @@ int mpm_batch_set_lane_table_min(mpm_batch* batch, int min_particles); /* see mp
 int mpm_batch_get_lane_table_min(const mpm_batch* batch);
 int mpm_batch_set_task_threads(mpm_batch* batch, int threads); /* see mpm_set_task_threads */
 int mpm_batch_get_task_threads(const mpm_batch* batch);
-int mpm_batch_set_bin_depth(mpm_batch* batch, int depth); /* see mpm_set_bin_depth */
-int mpm_batch_get_bin_depth(const mpm_batch* batch);
+int mpm_batch_set_bin_pairing(mpm_batch* batch, int max_particles); /* see mpm_set_bin_pairing */
+int mpm_batch_get_bin_pairing(const mpm_batch* batch);
 /* See mpm_autotune: the batch's particles and posvel are as before the call;
  * mpm_batch_download_grid returns zeros until the next step. */
 int mpm_batch_autotune(mpm_batch* batch, int substeps, int* chosen_task_size);

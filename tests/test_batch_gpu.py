@@ -162,32 +162,32 @@ def test_batch_task_size_and_autotune(cuda, pkg, oracle_mod):
     descs, recs = mixed_scenes(pkg, scene_mod)
     offs = np.concatenate([[0], np.cumsum([d.num_particles for d in descs])])
     results = []
-    configs = ((64, 256, 4), (1024, 256, 4), (128, 128, 4), (512, 512, 4), (64, 256, 8),
-               (1024, 128, 8), (0, 512, 8))
-    for cap, threads, depth in configs:
+    configs = ((64, 256, 0), (1024, 256, 0), (128, 128, 0), (512, 512, 0), (64, 256, 1 << 30),
+               (1024, 128, 1 << 30), (0, 512, 300))
+    for cap, threads, pairing in configs:
         batch = pkg.MLSMPMBatch(descs, recs)
         batch.setTaskSize(cap)
         batch.taskThreads = threads
-        batch.binDepth = depth
-        assert batch.binDepth == depth
+        batch.binPairing = pairing
+        assert batch.binPairing == pairing
         batch.step(3)
-        if depth == 8:  # and back, mid-run: the particles are binned again
-            batch.binDepth = 4
+        if pairing:  # and off, mid-run
+            batch.binPairing = 0
             batch.step(3)
-            batch.binDepth = 8
+            batch.binPairing = pairing
         else:
             batch.step(3)
         results.append(batch.downloadParticles())
         batch.close()
     for r, cfg in zip(results[1:], configs[1:]):
-        assert_bits_equal(results[0], r, f"task size 64 vs (task size, threads, depth) {cfg}")
+        assert_bits_equal(results[0], r, f"task size 64 vs (task size, threads, pairing) {cfg}")
     batch = pkg.MLSMPMBatch(descs, recs)
     batch.step(2)
     before = batch.downloadParticles()
     chosen = batch.autotune(2)
     assert chosen in (64, 128, 256, 512, 1024) and batch.taskSize == chosen
     assert batch.laneTableMin in (32, 128, 512, 1 << 30)
-    assert batch.binDepth in (4, 8)
+    assert batch.binPairing in (0, 256, 512, 1 << 30)
     assert_bits_equal(batch.downloadParticles(), before, "particles after autotune")
     batch.step(4)
     assert_bits_equal(batch.downloadParticles(), results[0], "after autotune")

@@ -402,13 +402,14 @@ def _quirk_scene():
     return parts
 
 
-@pytest.mark.parametrize("depth", [4, 8])
-def test_bin_depth_does_not_change_results(cuda, pkg, oracle_mod, depth):
-    """Bins of one brick (4 cells along z) or of two bricks stacked along z
-    (8), at every block size, with the smallest and the default task sizes
-    and the lane table always or never: same bits as the oracle on the
-    reference's UI scene (60 cells along z: an odd brick count), the 64k
-    lattice, a box of odd sizes and particles past every wall."""
+@pytest.mark.parametrize("pairing", [0, 256, 1 << 30])
+def test_bin_pairing_does_not_change_results(cuda, pkg, oracle_mod, pairing):
+    """One-brick tasks only (0), z pairs of at most 256 particles merged into
+    one task, or every pair whose two bins hold particles (2^30), at every
+    block size, with the smallest and the default task sizes and the lane
+    table always or never: same bits as the oracle on the reference's UI
+    scene (60 cells along z: an odd brick count), the 64k lattice, a box of
+    odd sizes and particles past every wall."""
     from oracle import scene
     cases = [([40.0, 30.0, 60.0], None, 70000),
              ([64.0, 64.0, 64.0], scene.lattice(40, 3.0, 0.5, 0.05, 8), None),
@@ -421,16 +422,16 @@ def test_bin_depth_does_not_change_results(cuda, pkg, oracle_mod, depth):
                 sim.reset(n, box)
             else:
                 sim.upload(parts, box)
-            sim.binDepth = depth
+            sim.binPairing = pairing
             sim.taskThreads = threads
             sim.taskSize = cap
             sim.laneTableMin = lane
-            assert sim.binDepth == depth
+            assert sim.binPairing == pairing
             ref = oracle_mod.OracleSim(sim.downloadParticles(), box)
             for _ in range(4):
                 sim.execute()
                 ref.execute(2, NTHREADS)
-            what = f"box {box}, bin depth {depth}, {threads} threads, task size {cap}, lane {lane}"
+            what = f"box {box}, pairing {pairing}, {threads} threads, task size {cap}, lane {lane}"
             assert_bits_equal(sim.downloadGrid(), ref.cells, what + " grid")
             p = sim.downloadParticles()
             finite = np.isfinite(ref.particles)
@@ -439,28 +440,28 @@ def test_bin_depth_does_not_change_results(cuda, pkg, oracle_mod, depth):
             sim.close()
 
 
-def test_bin_depth_switch_mid_run(cuda, pkg, oracle_mod):
-    """Switching the bin depth between frames re-bins the particles: the run
-    continues bit for bit, and the grid of the last frame stays readable."""
+def test_bin_pairing_switch_mid_run(cuda, pkg, oracle_mod):
+    """Changing the z-pair threshold between frames keeps the run bit for
+    bit, and the grid of the last frame stays readable."""
     box = [40.0, 30.0, 60.0]
     sim = make_sim(pkg, "sorted")
     sim.reset(70000, box)
     ref = oracle_mod.OracleSim(sim.downloadParticles(), box)
     ran = False
-    for depth in (4, 8, 4, 8):
-        sim.binDepth = depth
+    for pairing in (0, 1 << 30, 200, 0, 600):
+        sim.binPairing = pairing
         if ran:
-            assert_bits_equal(sim.downloadGrid(), ref.cells, f"grid after switching to {depth}")
+            assert_bits_equal(sim.downloadGrid(), ref.cells, f"grid after switching to {pairing}")
         for _ in range(2):
             sim.execute()
             ref.execute(2, NTHREADS)
         ran = True
-        assert_state_equal(sim, ref, f"bin depth {depth}")
-    sim.binDepth = 0
-    assert sim.binDepth == 4
-    for bad in (2, 6, 16, -4):
-        with pytest.raises(Exception):
-            sim.binDepth = bad
+        assert_state_equal(sim, ref, f"pairing {pairing}")
+    assert sim.binPairing == 600
+    sim.binPairing = 2**31 - 1
+    assert sim.binPairing == 512
+    with pytest.raises(Exception):
+        sim.binPairing = -1
     sim.close()
 
 
@@ -497,7 +498,7 @@ def test_autotune_keeps_the_state(cuda, pkg, oracle_mod):
     assert chosen in (64, 128, 256, 512, 1024) and sim.taskSize == chosen
     assert sim.laneTableMin in (32, 128, 512, 1 << 30)
     assert sim.taskThreads in (128, 256, 512)
-    assert sim.binDepth in (4, 8)
+    assert sim.binPairing in (0, 256, 512, 1 << 30)
     assert_bits_equal(sim.downloadParticles(), before[0], "particles after autotune")
     assert_bits_equal(sim.downloadGrid(), before[1], "grid after autotune")
     assert_bits_equal(sim.downloadPosvel(), before[2], "posvel after autotune")

@@ -165,10 +165,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "mpm_get_task_threads": (i32, [vp]),
         "mpm_batch_set_task_threads": (i32, [vp, i32]),
         "mpm_batch_get_task_threads": (i32, [vp]),
-        "mpm_set_bin_depth": (i32, [vp, i32]),
-        "mpm_get_bin_depth": (i32, [vp]),
-        "mpm_batch_set_bin_depth": (i32, [vp, i32]),
-        "mpm_batch_get_bin_depth": (i32, [vp]),
+        "mpm_set_bin_pairing": (i32, [vp, i32]),
+        "mpm_get_bin_pairing": (i32, [vp]),
+        "mpm_batch_set_bin_pairing": (i32, [vp, i32]),
+        "mpm_batch_get_bin_pairing": (i32, [vp]),
         "mpm_batch_autotune": (i32, [vp, i32, ctypes.POINTER(ctypes.c_int)]),
         "mpm_batch_create": (i32, [ctypes.POINTER(SceneDesc), i32, fp, ctypes.POINTER(vp)]),
         "mpm_batch_destroy": (i32, [vp]),

@@ -488,15 +488,14 @@ int mpm_get_task_threads(const mpm_sim* s) {
     return s ? sorted_threads(s->sorted) : MPM_E_INVALID;
 }
 
-int mpm_set_bin_depth(mpm_sim* s, int depth) {
+int mpm_set_bin_pairing(mpm_sim* s, int max_particles) {
     if (int rc = check_sim(s)) return rc;
-    DeviceGuard g(s->device);
-    if (sorted_set_bin_depth(s->sorted, depth) != 0) return fail(MPM_E_INVALID, sorted_error());
+    if (sorted_set_pair_max(s->sorted, max_particles) != 0) return fail(MPM_E_INVALID, sorted_error());
     return MPM_OK;
 }
 
-int mpm_get_bin_depth(const mpm_sim* s) {
-    return s ? sorted_bin_depth(s->sorted) : MPM_E_INVALID;
+int mpm_get_bin_pairing(const mpm_sim* s) {
+    return s ? sorted_pair_max(s->sorted) : MPM_E_INVALID;
 }
 
 

@@ -219,15 +219,14 @@ int mpm_batch_get_task_threads(const mpm_batch* b) {
     return b && b->sorted ? sorted_threads(b->sorted) : MPM_E_INVALID;
 }
 
-int mpm_batch_set_bin_depth(mpm_batch* b, int depth) {
+int mpm_batch_set_bin_pairing(mpm_batch* b, int max_particles) {
     if (int rc = check_batch(b)) return rc;
-    DeviceGuard g(b->device);
-    if (sorted_set_bin_depth(b->sorted, depth) != 0) return fail(MPM_E_INVALID, sorted_error());
+    if (sorted_set_pair_max(b->sorted, max_particles) != 0) return fail(MPM_E_INVALID, sorted_error());
     return MPM_OK;
 }
 
-int mpm_batch_get_bin_depth(const mpm_batch* b) {
-    return b && b->sorted ? sorted_bin_depth(b->sorted) : MPM_E_INVALID;
+int mpm_batch_get_bin_pairing(const mpm_batch* b) {
+    return b && b->sorted ? sorted_pair_max(b->sorted) : MPM_E_INVALID;
 }
 
 int mpm_batch_autotune(mpm_batch* b, int substeps, int* chosen_task_size) {

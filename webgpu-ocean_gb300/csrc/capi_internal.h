@@ -64,18 +64,18 @@ long long grid_count_of(const float b[3]);
 // (capi_batch.cu).
 int scene_consts(const mpm_scene_desc& d, SimConsts& k);
 
-// Times `substeps` sorted-engine substeps for each combination of bin depth,
-// task-kernel block size, task size and lane-table threshold from the same
-// saved state and keeps the fastest.  Each candidate first runs once untimed, so that
+// Times `substeps` sorted-engine substeps for each combination of z-pair
+// threshold, task-kernel block size, task size and lane-table threshold from
+// the same saved state and keeps the fastest.  Each candidate first runs once untimed, so that
 // the CUDA graphs the timed run replays are captured outside it.  The state
 // after the call is the state before it (particles, posvel, counters, grid).
 template <class StepFn>
 int tune_engine(SortedEngine* e, ParticleStore& ps, int n, float4* posvel,
                 unsigned long long* counters, int substeps, cudaStream_t st, StepFn step,
                 int* chosen, int* chosen_lane, double* ms_out, int* chosen_threads = nullptr) {
-    static const int kDepths[] = {4, 8};
+    static const int kPairs[] = {0, 256, 512, 1 << 30};
     static const int kThreads[] = {128, 256, 512};
-    static const int kCaps[] = {64, 128, 256, 512, 1024};
+    static const int kCaps[] = {128, 256, 512, 1024};
     static const int kLanes[] = {32, 128, 512, 1 << 30};  // 1 << 30: no lane table
     Particles save{};
     float4* pv = nullptr;
@@ -121,14 +121,14 @@ int tune_engine(SortedEngine* e, ParticleStore& ps, int n, float4* posvel,
         sorted_invalidate(e);
         return cudaGetLastError();
     };
-    int best = 0, best_lane = 0, best_threads = 0, best_depth = 0;
+    int best = 0, best_lane = 0, best_threads = 0, best_pair = 0;
     double best_ms = 0.0;
-    for (int depth : kDepths)
+    for (int pair : kPairs)
     for (int th : kThreads)
     for (int cap : kCaps) {
         for (int lane : kLanes) {
             if (err != cudaSuccess) break;
-            if (sorted_set_bin_depth(e, depth) != 0 || sorted_set_threads(e, th) != 0 ||
+            if (sorted_set_pair_max(e, pair) != 0 || sorted_set_threads(e, th) != 0 ||
                 sorted_set_task_cap(e, cap) != 0 || sorted_set_lane_table_min(e, lane) != 0)
                 continue;
             if ((err = restore()) != cudaSuccess) break;
@@ -145,7 +145,7 @@ int tune_engine(SortedEngine* e, ParticleStore& ps, int n, float4* posvel,
                 best = cap;
                 best_lane = lane;
                 best_threads = th;
-                best_depth = depth;
+                best_pair = pair;
                 best_ms = ms;
             }
         }
@@ -158,7 +158,7 @@ int tune_engine(SortedEngine* e, ParticleStore& ps, int n, float4* posvel,
     cleanup();
     if (err != cudaSuccess) return cuda_fail(err, "autotune");
     if (best) {
-        sorted_set_bin_depth(e, best_depth);
+        sorted_set_pair_max(e, best_pair);
         sorted_set_threads(e, best_threads);
         sorted_set_task_cap(e, best);
         sorted_set_lane_table_min(e, best_lane);

@@ -14,10 +14,13 @@
 //    substep, and kept physically in that order: g2p writes each particle to
 //    its position in the bin order of the other particle buffer (an id array
 //    rides along), so the next substep reads nearly contiguous memory.  A bin
-//    is one brick (4x4x4 cells) or two bricks stacked along z (4x4x8 cells),
-//    chosen per engine (sorted_set_bin_depth) or by the autotuner.
-//  * A task is one bin's particles; CTAs claim tasks from an atomic work
-//    counter and walk a task in chunks of one particle per thread.  In tasks
+//    is one brick; the bins of the two bricks of an aligned z pair are
+//    adjacent in the order.
+//  * A task is one bin's particles, or the particles of both bins of a z
+//    pair (4x4x8 cells) when together they number at most Dev::pair_max (a
+//    runtime parameter, autotuned: sparse bricks then share one task's fixed
+//    costs).  CTAs claim tasks from an atomic work counter and walk a task in
+//    chunks of one particle per thread.  In tasks
 //    of at least Dev::lane_min particles (a runtime parameter, autotuned),
 //    p2g_2 first reorders the bin's particles into a lane table that puts
 //    particles of 32 different shared-memory bank classes in the 32 lanes of
@@ -84,6 +87,15 @@ constexpr int kMaxSort = 1024;   // tasks with more particles keep the bin order
 // p2g_1 dirty-brick flags per task: the 3 x 3 x 4 stored bricks around a bin
 // (a 4x4x8 bin's 8x8x12 arena reaches four bricks along z)
 constexpr int kTouch = 36;
+// Task::bin flag of a z-pair task; arena slot offset flag of the slots only
+// a z-pair task's arena has (az >= 6 in the 6^3 arena, >= 8 in the 8^3 one).
+constexpr int kPairBit = 1 << 30;
+constexpr int kPairSlot = 1 << 30;
+// Default z-pair threshold: on the 1M-particle dam-break, pairs of at most
+// 512 particles gave the fastest whole run of the values tried (0, 128,
+// 256, 512, all).
+constexpr int kPairMaxDefault = 512;
+constexpr int kPairDefaultRequest = INT_MAX;  // sorted_set_pair_max: restore the default
 constexpr int kScanThreads = 1024;
 // A bin holding more than `task_cap` particles is split into tasks of at
 // most task_cap particles (same brick, separate arena flushes), so that small
@@ -117,16 +129,17 @@ struct Geo {
     int BX, BY, BZ;    // bricks per axis covering the grid
     int PY, PZ;        // stored bricks along y and z (the grid's plus padding)
     int nbricks;       // stored bricks: (BX + 2) * PY * PZ
-    int zs;            // log2 of a bin's cells along z: 2 (4x4x4) or 3 (4x4x8)
-    int NZ;            // bins along z
-    int nbins;         // BX * BY * NZ; bin id nbins collects irregular particles
+    int NZ;            // bins along z: BZ rounded up to even (z pairs)
+    int nbins;         // BX * BY * NZ; bin nbins collects irregular particles and
+                       // bin nbins + 1 stays empty (the scene's bins are an even count)
 };
 
 // A task: particles [first, first + count) of the bin order, all in `bin`
-// (scene-local; -1: the scene's bin of irregular particles) of `scene`.
-// (x0, y0, z0) is the bin's first cell; abase the int4 offset (scene-local)
-// of the stored brick (x0/4 - 1, y0/4 - 1, z0/4 - 1), from which the arena
-// slot offsets count.
+// (scene-local; -1: the scene's bin of irregular particles; kPairBit set:
+// also in the next bin, the brick above along z) of `scene`.  (x0, y0, z0)
+// is the bin's first cell; abase the int4 offset (scene-local) of the stored
+// brick (x0/4 - 1, y0/4 - 1, z0/4 - 1), from which the arena slot offsets
+// count.
 struct __align__(16) Task {
     int first;
     int count;
@@ -171,6 +184,7 @@ struct Dev {
     int cap_shift;                // log2(task_cap) when it is a power of two, else -1
     int chunk;                    // particles per chunk: the task kernels' block size
     int task_slots;               // entries of `tasks`
+    int pair_max;                 // z pairs of at most this many particles share a task
     int lane_min;                 // tasks of at least this many particles use the lane table
 };
 
@@ -205,6 +219,11 @@ __device__ __forceinline__ int claim_task(const Dev& d, int ctr) {
 // back) last, so that the launch ends on short tasks.
 __device__ __forceinline__ int task_slot(const Dev& d, int nbig, int t) {
     return t < nbig ? t : d.task_slots - 1 - (t - nbig);
+}
+
+// Cells along z of a task's region: 8 for a z pair, else 4.
+__device__ __forceinline__ unsigned task_zext(const Task& t) {
+    return (t.bin & kPairBit) ? 8u : 4u;
 }
 
 // Stored brick of cell (x, y, z); cells down to -4 and up to the padding's
@@ -284,7 +303,7 @@ __device__ __forceinline__ void count_bin(const Dev& d, bool active, int slot, u
 
 __device__ __forceinline__ uint32_t bin_key(const Geo& g, uint32_t base, bool reg, int bx, int by,
                                            int bz) {
-    return base + (reg ? (uint32_t)(((bx >> 2) * g.BY + (by >> 2)) * g.NZ + (bz >> g.zs))
+    return base + (reg ? (uint32_t)(((bx >> 2) * g.BY + (by >> 2)) * g.NZ + (bz >> 2))
                        : (uint32_t)g.nbins);
 }
 
@@ -319,26 +338,32 @@ __device__ __forceinline__ void clear_dirty(const Dev& d, int gi) {
 
 // int4 offset of arena slot li, counted from the stored brick (x0/4 - 1,
 // y0/4 - 1, z0/4 - 1) of a task's bin at (x0, y0, z0).  The arena spans E
-// cells along x and y and ez along z from (x0 - H, y0 - H, z0 - H) with
-// strides (SX, SY, 1); slots past its extent (padding) and past N give -1.
+// cells along x and y and E + 4 along z (a z pair's) from (x0 - H, y0 - H,
+// z0 - H) with strides (SX, SY, 1); slots past that extent (padding) and
+// past N give -1, slots only a z pair's arena has carry kPairSlot.
 template <int E, int SX, int SY, int H, int N>
-__device__ __forceinline__ int slot_offset(const Geo& g, int li, int ez) {
+__device__ __forceinline__ int slot_offset(const Geo& g, int li) {
     const int ax = li / SX;
     const int r = li - ax * SX;
     const int ay = r / SY;
     const int az = r - ay * SY;
-    if (li >= N || ay >= E || az >= ez) return -1;
+    if (li >= N || ay >= E || az >= E + 4) return -1;
     const int tx = ax + 4 - H, ty = ay + 4 - H, tz = az + 4 - H;
-    return (((tx >> 2) * g.PY + (ty >> 2)) * g.PZ + (tz >> 2)) * 64 + ((tx & 3) << 4) +
-           ((ty & 3) << 2) + (tz & 3);
+    return ((((tx >> 2) * g.PY + (ty >> 2)) * g.PZ + (tz >> 2)) * 64 + ((tx & 3) << 4) +
+            ((ty & 3) << 2) + (tz & 3)) |
+           (az >= E ? kPairSlot : 0);
 }
 
 // The offsets of this thread's slots li = threadIdx.x + q * TH.
 template <int E, int SX, int SY, int H, int N, int TH, int PER>
-__device__ __forceinline__ void slot_offsets(const Geo& g, int ez, int (&off)[PER]) {
+__device__ __forceinline__ void slot_offsets(const Geo& g, int (&off)[PER]) {
 #pragma unroll
-    for (int q = 0; q < PER; ++q)
-        off[q] = slot_offset<E, SX, SY, H, N>(g, (int)threadIdx.x + q * TH, ez);
+    for (int q = 0; q < PER; ++q) off[q] = slot_offset<E, SX, SY, H, N>(g, (int)threadIdx.x + q * TH);
+}
+
+// A slot the task's arena has: its offset (flag cleared), else -1.
+__device__ __forceinline__ int task_offset(int off, bool pair) {
+    return (off < 0 || (!pair && (off & kPairSlot))) ? -1 : (off & ~kPairSlot);
 }
 
 // Global-path mass source (flat indices, as the reference's shaders address).
@@ -392,7 +417,7 @@ __device__ __forceinline__ void build_lane_table(const Particles& P, const Geo& 
         base_cell(x, bx, by, bz);
         const int ax = bx - task.x0, ay = by - task.y0, az = bz - task.z0;
         const bool in = regular_base(g, bx, by, bz) && (unsigned)ax <= 3u && (unsigned)ay <= 3u &&
-                        (unsigned)az < (1u << g.zs);
+                        (unsigned)az < task_zext(task);
         const int cls = in ? ((16 * ax + 12 * ay + az) & 31) : 32;
         const int r = atomicAdd(&lt.cnt[cls], 1);
         lt.tmp[j] = slot;
@@ -477,11 +502,10 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     // off_scene (recomputed when a batch's task belongs to another scene)
     int off[kPer];
     int off_scene = 0;
-    slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPer>(one.g, (1 << one.g.zs) + 2, off);
+    slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPer>(one.g, off);
     auto offsets_for = [&](int scene) {
         if (BATCH && scene != off_scene) {
-            const Geo& tg = scene_ref<BATCH>(d, one, scene).g;
-            slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPer>(tg, (1 << tg.zs) + 2, off);
+            slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPer>(scene_ref<BATCH>(d, one, scene).g, off);
             off_scene = scene;
         }
     };
@@ -500,9 +524,12 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         offsets_for(tk.scene);
         const int* grid = reinterpret_cast<const int*>(
             grid_all + (size_t)brick_base<BATCH>(ts) * 64 + tk.abase);
+        const bool pair = (tk.bin & kPairBit) != 0;
 #pragma unroll
-        for (int q = 0; q < kPer; ++q)
-            if (off[q] >= 0) m[q] = __ldcg(grid + 4 * off[q] + 3);
+        for (int q = 0; q < kPer; ++q) {
+            const int o = task_offset(off[q], pair);
+            if (o >= 0) m[q] = __ldcg(grid + 4 * o + 3);
+        }
     };
     auto store_mass = [&](int buf, const int m[kPer], float fm) {
 #pragma unroll
@@ -526,7 +553,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
             s_q[buf][1][li] = 0;
             s_q[buf][2][li] = 0;
             if (off[q] < 0) continue;  // unreachable: stencils stay inside the arena
-            int* c = grid + 4 * off[q];
+            int* c = grid + 4 * (off[q] & ~kPairSlot);
             if (q0) atomicAdd(c + 0, q0);
             if (q1) atomicAdd(c + 1, q1);
             if (q2) atomicAdd(c + 2, q2);
@@ -565,7 +592,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         const bool table = task.bin >= 0 && task.count <= kMaxSort &&
                            task.count >= d.lane_min;  // uniform
         if (table) build_lane_table<TH>(P, g, d, task, s_lt);
-        const unsigned zext = 1u << g.zs;
+        const unsigned zext = task_zext(task);
         for (int j = threadIdx.x; j < task.count; j += TH) {
             const int slot = table ? (int)s_lt.slot[j] : (int)d.order[task.first + j];
             PState s;
@@ -700,11 +727,10 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     // flush computes those of its touched p2g_1 slots
     int offA[kPerA];
     int off_scene = 0;
-    if (DO_G2P) slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPerA>(one.g, (1 << one.g.zs) + 2, offA);
+    if (DO_G2P) slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPerA>(one.g, offA);
     auto offsets_for = [&](int scene) {
         if (BATCH && DO_G2P && scene != off_scene) {
-            const Geo& tg = scene_ref<BATCH>(d, one, scene).g;
-            slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPerA>(tg, (1 << tg.zs) + 2, offA);
+            slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPerA>(scene_ref<BATCH>(d, one, scene).g, offA);
             off_scene = scene;
         }
     };
@@ -718,16 +744,18 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         offsets_for(tk.scene);
         const Scene& ts = scene_ref<BATCH>(d, one, tk.scene);
         const float4* gvsrc = gv_all + (size_t)brick_base<BATCH>(ts) * 64 + tk.abase;
+        const bool pair = (tk.bin & kPairBit) != 0;
 #pragma unroll
-        for (int q = 0; q < kPerA; ++q)
-            if (offA[q] >= 0) cp_async16(&s_v[buf][(int)threadIdx.x + q * TH], gvsrc + offA[q]);
+        for (int q = 0; q < kPerA; ++q) {
+            const int o = task_offset(offA[q], pair);
+            if (o >= 0) cp_async16(&s_v[buf][(int)threadIdx.x + q * TH], gvsrc + o);
+        }
         cp_async_commit();
     };
     // flush the p2g_1 arena of task tk
     auto flush = [&](int buf, const Task& tk) {
         const Scene& ts = scene_ref<BATCH>(d, one, tk.scene);
         int* gdst = reinterpret_cast<int*>(gdst_all + (size_t)brick_base<BATCH>(ts) * 64 + tk.abase);
-        const int ez = (1 << ts.g.zs) + 4;
 #pragma unroll
         for (int q = 0; q < kPerB; ++q) {
             const int li = (int)threadIdx.x + q * TH;
@@ -739,9 +767,9 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
             s_a[buf][1][li] = 0;
             s_a[buf][2][li] = 0;
             s_a[buf][3][li] = 0;
-            const int o = slot_offset<kB, kSXB, kSYB, 2, kNB>(ts.g, li, ez);
+            const int o = slot_offset<kB, kSXB, kSYB, 2, kNB>(ts.g, li);
             if (o < 0) continue;  // unreachable: stencils stay inside the arena
-            int* c = gdst + 4 * o;
+            int* c = gdst + 4 * (o & ~kPairSlot);
             if (q0) atomicAdd(c + 0, q0);
             if (q1) atomicAdd(c + 1, q1);
             if (q2) atomicAdd(c + 2, q2);
@@ -786,7 +814,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         const uint32_t binb = bin_base<BATCH>(sc);
         const float4* __restrict__ gvsrc = gv_all + (size_t)bb * 64;
         int4* __restrict__ gdst = gdst_all + (size_t)bb * 64;
-        const unsigned zext = 1u << g.zs;
+        const unsigned zext = task_zext(task);
         for (int base = 0; base < task.count; base += TH) {
             const bool active = base + (int)threadIdx.x < task.count;
             const int jo = task.first + base + (active ? (int)threadIdx.x : 0);  // bin order
@@ -1001,6 +1029,30 @@ __device__ __forceinline__ void bin_tasks(const Dev& d, uint32_t c, uint32_t& bi
     small = (cap_big ? 0u : full) + (rem != 0u && rem <= th ? 1u : 0u);
 }
 
+// The bins of a z pair (c0 and c1 particles) share one task: both hold
+// particles and together at most pair_max and task_cap.  A scene's irregular
+// bin is paired with its always-empty last bin, so it never merges.
+__device__ __forceinline__ bool pair_merges(const Dev& d, uint32_t c0, uint32_t c1) {
+    const uint32_t c = c0 + c1;
+    return c0 != 0u && c1 != 0u && c <= (uint32_t)d.pair_max && c <= (uint32_t)d.task_cap;
+}
+
+// Tasks of the z pair of bins (c0, c1 particles), as bin_tasks.
+__device__ __forceinline__ void pair_tasks(const Dev& d, uint32_t c0, uint32_t c1, uint32_t& big,
+                                           uint32_t& small) {
+    if (pair_merges(d, c0, c1)) {
+        const bool b = c0 + c1 > (uint32_t)d.chunk;
+        big = b ? 1u : 0u;
+        small = b ? 0u : 1u;
+        return;
+    }
+    uint32_t b0, s0, b1, s1;
+    bin_tasks(d, c0, b0, s0);
+    bin_tasks(d, c1, b1, s1);
+    big = b0 + b1;
+    small = s0 + s1;
+}
+
 __global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, Geo one_g, int nbins) {
     __shared__ uint32_t s_scan[3 * 32];
     const int base = blockIdx.x * kScanThreads;
@@ -1010,16 +1062,15 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, Geo one_g, int nbi
         const uint4* c4 = reinterpret_cast<const uint4*>(d.bin_count);
         const int n4 = base / 4;  // base is a multiple of 1024
         for (int i = threadIdx.x; i < n4; i += kScanThreads) {
-            const uint4 q = __ldcg(c4 + i);
-            const uint32_t cs[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                uint32_t bg, sm;
-                bin_tasks(d, cs[j], bg, sm);
-                pre[0] += cs[j];
-                pre[1] += bg;
-                pre[2] += sm;
-            }
+            const uint4 q = __ldcg(c4 + i);  // two z pairs
+            uint32_t bg, sm;
+            pair_tasks(d, q.x, q.y, bg, sm);
+            pre[1] += bg;
+            pre[2] += sm;
+            pair_tasks(d, q.z, q.w, bg, sm);
+            pre[1] += bg;
+            pre[2] += sm;
+            pre[0] += q.x + q.y + q.z + q.w;
         }
         uint32_t tot[3];
         block_scan<3>(pre, tot, s_scan);
@@ -1030,14 +1081,23 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, Geo one_g, int nbi
     __syncthreads();  // s_scan reused below
     const int bin = base + (int)threadIdx.x;
     const uint32_t c = bin < nbins ? __ldcg(d.bin_count + bin) : 0u;
+    const uint32_t cpart = __shfl_xor_sync(0xffffffffu, c, 1);  // the other bin of the z pair
+    const bool lead = (bin & 1) == 0;
+    const bool merged = pair_merges(d, c, cpart);
     uint32_t v[3], tot[3];
     v[0] = c;
-    bin_tasks(d, c, v[1], v[2]);
+    if (merged) {  // the pair's task belongs to its first bin
+        const bool b = c + cpart > (uint32_t)d.chunk;
+        v[1] = lead && b ? 1u : 0u;
+        v[2] = lead && !b ? 1u : 0u;
+    } else {
+        bin_tasks(d, c, v[1], v[2]);
+    }
     block_scan<3>(v, tot, s_scan);
     if (bin < nbins) {
         const uint32_t start = pre[0] + v[0];
         d.bin_start[bin] = start;
-        if (c) {
+        if (c && (lead || !merged)) {
             Task tk;
             tk.scene = d.bin_scene ? (int)__ldg(d.bin_scene + bin) : 0;
             const Geo& g = d.bin_scene ? d.scenes[tk.scene].g : one_g;
@@ -1049,14 +1109,20 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, Geo one_g, int nbi
                 const int bx = local / byz;
                 const int r = local - bx * byz;
                 const int by = r / g.NZ;
-                const int bz = (r - by * g.NZ) << (g.zs - 2);  // in bricks
+                const int bz = r - by * g.NZ;
                 tk.x0 = 4 * bx;
                 tk.y0 = 4 * by;
                 tk.z0 = 4 * bz;
                 tk.abase = ((bx * g.PY + by) * g.PZ + bz) * 64;
             }
             uint32_t full, rem;
-            bin_split(d, c, full, rem);
+            if (merged) {
+                tk.bin |= kPairBit;
+                full = 0u;
+                rem = c + cpart;
+            } else {
+                bin_split(d, c, full, rem);
+            }
             const uint32_t cap = (uint32_t)d.task_cap;
             uint32_t jb = pre[1] + v[1], js = pre[2] + v[2];
             for (uint32_t q = 0; q < full + (rem ? 1u : 0u); ++q) {
@@ -1175,7 +1241,6 @@ struct SortedEngine {
     int task_cap = kMaxSort;     // most particles per task (see kMinTaskCap)
     bool task_cap_auto = true;   // task_cap follows the particle count
     int ncells_linear = 0;       // batch: cells of all scenes' reference-layout grids
-    int zs = 2;                  // log2 of a bin's cells along z (Geo::zs)
     std::vector<GraphEntry> graphs;
 };
 
@@ -1238,17 +1303,9 @@ int occupancy_blocks(const void* fn, int threads) {
     return nsm * per;
 }
 
-// Bins along z and in all for a bin depth of 1 << zs cells.
-void set_bins(Geo& g, int zs) {
-    g.zs = zs;
-    const int per = 1 << (zs - 2);  // bricks per bin along z
-    g.NZ = (g.BZ + per - 1) / per;
-    g.nbins = g.BX * g.BY * g.NZ;
-}
-
 // Brick geometry of one scene; false for a degenerate box or one too large
 // for i32 cell addresses.
-bool make_geo(const SimConsts& k, int zs, Geo& g) {
+bool make_geo(const SimConsts& k, Geo& g) {
     if (k.Y <= 0 || k.Z <= 0 || k.grid_count <= 0) return false;
     g = Geo{};
     g.Y = k.Y;
@@ -1268,12 +1325,16 @@ bool make_geo(const SimConsts& k, int zs, Geo& g) {
     const long long nb = (long long)(g.BX + 2) * g.PY * g.PZ;
     if (nb * 64 > INT_MAX) return false;
     g.nbricks = (int)nb;
-    set_bins(g, zs);
+    g.NZ = (g.BZ + 1) & ~1;
+    const long long nbins = (long long)g.BX * g.BY * g.NZ;
+    if (nbins + 2 > INT_MAX / 2) return false;
+    g.nbins = (int)nbins;
     return true;
 }
 
-// Bins of a scene at the finest bin depth (the bin arrays' size).
-long long max_bins(const Geo& g) { return (long long)g.BX * g.BY * g.BZ + 1; }
+// Bins of a scene: its bricks' (z rounded up to pairs), the irregular bin
+// and an empty one.
+long long scene_bins(const Geo& g) { return (long long)g.nbins + 2; }
 
 // Grids, dirty lists, bin arrays and the task list for `bricks` bricks and
 // `bins` bins (kept when large enough).
@@ -1328,6 +1389,7 @@ int sorted_create(SortedEngine** out, int max_particles) {
     e->d.task_cap = kMaxSort;
     e->d.cap_shift = 10;
     e->d.chunk = kTask;
+    e->d.pair_max = kPairMaxDefault;
     e->d.lane_min = MPM_LANE_TABLE_MIN;
     const size_t np = (size_t)(max_particles > 0 ? max_particles : 1);
     cudaError_t r = cudaMalloc(&e->d.bin_of, 4 * np);
@@ -1377,7 +1439,7 @@ int sorted_configure(SortedEngine* e, const SimConsts& k) {
     e->primed = false;
     e->has_grid = false;
     Geo g;
-    if (!make_geo(k, e->zs, g)) return -1;
+    if (!make_geo(k, g)) return -1;
     // Captured graphs hold the scene by value: they stay valid across a
     // reconfiguration with the same constants and geometry (a re-upload of
     // the same scene) and are dropped otherwise.
@@ -1385,13 +1447,13 @@ int sorted_configure(SortedEngine* e, const SimConsts& k) {
     one.g = g;
     one.k = k;
     if (e->batch || std::memcmp(&one, &e->one, sizeof(Scene)) != 0) drop_graphs(e);
-    if (ensure_grid_state(e, g.nbricks, max_bins(g))) return -1;
+    if (ensure_grid_state(e, g.nbricks, scene_bins(g))) return -1;
     free_tables(e);
     e->batch = false;
     e->scenes.clear();
     e->one = one;
     e->nbricks = g.nbricks;
-    e->nbins = g.nbins + 1;
+    e->nbins = (int)scene_bins(g);
     apply_task_cap(e, k.n);
     e->configured = true;
     return 0;
@@ -1406,9 +1468,9 @@ int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes) {
         return -1;
     }
     std::vector<Scene> hs((size_t)nscenes);
-    long long bricks = 0, bins = 0, bins_alloc = 0, parts = 0, lcells = 0;
+    long long bricks = 0, bins = 0, parts = 0, lcells = 0;
     for (int s = 0; s < nscenes; ++s) {
-        if (!make_geo(ks[s], e->zs, hs[s].g)) {
+        if (!make_geo(ks[s], hs[s].g)) {
             g_err = "scene " + std::to_string(s) + " has a degenerate box";
             return -1;
         }
@@ -1418,8 +1480,7 @@ int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes) {
         hs[s].lbase = (int)lcells;
         hs[s].k = ks[s];
         bricks += hs[s].g.nbricks;
-        bins += (long long)hs[s].g.nbins + 1;
-        bins_alloc += max_bins(hs[s].g);
+        bins += scene_bins(hs[s].g);
         parts += ks[s].n;
         lcells += ks[s].grid_count;
         if (bricks * 64 > INT_MAX || parts > e->max_particles || lcells > INT_MAX) {
@@ -1428,16 +1489,21 @@ int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes) {
         }
     }
     drop_graphs(e);
-    if (ensure_grid_state(e, bricks, bins_alloc)) return -1;
+    if (bins > INT_MAX / 2) {
+        g_err = "batch exceeds the engine's capacity";
+        return -1;
+    }
+    if (ensure_grid_state(e, bricks, bins)) return -1;
     free_tables(e);
     std::vector<uint32_t> brick_scene((size_t)bricks), bin_scene((size_t)bins);
     for (int s = 0; s < nscenes; ++s) {
         for (int b = 0; b < hs[s].g.nbricks; ++b) brick_scene[(size_t)hs[s].bbase + b] = (uint32_t)s;
-        for (int b = 0; b <= hs[s].g.nbins; ++b) bin_scene[(size_t)hs[s].binbase + b] = (uint32_t)s;
+        for (long long b = 0; b < scene_bins(hs[s].g); ++b)
+            bin_scene[(size_t)hs[s].binbase + b] = (uint32_t)s;
     }
     SE_CUDA(cudaMalloc(&e->scenes_d, sizeof(Scene) * (size_t)nscenes));
     SE_CUDA(cudaMalloc(&e->brick_scene_d, 4 * (size_t)bricks));
-    SE_CUDA(cudaMalloc(&e->bin_scene_d, 4 * (size_t)bins_alloc));
+    SE_CUDA(cudaMalloc(&e->bin_scene_d, 4 * (size_t)bins));
     SE_CUDA(cudaMemcpy(e->scenes_d, hs.data(), sizeof(Scene) * (size_t)nscenes, cudaMemcpyHostToDevice));
     SE_CUDA(cudaMemcpy(e->brick_scene_d, brick_scene.data(), 4 * (size_t)bricks, cudaMemcpyHostToDevice));
     SE_CUDA(cudaMemcpy(e->bin_scene_d, bin_scene.data(), 4 * (size_t)bins, cudaMemcpyHostToDevice));
@@ -1507,45 +1573,19 @@ int sorted_set_threads(SortedEngine* e, int threads) {
 
 int sorted_threads(const SortedEngine* e) { return e->threads; }
 
-int sorted_set_bin_depth(SortedEngine* e, int depth) {
-    if (depth == 0) depth = 4;
-    if (depth != 4 && depth != 8) {
-        g_err = "bin depth must be 4 or 8 cells (0: default 4)";
+int sorted_set_pair_max(SortedEngine* e, int max_particles) {
+    if (max_particles < 0) {
+        g_err = "z-pair threshold must be >= 0 (0: never pair)";
         return -1;
     }
-    const int zs = depth == 8 ? 3 : 2;
-    if (zs == e->zs) return 0;
-    e->zs = zs;
-    if (!e->configured) return 0;
-    drop_graphs(e);
-    e->primed = false;  // the particles are binned again before the next substep
-    if (!e->batch) {
-        set_bins(e->one.g, zs);
-        e->nbins = e->one.g.nbins + 1;
-        return 0;
-    }
-    // the scene table and the bin -> scene map change; no launch may read
-    // them meanwhile
-    SE_CUDA(cudaDeviceSynchronize());
-    long long bins = 0;
-    for (Scene& sc : e->scenes) {
-        set_bins(sc.g, zs);
-        sc.binbase = (int)bins;
-        bins += (long long)sc.g.nbins + 1;
-    }
-    std::vector<uint32_t> bin_scene((size_t)bins);
-    for (size_t s = 0; s < e->scenes.size(); ++s)
-        for (int b = 0; b <= e->scenes[s].g.nbins; ++b)
-            bin_scene[(size_t)e->scenes[s].binbase + b] = (uint32_t)s;
-    SE_CUDA(cudaMemcpy(e->scenes_d, e->scenes.data(), sizeof(Scene) * e->scenes.size(),
-                       cudaMemcpyHostToDevice));
-    SE_CUDA(cudaMemcpy(e->bin_scene_d, bin_scene.data(), 4 * (size_t)bins, cudaMemcpyHostToDevice));
-    e->one = e->scenes[0];
-    e->nbins = (int)bins;
+    if (max_particles == kPairDefaultRequest) max_particles = kPairMaxDefault;
+    if (max_particles == e->d.pair_max) return 0;
+    drop_graphs(e);  // the captured launches carry it
+    e->d.pair_max = max_particles;
     return 0;
 }
 
-int sorted_bin_depth(const SortedEngine* e) { return 1 << e->zs; }
+int sorted_pair_max(const SortedEngine* e) { return e->d.pair_max; }
 
 int sorted_set_scene_consts(SortedEngine* e, int scene, const SimConsts& k, cudaStream_t st) {
     if (!e->configured || !e->batch || scene < 0 || scene >= (int)e->scenes.size()) {

@@ -45,12 +45,14 @@ int sorted_lane_table_min(const SortedEngine* e);
 int sorted_set_threads(SortedEngine* e, int threads);
 int sorted_threads(const SortedEngine* e);
 
-// Cells along z of a sort bin (a task's particles): 4 (one 4x4x4 brick) or
-// 8 (two bricks stacked along z; half the tasks for the same arenas' shared
-// memory), 0: the default, 4.  A change re-bins the particles before the
-// next substep.  Results do not depend on it.
-int sorted_set_bin_depth(SortedEngine* e, int depth);
-int sorted_bin_depth(const SortedEngine* e);
+// The bins of two bricks stacked along z (an aligned pair) whose particles
+// together number at most max_particles (and at most the task size) share
+// one task, with a 4x4x8-cell region and arenas 4 cells deeper: sparse
+// bricks then share the fixed costs of a task.  0 never pairs; 2^30 pairs
+// every pair whose two bins hold particles; INT_MAX restores the default
+// (512).  Results do not depend on it.
+int sorted_set_pair_max(SortedEngine* e, int max_particles);
+int sorted_pair_max(const SortedEngine* e);
 
 // Forgets the carried-over state (the next step re-bins and redoes p2g_1).
 void sorted_invalidate(SortedEngine* e);

@@ -283,25 +283,27 @@ class MLSMPMSimulator:
         _check(self._lib.mpm_set_task_threads(self._handle, int(threads)), "taskThreads")
 
     @property
-    def binDepth(self) -> int:
-        """Cells along z of the sorted engine's bins (4: one 4x4x4 brick per
-        task, 8: two bricks stacked along z; 0 to set: the default, 4)."""
-        return _check(self._lib.mpm_get_bin_depth(self._handle), "binDepth")
+    def binPairing(self) -> int:
+        """Two 4x4x4-cell bins stacked along z whose particles together
+        number at most this share one task (default 512; 0: never; 2**30:
+        every pair whose bins both hold particles; 2**31 - 1 to set: the
+        default)."""
+        return _check(self._lib.mpm_get_bin_pairing(self._handle), "binPairing")
 
-    @binDepth.setter
-    def binDepth(self, depth: int) -> None:
-        _check(self._lib.mpm_set_bin_depth(self._handle, int(depth)), "binDepth")
+    @binPairing.setter
+    def binPairing(self, max_particles: int) -> None:
+        _check(self._lib.mpm_set_bin_pairing(self._handle, int(max_particles)), "binPairing")
 
     def tuning(self) -> dict:
         """The engine's tunable configuration."""
-        return {"bin_depth": self.binDepth, "task_threads": self.taskThreads,
+        return {"bin_pairing": self.binPairing, "task_threads": self.taskThreads,
                 "task_size": self.taskSize, "lane_table_min": self.laneTableMin}
 
     def autotune(self, substeps: int = 8, cache: str | None = None,
                  key: str | None = None) -> int:
-        """Picks the fastest bin depth, task-kernel block size, task size and
-        lane-table threshold for the current scene (returns the task size);
-        state unchanged.  cache: a JSON file of earlier choices by workload key
+        """Picks the fastest z-pair threshold, task-kernel block size, task
+        size and lane-table threshold for the current scene (returns the task
+        size); state unchanged.  cache: a JSON file of earlier choices by workload key
         (default key: particle count and grid size); a hit applies the
         stored choice without timing anything, a miss times and stores."""
         key = key or f"MLSMPMSimulator/n={self.numParticles}/cells={self.gridCount}"
@@ -316,7 +318,7 @@ class MLSMPMSimulator:
         return int(choice["task_size"])
 
     def _apply_tuning(self, choice: dict) -> None:
-        self.binDepth = choice.get("bin_depth", 4)
+        self.binPairing = choice.get("bin_pairing", 2**31 - 1)
         self.taskThreads = choice["task_threads"]
         self.taskSize = choice["task_size"]
         self.laneTableMin = choice["lane_table_min"]
@@ -567,22 +569,22 @@ class MLSMPMBatch:
         _check(self._lib.mpm_batch_set_task_threads(self._handle, int(threads)), "taskThreads")
 
     @property
-    def binDepth(self) -> int:
-        """See MLSMPMSimulator.binDepth."""
-        return _check(self._lib.mpm_batch_get_bin_depth(self._handle), "binDepth")
+    def binPairing(self) -> int:
+        """See MLSMPMSimulator.binPairing."""
+        return _check(self._lib.mpm_batch_get_bin_pairing(self._handle), "binPairing")
 
-    @binDepth.setter
-    def binDepth(self, depth: int) -> None:
-        _check(self._lib.mpm_batch_set_bin_depth(self._handle, int(depth)), "binDepth")
+    @binPairing.setter
+    def binPairing(self, max_particles: int) -> None:
+        _check(self._lib.mpm_batch_set_bin_pairing(self._handle, int(max_particles)), "binPairing")
 
     def tuning(self) -> dict:
-        return {"bin_depth": self.binDepth, "task_threads": self.taskThreads,
+        return {"bin_pairing": self.binPairing, "task_threads": self.taskThreads,
                 "task_size": self.taskSize, "lane_table_min": self.laneTableMin}
 
     def autotune(self, substeps: int = 4, cache: str | None = None,
                  key: str | None = None) -> int:
-        """Bin depth, block size, task size and lane-table threshold, as
-        MLSMPMSimulator.autotune (default key: scene and particle counts)."""
+        """Z-pair threshold, block size, task size and lane-table threshold,
+        as MLSMPMSimulator.autotune (default key: scene and particle counts)."""
         key = key or f"MLSMPMBatch/scenes={self.numScenes}/n={self.numParticles}"
 
         def run():
@@ -592,7 +594,7 @@ class MLSMPMBatch:
             return self.tuning()
 
         def apply(choice):
-            self.binDepth = choice.get("bin_depth", 4)
+            self.binPairing = choice.get("bin_pairing", 2**31 - 1)
             self.taskThreads = choice["task_threads"]
             self.taskSize = choice["task_size"]
             self.laneTableMin = choice["lane_table_min"]
