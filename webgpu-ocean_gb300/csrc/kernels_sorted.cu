@@ -97,6 +97,9 @@ constexpr int kPairSlot = 1 << 30;
 constexpr int kPairMaxDefault = 512;
 constexpr int kPairDefaultRequest = INT_MAX;  // sorted_set_pair_max: restore the default
 constexpr int kScanThreads = 1024;
+// With more bin chunks (of kScanThreads bins) than this, k_chunk_sums sums
+// each chunk once before k_scan.
+constexpr int kChunkedScanMin = 64;
 // A bin holding more than `task_cap` particles is split into tasks of at
 // most task_cap particles (same brick, separate arena flushes), so that small
 // scenes, whose bricks are few and full, still spread over every SM.
@@ -171,6 +174,7 @@ struct Dev {
     uint32_t* rank_of;
     uint32_t* bin_count;  // [bins + 1]
     uint32_t* bin_start;  // [bins + 2]
+    uint32_t* chunk_sum;  // [3 * chunks]: per 1024 bins, particles and multi-/single-chunk tasks
     uint32_t* order;
     Task* tasks;          // [task_slots]: multi-chunk tasks from the front, the others from the back
     uint32_t* ntasks;     // [2]: all tasks, multi-chunk tasks
@@ -1053,30 +1057,57 @@ __device__ __forceinline__ void pair_tasks(const Dev& d, uint32_t c0, uint32_t c
     small = s0 + s1;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, Geo one_g, int nbins) {
+// Sum of a range of bins' particles and tasks (four bins, two z pairs,
+// per uint4), reduced over the block into pre[] (every thread gets it).
+__device__ __forceinline__ void sum_bins(const Dev& d, int b0, int b1, uint32_t (&pre)[3],
+                                         uint32_t* s_scan) {
+    pre[0] = pre[1] = pre[2] = 0u;
+    const uint4* c4 = reinterpret_cast<const uint4*>(d.bin_count);
+    for (int i = b0 / 4 + threadIdx.x; i < b1 / 4; i += kScanThreads) {
+        const uint4 q = __ldcg(c4 + i);  // two z pairs
+        uint32_t bg, sm;
+        pair_tasks(d, q.x, q.y, bg, sm);
+        pre[1] += bg;
+        pre[2] += sm;
+        pair_tasks(d, q.z, q.w, bg, sm);
+        pre[1] += bg;
+        pre[2] += sm;
+        pre[0] += q.x + q.y + q.z + q.w;
+    }
+    uint32_t tot[3];
+    block_scan<3>(pre, tot, s_scan);
+    pre[0] = tot[0];
+    pre[1] = tot[1];
+    pre[2] = tot[2];
+}
+
+// Per-chunk sums for k_scan when there are many chunks (otherwise each
+// k_scan CTA reduces all earlier bins itself, which costs a quadratic
+// number of reads).  The bin counts beyond nbins are zero.
+__global__ void __launch_bounds__(kScanThreads) k_chunk_sums(Dev d) {
+    __shared__ uint32_t s_scan[3 * 32];
+    uint32_t pre[3];
+    sum_bins(d, blockIdx.x * kScanThreads, (blockIdx.x + 1) * kScanThreads, pre, s_scan);
+    if (threadIdx.x < 3) d.chunk_sum[3 * blockIdx.x + threadIdx.x] = pre[threadIdx.x];
+}
+
+// chunked: k_chunk_sums ran before (chunk_sum holds every chunk's sums).
+__global__ void __launch_bounds__(kScanThreads) k_scan(Dev d, Geo one_g, int nbins, int chunked) {
     __shared__ uint32_t s_scan[3 * 32];
     const int base = blockIdx.x * kScanThreads;
     // counts of all bins before this CTA's range (particles, big and small tasks)
     uint32_t pre[3] = {0u, 0u, 0u};
-    {
-        const uint4* c4 = reinterpret_cast<const uint4*>(d.bin_count);
-        const int n4 = base / 4;  // base is a multiple of 1024
-        for (int i = threadIdx.x; i < n4; i += kScanThreads) {
-            const uint4 q = __ldcg(c4 + i);  // two z pairs
-            uint32_t bg, sm;
-            pair_tasks(d, q.x, q.y, bg, sm);
-            pre[1] += bg;
-            pre[2] += sm;
-            pair_tasks(d, q.z, q.w, bg, sm);
-            pre[1] += bg;
-            pre[2] += sm;
-            pre[0] += q.x + q.y + q.z + q.w;
-        }
+    if (chunked) {
+        for (int c = threadIdx.x; c < (int)blockIdx.x; c += kScanThreads)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) pre[k] += __ldcg(d.chunk_sum + 3 * c + k);
         uint32_t tot[3];
         block_scan<3>(pre, tot, s_scan);
         pre[0] = tot[0];
         pre[1] = tot[1];
         pre[2] = tot[2];
+    } else {
+        sum_bins(d, 0, base, pre, s_scan);
     }
     __syncthreads();  // s_scan reused below
     const int bin = base + (int)threadIdx.x;
@@ -1275,8 +1306,9 @@ void free_grid_state(SortedEngine* e) {
     }
     cudaFree(e->d.bin_count);
     cudaFree(e->d.bin_start);
+    cudaFree(e->d.chunk_sum);
     cudaFree(e->d.tasks);
-    e->d.bin_count = e->d.bin_start = nullptr;
+    e->d.bin_count = e->d.bin_start = e->d.chunk_sum = nullptr;
     e->d.tasks = nullptr;
     e->grid_cells_alloc = 0;
     e->bricks_alloc = 0;
@@ -1352,6 +1384,7 @@ int ensure_grid_state(SortedEngine* e, long long bricks, long long bins) {
     }
     SE_CUDA(cudaMalloc(&e->d.bin_count, 4 * ((size_t)bins + kScanThreads)));
     SE_CUDA(cudaMalloc(&e->d.bin_start, 4 * ((size_t)bins + 1)));
+    SE_CUDA(cudaMalloc(&e->d.chunk_sum, 4 * 3 * ((size_t)bins / kScanThreads + 2)));
     SE_CUDA(cudaMalloc(&e->d.tasks, sizeof(Task) * (size_t)max_tasks));
     e->grid_cells_alloc = cells;
     e->bricks_alloc = (int)bricks;
@@ -1664,6 +1697,15 @@ void launch_g2p(SortedEngine* e, const Particles& Pin, const Particles& Pout,
     }
 }
 
+// The counting sort's scan (and, for many bins, the chunk sums before it).
+void launch_scan(SortedEngine* e, const Scene& one, int nbins, cudaStream_t st,
+                 LaunchProfiler* prof) {
+    const int chunks = (nbins + kScanThreads - 1) / kScanThreads;
+    const int chunked = chunks > kChunkedScanMin ? 1 : 0;
+    if (chunked) LAUNCH(KID_SCAN, (k_chunk_sums<<<chunks, kScanThreads, 0, st>>>(e->d)));
+    LAUNCH(KID_SCAN, (k_scan<<<chunks, kScanThreads, 0, st>>>(e->d, one.g, nbins, chunked)));
+}
+
 // Issues the kernels of `substeps` substeps and advances the engine state.
 template <bool BATCH>
 int enqueue_substeps(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned long long* oob,
@@ -1682,7 +1724,7 @@ int enqueue_substeps(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigne
             LAUNCH(KID_SORTED_G2P_P2G_1,
                    (launch_g2p<BATCH, true, false>(e, ps->P[pin], ps->P[pout], ps->id[pin],
                                                    ps->id[pout], posvel, one, cur, nxt, oob, st)));
-        LAUNCH(KID_SCAN, (k_scan<<<(nbins + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(e->d, one.g, nbins)));
+        launch_scan(e, one, nbins, st, prof);
         LAUNCH(KID_SCATTER, (k_scatter<<<(max(n, nbins) + 255) / 256, 256, 0, st>>>(e->d, n, nbins)));
         e->last = cur;
         e->cur = nxt;
@@ -1706,10 +1748,11 @@ int prime(SortedEngine* e, ParticleStore* ps, float4* posvel, unsigned long long
     SE_CUDA(cudaMemsetAsync(e->d.dirty_n, 0, 8, st));
     SE_CUDA(cudaMemsetAsync(e->d.ticket, 0, 4, st));
     SE_CUDA(cudaMemsetAsync(e->d.task_next, 0, 4 * 3, st));
-    SE_CUDA(cudaMemsetAsync(e->d.bin_count, 0, 4 * (size_t)nbins, st));
+    // k_chunk_sums reads the whole last chunk: the counts past nbins stay zero
+    SE_CUDA(cudaMemsetAsync(e->d.bin_count, 0, 4 * ((size_t)nbins + kScanThreads), st));
     const Particles& P = ps->P[ps->cur];
     LAUNCH(KID_BIN, (k_bin<BATCH><<<(n + kTask - 1) / kTask, kTask, 0, st>>>(P, one, e->d, n)));
-    LAUNCH(KID_SCAN, (k_scan<<<(nbins + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(e->d, one.g, nbins)));
+    launch_scan(e, one, nbins, st, prof);
     LAUNCH(KID_SCATTER, (k_scatter<<<(max(n, nbins) + 255) / 256, 256, 0, st>>>(e->d, n, nbins)));
     e->cur = 0;
     LAUNCH(KID_SORTED_P2G_1,
