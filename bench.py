@@ -312,10 +312,10 @@ def run_reference(args) -> None:
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
 # capture of `bench.py --quick` on this workload: its posvel-writing variant
 # (profiles/k_g2p_p2g1_1M_128.md).
-MEASURED_TRAFFIC_PER_LAUNCH = {"sorted_g2p_p2g_1": 95.2e6}
+MEASURED_TRAFFIC_PER_LAUNCH = {"sorted_g2p_p2g_1": 96.26e6}
 # ncu smsp__inst_executed.sum of one launch at the early dam-break state
 # (profiles/k_g2p_p2g1_1M_128.md): the instruction-issue roofline.
-MEASURED_WARP_INSTRUCTIONS_PER_LAUNCH = {"sorted_g2p_p2g_1": 76.7e6}
+MEASURED_WARP_INSTRUCTIONS_PER_LAUNCH = {"sorted_g2p_p2g_1": 69.55e6}
 
 
 def algorithmic_bytes(kernel: str, n: int, cells: int) -> float | None:
@@ -426,6 +426,28 @@ def measure_batched(pkg, torch, stream, repeats: int = 3, autotune: bool = True)
 
     plain_ms = loop_ms(False)
     graph_ms = loop_ms(True)
+
+    def loop_initial_ms(graph: bool) -> float:
+        # the same 100 substeps from the scenes' initial state (uploads
+        # outside the timed region), best of 2
+        best = None
+        for _ in range(2):
+            for s, sim in enumerate(sims):
+                sim.setGraph(graph)
+                sim.upload(recs[offs[s]:offs[s + 1]], list(descs[s].init_box))
+            stream.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for sim in sims:
+                sim.execute(stream, substeps=K)
+            b.record(stream)
+            torch.cuda.synchronize()
+            t = a.elapsed_time(b)
+            best = t if best is None else min(best, t)
+        return best
+
+    plain_first_ms = loop_initial_ms(False)
+    graph_first_ms = loop_initial_ms(True)
     for sim in sims:
         sim.close()
     batch.close()
@@ -466,7 +488,12 @@ def measure_batched(pkg, torch, stream, repeats: int = 3, autotune: bool = True)
         "batch_autotune": tuned,
         "from_initial_state": {"ms_per_rollout": first_ms,
                                "scene_substeps_per_s": S * K / (first_ms / 1e3),
-                               "particle_substeps_per_s": total * K / (first_ms / 1e3)},
+                               "particle_substeps_per_s": total * K / (first_ms / 1e3),
+                               "fraction_of_warmed_rate": batch_ms / first_ms,
+                               "loop_plain_ms": plain_first_ms,
+                               "loop_graph_ms": graph_first_ms,
+                               "speedup_vs_loop_plain": plain_first_ms / first_ms,
+                               "speedup_vs_loop_graph": graph_first_ms / first_ms},
         "timing": f"CUDA events around each {K}-substep rollout, best of {repeats}, after a "
                   f"{K}-substep warm-up (batch and loop over the same substeps); "
                   "loop = MLSMPMSimulator.execute(substeps=100) per scene, back to back "
@@ -717,18 +744,30 @@ def measure_c0(pkg, torch, stream, steps: int = 50, warmup: int = 5) -> dict:
 
 def measure_expanding(pkg, torch, substeps: int = 40) -> dict:
     """The inverse problem's 64 scenes (1.52M particles) stepped from their
-    initial state without CUDA graphs (one launch per kernel, for launch-level
-    profiles): the blocks expand over the rollout and every substep costs more
-    than the one before."""
+    initial state without CUDA graphs (one launch per kernel, each timed with
+    CUDA events): the blocks expand over the rollout, bricks hold fewer
+    particles and later substeps cost more.  Reports the p2g_2 kernel and the
+    whole substep at substeps 2 and `substeps`."""
     descs, recs, _ = pkg.inverse.inverse_scenes(64, seed=BATCH_SEED)
     b = pkg.MLSMPMBatch(descs, recs, graph=False)
+    per = []
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    b.step(substeps)
+    for _ in range(substeps):
+        b.setProfiling(True)  # resets the counters
+        b.step(1)
+        st = b.kernelStats()
+        per.append((st.get("sorted_p2g_2", (0, 0, 0.0))[2], sum(v[2] for v in st.values())))
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    out = {"particles": int(b.numParticles), "substeps": substeps, "ms": 1e3 * dt,
-           "health_ok": bool(b.checkHealth()["ok"])}
+    b.setProfiling(False)
+    out = {"particles": int(b.numParticles), "substeps": substeps,
+           "wall_ms_profiled": 1e3 * dt, "health_ok": bool(b.checkHealth()["ok"]),
+           "p2g2_ms_substep_2": per[1][0], f"p2g2_ms_substep_{substeps}": per[-1][0],
+           "p2g2_ratio": per[-1][0] / per[1][0],
+           "substep_ms_substep_2": per[1][1], f"substep_ms_substep_{substeps}": per[-1][1],
+           "substep_ratio": per[-1][1] / per[1][1],
+           "timing": "CUDA events around each kernel of the substep (no CUDA graph)"}
     b.close()
     return out
 
@@ -993,6 +1032,7 @@ def run_ours(args) -> None:
                                                              autotune=not args.no_autotune)
     adjoint = None if args.skip_adjoint else measure_adjoint(pkg, torch)
     inverse = None if args.skip_adjoint else measure_inverse(pkg)
+    expanding = measure_expanding(pkg, torch)
     render = None if args.skip_batched else measure_render(pkg, torch)
     sph = None if args.skip_batched else measure_sph(pkg, torch)
 
@@ -1051,6 +1091,7 @@ def run_ours(args) -> None:
         "wall_s_timed_region": wall,
         "kernels": kernels,
         "batched": batched,
+        "expanding_batch": expanding,
         "adjoint": adjoint,
         "inverse_problem": inverse,
         "render": render,

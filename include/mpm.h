@@ -309,6 +309,8 @@ int mpm_batch_download_grid(mpm_batch* batch, int scene, int32_t* out_cells);
 void* mpm_batch_posvel_device_ptr(mpm_batch* batch);
 int mpm_batch_check_health(mpm_batch* batch, mpm_health* out);
 int64_t mpm_batch_launch_count(const mpm_batch* batch);
+int mpm_batch_set_profiling(mpm_batch* batch, int enable);   /* see mpm_set_profiling */
+int mpm_batch_kernel_stats(mpm_batch* batch, mpm_kernel_stat* out, int max_entries);
 
 /* Differentiation: a forward / backward pair over a batch of scenes (one
  * scene for a single simulation).  The derivative is that of the continuous

@@ -194,6 +194,25 @@ def test_batch_task_size_and_autotune(cuda, pkg, oracle_mod):
     batch.close()
 
 
+def test_batch_kernel_stats(cuda, pkg):
+    """Per-kernel event timing of a batch: every stage of a substep is
+    counted and timed; the results equal an unprofiled batch's."""
+    from oracle import scene as scene_mod
+    descs, recs = mixed_scenes(pkg, scene_mod)
+    plain = pkg.MLSMPMBatch(descs, recs)
+    plain.step(3)
+    timed = pkg.MLSMPMBatch(descs, recs)
+    timed.setProfiling(True)
+    timed.step(3)
+    st = timed.kernelStats()
+    for name in ("sorted_p2g_2", "updateGrid", "sorted_g2p_p2g_1", "scan", "scatter"):
+        launches, timed_launches, ms = st[name]
+        assert launches >= 3 and timed_launches == launches and ms > 0.0, (name, st[name])
+    assert_bits_equal(timed.downloadParticles(), plain.downloadParticles(), "profiled batch")
+    plain.close()
+    timed.close()
+
+
 def test_batch_upload_restarts_and_reuses_graphs(cuda, pkg):
     """upload() restarts every scene from new records exactly as a fresh batch
     would, with the CUDA graph captured before the upload replayed."""

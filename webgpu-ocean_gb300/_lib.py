@@ -183,6 +183,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "mpm_batch_posvel_device_ptr": (vp, [vp]),
         "mpm_batch_check_health": (i32, [vp, ctypes.POINTER(Health)]),
         "mpm_batch_launch_count": (i64, [vp]),
+        "mpm_batch_set_profiling": (i32, [vp, i32]),
+        "mpm_batch_kernel_stats": (i32, [vp, ctypes.POINTER(KernelStat), i32]),
         "mpm_adjoint_create": (i32, [ctypes.POINTER(SceneDesc), i32, i32, i32, ctypes.POINTER(vp)]),
         "mpm_adjoint_destroy": (i32, [vp]),
         "mpm_adjoint_set_tape": (i32, [vp, i32]),

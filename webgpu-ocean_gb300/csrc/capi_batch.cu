@@ -313,5 +313,32 @@ int64_t mpm_batch_launch_count(const mpm_batch* b) {
     return t;
 }
 
+int mpm_batch_set_profiling(mpm_batch* b, int enable) {
+    if (int rc = check_batch(b)) return rc;
+    DeviceGuard g(b->device);
+    b->prof.reset();
+    b->prof.enabled = enable != 0;
+    return MPM_OK;
+}
+
+int mpm_batch_kernel_stats(mpm_batch* b, mpm_kernel_stat* out, int max_entries) {
+    if (int rc = check_batch(b)) return rc;
+    if (max_entries < 0 || (max_entries > 0 && !out)) return fail(MPM_E_INVALID, "bad arguments");
+    DeviceGuard g(b->device);
+    if (b->prof.collect() != 0) return fail(MPM_E_CUDA, "profiling events failed");
+    int count = 0;
+    for (int id = 0; id < KID_COUNT; ++id) {
+        if (b->prof.launches[id] == 0) continue;
+        if (count < max_entries) {
+            out[count].name = kernel_name(id);
+            out[count].launches = b->prof.launches[id];
+            out[count].timed_launches = b->prof.timed[id];
+            out[count].total_ms = b->prof.total_ms[id];
+        }
+        ++count;
+    }
+    return count;
+}
+
 }  // extern "C"
 

@@ -1062,17 +1062,27 @@ __device__ __forceinline__ void pair_tasks(const Dev& d, uint32_t c0, uint32_t c
 __device__ __forceinline__ void sum_bins(const Dev& d, int b0, int b1, uint32_t (&pre)[3],
                                          uint32_t* s_scan) {
     pre[0] = pre[1] = pre[2] = 0u;
-    const uint4* c4 = reinterpret_cast<const uint4*>(d.bin_count);
-    for (int i = b0 / 4 + threadIdx.x; i < b1 / 4; i += kScanThreads) {
-        const uint4 q = __ldcg(c4 + i);  // two z pairs
-        uint32_t bg, sm;
-        pair_tasks(d, q.x, q.y, bg, sm);
-        pre[1] += bg;
-        pre[2] += sm;
-        pair_tasks(d, q.z, q.w, bg, sm);
-        pre[1] += bg;
-        pre[2] += sm;
-        pre[0] += q.x + q.y + q.z + q.w;
+    const uint4* c4 = reinterpret_cast<const uint4*>(d.bin_count) + b0 / 4;
+    const int n4 = (b1 - b0) / 4;
+    constexpr int kU = 8;  // loads in flight per thread
+    for (int i0 = 0; i0 < n4; i0 += kU * kScanThreads) {
+        uint4 q[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const int i = i0 + u * kScanThreads + (int)threadIdx.x;
+            q[u] = i < n4 ? __ldcg(c4 + i) : make_uint4(0u, 0u, 0u, 0u);
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {  // two z pairs each
+            uint32_t bg, sm;
+            pair_tasks(d, q[u].x, q[u].y, bg, sm);
+            pre[1] += bg;
+            pre[2] += sm;
+            pair_tasks(d, q[u].z, q[u].w, bg, sm);
+            pre[1] += bg;
+            pre[2] += sm;
+            pre[0] += q[u].x + q[u].y + q[u].z + q[u].w;
+        }
     }
     uint32_t tot[3];
     block_scan<3>(pre, tot, s_scan);

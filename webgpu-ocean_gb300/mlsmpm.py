@@ -626,6 +626,18 @@ class MLSMPMBatch:
                 "out_of_range_accesses": int(h.out_of_range_accesses),
                 "ok": code == L.MPM_OK}
 
+    def setProfiling(self, enable: bool) -> None:
+        """Per-kernel CUDA-event timing on the launch stream (resets counters;
+        CUDA graphs are bypassed while it is on)."""
+        _check(self._lib.mpm_batch_set_profiling(self._handle, int(bool(enable))), "setProfiling")
+
+    def kernelStats(self) -> dict:
+        """{kernel name: (launches, timed launches, total device ms)}."""
+        buf = (L.KernelStat * 32)()
+        n = _check(self._lib.mpm_batch_kernel_stats(self._handle, buf, 32), "kernelStats")
+        return {buf[i].name.decode(): (int(buf[i].launches), int(buf[i].timed_launches),
+                                       float(buf[i].total_ms)) for i in range(min(n, 32))}
+
     def launchCount(self) -> int:
         return int(self._lib.mpm_batch_launch_count(self._handle))
 
