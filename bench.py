@@ -570,29 +570,35 @@ def measure_adjoint(pkg, torch, repeats: int = 3) -> dict:
         dt = time.perf_counter() - t0
         plain64 = dt if plain64 is None else min(plain64, dt)
     b.close()
-    adj = pkg.MLSMPMAdjoint(descs, 100, 20, tape="fixed")
     seed = np.zeros((len(recs64), 20), np.float32)
     seed[:, 0:3] = 1e-6
-    fwd = bwd = None
-    for _ in range(2):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        adj.forward(recs64, 100)
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        adj.backward({100: seed})
-        torch.cuda.synchronize()
-        t2 = time.perf_counter()
-        fwd = t1 - t0 if fwd is None else min(fwd, t1 - t0)
-        bwd = t2 - t1 if bwd is None else min(bwd, t2 - t1)
-    adj.close()
-    out["batch_64_scenes"] = {
-        "particles": int(len(recs64)), "substeps": 100, "tape": "fixed",
-        "plain_batched_forward_ms": 1e3 * plain64,
-        "forward_ms": 1e3 * fwd, "backward_ms": 1e3 * bwd,
-        "fwd_plus_adj_over_own_forward": (fwd + bwd) / fwd,
-        "fwd_plus_adj_over_plain_forward": (fwd + bwd) / plain64,
-        "note": "forward_ms and plain_batched_forward_ms include uploading the initial state from host memory"}
+    # checkpoints every 20 substeps (the backward recomputes 4 of the 5
+    # segments), and the full tape (every substep's state and grid kept:
+    # ~24 GB at this size; no recompute)
+    for name, every in (("batch_64_scenes", 20), ("batch_64_scenes_full_tape", 1)):
+        adj = pkg.MLSMPMAdjoint(descs, 100, every, tape="fixed")
+        fwd = bwd = None
+        for _ in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            adj.forward(recs64, 100)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            adj.backward({100: seed})
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            fwd = t1 - t0 if fwd is None else min(fwd, t1 - t0)
+            bwd = t2 - t1 if bwd is None else min(bwd, t2 - t1)
+        adj.close()
+        out[name] = {
+            "particles": int(len(recs64)), "substeps": 100, "tape": "fixed",
+            "checkpoint_every": every,
+            "plain_batched_forward_ms": 1e3 * plain64,
+            "forward_ms": 1e3 * fwd, "backward_ms": 1e3 * bwd,
+            "fwd_plus_adj_over_own_forward": (fwd + bwd) / fwd,
+            "fwd_plus_adj_over_plain_forward": (fwd + bwd) / plain64,
+            "note": "forward_ms and plain_batched_forward_ms include uploading the initial state "
+                    "from host memory"}
     out["timing"] = ("host wall clock around synchronised calls, best of "
                      f"{repeats}; plain forward = upload of the same initial state + "
                      "MLSMPMSimulator.execute(substeps=200) (CUDA graph, autotuned task size and "

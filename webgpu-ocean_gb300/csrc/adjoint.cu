@@ -207,20 +207,30 @@ __global__ void __launch_bounds__(kThreads)
     k_adj_bin(Tape tp, const AdjScene* __restrict__ scenes, const int* __restrict__ pscene, int n,
               AdjSort so) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const AdjScene& sc = scenes[pscene[i]];
-    const SimConsts& k = sc.k;
-    float x[3];
-    tp.pos(i, x);
-    int bin = so.nbins - 1;
-    if (x[0] >= 1.0f && x[1] >= 1.0f && x[2] >= 1.0f && x[0] < 1.0e9f && x[1] < 1.0e9f &&
-        x[2] < 1.0e9f) {
-        const int cx = (int)floorf(x[0]), cy = (int)floorf(x[1]), cz = (int)floorf(x[2]);
-        const long long top = ((long long)(cx + 1) * k.Y + (cy + 1)) * k.Z + (cz + 1);
-        if (cy + 1 < k.Y && cz + 1 < k.Z && top < k.grid_count)
-            bin = sc.bbase + ((cx >> 2) * sc.BY + (cy >> 2)) * sc.BZ + (cz >> 2);
+    const bool active = i < n;
+    int bin = -1;  // inactive lanes: a key no bin has
+    if (active) {
+        const AdjScene& sc = scenes[pscene[i]];
+        const SimConsts& k = sc.k;
+        float x[3];
+        tp.pos(i, x);
+        bin = so.nbins - 1;
+        if (x[0] >= 1.0f && x[1] >= 1.0f && x[2] >= 1.0f && x[0] < 1.0e9f && x[1] < 1.0e9f &&
+            x[2] < 1.0e9f) {
+            const int cx = (int)floorf(x[0]), cy = (int)floorf(x[1]), cz = (int)floorf(x[2]);
+            const long long top = ((long long)(cx + 1) * k.Y + (cy + 1)) * k.Z + (cz + 1);
+            if (cy + 1 < k.Y && cz + 1 < k.Z && top < k.grid_count)
+                bin = sc.bbase + ((cx >> 2) * sc.BY + (cy >> 2)) * sc.BZ + (cz >> 2);
+        }
     }
-    so.key_rank[i] = make_int2(bin, atomicAdd(so.bin_count + bin, 1));
+    // warp-aggregated rank: one atomic per distinct bin of the warp
+    const unsigned peers = __match_any_sync(0xffffffffu, bin);
+    const int leader = __ffs(peers) - 1;
+    const unsigned lane = threadIdx.x & 31u;
+    int base = 0;
+    if (active && (int)lane == leader) base = atomicAdd(so.bin_count + bin, __popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (active) so.key_rank[i] = make_int2(bin, base + __popc(peers & ((1u << lane) - 1u)));
 }
 
 // One thread per bin: the bin's first slot in the sorted order (bins are
@@ -452,6 +462,12 @@ __global__ void __launch_bounds__(kThreads)
                  int nscenes, int ncells) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= ncells) return;
+    const float4 vb = gadj[j];
+    // a cell no particle's g2p adjoint reached holds +0 and maps to +0 (with
+    // a finite tape): most cells of an expanded scene, left as they are
+    if ((__float_as_uint(vb.x) | __float_as_uint(vb.y) | __float_as_uint(vb.z) |
+         __float_as_uint(vb.w)) == 0u)
+        return;
     int lo = 0, hi = nscenes - 1;  // last scene with lbase <= j
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -460,7 +476,6 @@ __global__ void __launch_bounds__(kThreads)
     }
     const SimConsts& k = scenes[lo].k;
     const int id = j - scenes[lo].lbase;
-    const float4 vb = gadj[j];
     if (!tp.updated(j)) {  // not updated: g2p read the raw momentum as velocity
         gadj[j] = make_float4(vb.x, vb.y, vb.z, 0.0f);
         return;

@@ -1200,45 +1200,14 @@ __global__ void k_export(const int4* __restrict__ grid, Geo g, int4* __restrict_
 }
 
 // The same for every scene of a batch, into the concatenation of their
-// reference-layout grids (scene s at lbase).
-// k_export_all and the particles put back in index order (dst[id[j]] =
-// src[j]) in one launch: threads [0, ncells) export, the next n copy.
-__global__ void k_export_all_canon(const int4* __restrict__ grid, Dev d, int ncells,
-                                   int4* __restrict__ out, Particles src,
-                                   const uint32_t* __restrict__ id, Particles dst, int n) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < ncells) {
-        int lo = 0, hi = d.nscenes - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (d.scenes[mid].lbase <= j) lo = mid;
-            else hi = mid - 1;
-        }
-        const Scene& sc = d.scenes[lo];
-        out[j] = grid[(size_t)sc.bbase * 64 + flat_to_addr(sc.g, j - sc.lbase)];
-        return;
-    }
-    const int p = j - ncells;
-    if (p >= n) return;
-    const uint32_t i = id[p];
-    dst.p0[i] = src.p0[p];
-    dst.p1[i] = src.p1[p];
-    dst.p2[i] = src.p2[p];
-    dst.p3[i] = src.p3[p];
-}
-
-__global__ void k_export_all(const int4* __restrict__ grid, Dev d, int ncells,
-                             int4* __restrict__ out) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= ncells) return;
-    int lo = 0, hi = d.nscenes - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (d.scenes[mid].lbase <= j) lo = mid;
-        else hi = mid - 1;
-    }
-    const Scene& sc = d.scenes[lo];
-    out[j] = grid[(size_t)sc.bbase * 64 + flat_to_addr(sc.g, j - sc.lbase)];
+// reference-layout grids (scene s at lbase): block row y exports scene
+// s0 + y.
+__global__ void k_export_scenes(const int4* __restrict__ grid, Dev d, int s0,
+                                int4* __restrict__ out) {
+    const Scene& sc = d.scenes[s0 + (int)blockIdx.y];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sc.g.grid_count) return;
+    out[sc.lbase + i] = grid[(size_t)sc.bbase * 64 + flat_to_addr(sc.g, i)];
 }
 
 }  // namespace
@@ -1282,6 +1251,7 @@ struct SortedEngine {
     int task_cap = kMaxSort;     // most particles per task (see kMinTaskCap)
     bool task_cap_auto = true;   // task_cap follows the particle count
     int ncells_linear = 0;       // batch: cells of all scenes' reference-layout grids
+    int max_scene_cells = 0;     // batch: most cells of one scene's reference-layout grid
     std::vector<GraphEntry> graphs;
 };
 
@@ -1560,6 +1530,8 @@ int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes) {
     e->nbricks = (int)bricks;
     e->nbins = (int)bins;
     e->ncells_linear = (int)lcells;
+    e->max_scene_cells = 0;
+    for (int s = 0; s < nscenes; ++s) e->max_scene_cells = std::max(e->max_scene_cells, ks[s].grid_count);
     apply_task_cap(e, parts);
     e->configured = true;
     return 0;
@@ -1895,32 +1867,18 @@ int sorted_export_scene_grid(SortedEngine* e, int scene, int4* out, cudaStream_t
 int sorted_export_all_canonical(SortedEngine* e, int4* out, const ParticleStore& ps,
                                 const Particles& dst, int n, cudaStream_t st,
                                 LaunchProfiler* prof) {
-    if (!e->configured || !e->has_grid || !e->batch) {
-        g_err = "no batched sorted-engine grid to export";
-        return -1;
-    }
-    const int nc = e->ncells_linear;
+    if (sorted_export_all(e, out, st, prof) != 0) return -1;
     const int c = ps.cur;
-    if (ps.canonical || (long long)nc + n > INT_MAX) {  // a plain copy / two launches
-        if (!ps.canonical) {
-            if (sorted_export_all(e, out, st, prof) != 0) return -1;
-            if (n > 0)
-                LAUNCH(KID_CANONICALIZE, launch_canonicalize(ps.P[c], ps.id[c], dst, nullptr, n, st));
-            SE_CUDA(cudaGetLastError());
-            return 0;
-        }
-        if (sorted_export_all(e, out, st, prof) != 0) return -1;
-        const float4* s[4] = {ps.P[c].p0, ps.P[c].p1, ps.P[c].p2, ps.P[c].p3};
-        float4* d[4] = {dst.p0, dst.p1, dst.p2, dst.p3};
-        for (int q = 0; q < 4 && n > 0; ++q)
-            SE_CUDA(cudaMemcpyAsync(d[q], s[q], sizeof(float4) * (size_t)n,
-                                    cudaMemcpyDeviceToDevice, st));
+    if (!ps.canonical) {
+        if (n > 0)
+            LAUNCH(KID_CANONICALIZE, launch_canonicalize(ps.P[c], ps.id[c], dst, nullptr, n, st));
+        SE_CUDA(cudaGetLastError());
         return 0;
     }
-    const long long total = (long long)nc + (n > 0 ? n : 0);
-    LAUNCH(KID_EXPORT, (k_export_all_canon<<<(int)((total + 255) / 256), 256, 0, st>>>(
-                           e->d.grid[e->last], e->d, nc, out, ps.P[c], ps.id[c], dst, n)));
-    SE_CUDA(cudaGetLastError());
+    const float4* s[4] = {ps.P[c].p0, ps.P[c].p1, ps.P[c].p2, ps.P[c].p3};
+    float4* d[4] = {dst.p0, dst.p1, dst.p2, dst.p3};
+    for (int q = 0; q < 4 && n > 0; ++q)
+        SE_CUDA(cudaMemcpyAsync(d[q], s[q], sizeof(float4) * (size_t)n, cudaMemcpyDeviceToDevice, st));
     return 0;
 }
 
@@ -1929,9 +1887,13 @@ int sorted_export_all(SortedEngine* e, int4* out, cudaStream_t st, LaunchProfile
         g_err = "no batched sorted-engine grid to export";
         return -1;
     }
-    const int nc = e->ncells_linear;
-    LAUNCH(KID_EXPORT,
-           (k_export_all<<<(nc + 255) / 256, 256, 0, st>>>(e->d.grid[e->last], e->d, nc, out)));
+    const int S = (int)e->scenes.size();
+    for (int s0 = 0; s0 < S; s0 += 65535) {
+        const dim3 blocks((unsigned)((e->max_scene_cells + 255) / 256),
+                          (unsigned)std::min(65535, S - s0));
+        LAUNCH(KID_EXPORT,
+               (k_export_scenes<<<blocks, 256, 0, st>>>(e->d.grid[e->last], e->d, s0, out)));
+    }
     SE_CUDA(cudaGetLastError());
     return 0;
 }
