@@ -561,7 +561,7 @@ def measure_adjoint(pkg, torch, repeats: int = 3) -> dict:
     b = pkg.MLSMPMBatch(descs, recs64)
     b.step(100)
     plain64 = None
-    for _ in range(2):
+    for _ in range(3):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         b.upload(recs64)
@@ -578,7 +578,7 @@ def measure_adjoint(pkg, torch, repeats: int = 3) -> dict:
     for name, every in (("batch_64_scenes", 20), ("batch_64_scenes_full_tape", 1)):
         adj = pkg.MLSMPMAdjoint(descs, 100, every, tape="fixed")
         fwd = bwd = None
-        for _ in range(2):
+        for _ in range(3):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             adj.forward(recs64, 100)
@@ -612,11 +612,13 @@ def measure_inverse(pkg) -> dict:
     grids, hidden stiffness / viscosity, 100-substep rollouts, 50 Adam
     iterations of batched forward + adjoint."""
     import numpy as np
-    r = pkg.inverse.run_inverse_problem(64, seed=BATCH_SEED, substeps=100, iters=50)
+    # full tape (every substep's state and grid kept, ~24 GB): no recompute
+    r = pkg.inverse.run_inverse_problem(64, seed=BATCH_SEED, substeps=100, iters=50,
+                                        checkpoint_every=1)
     rel = r["rel_err"]
     h = r["history"]
     return {"scenes": r["scenes"], "particles": r["particles"], "substeps": 100,
-            "iterations": 50, "tape": "fixed", "checkpoint_every": 20,
+            "iterations": 50, "tape": "fixed", "checkpoint_every": 1,
             "observed_substeps": [20, 40, 60, 80, 100],
             "seconds": r["seconds"], "ms_per_iteration": 1e3 * r["seconds"] / 50,
             "stiffness_rel_err_median": float(np.median(rel[:, 0])),
@@ -628,7 +630,7 @@ def measure_inverse(pkg) -> dict:
                     "observed substeps; loss and seeds computed on the device "
                     "(MLSMPMAdjoint.observationLoss / backwardObserved)",
             "timing": "host wall clock around the 50 iterations (scene constants, forward with "
-                      "checkpoints, loss, backward, Adam step)"}
+                      "the full tape, loss, backward, Adam step)"}
 
 
 def measure_render(pkg, torch, frames: int = 10) -> dict:
