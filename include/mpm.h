@@ -446,6 +446,13 @@ int mpm_sph_step(mpm_sph* sph, int substeps, void* stream);
 /* Frames replay as CUDA graphs (captured once per substep and particle
  * count); 0 launches every kernel each frame.  Results are the same. */
 int mpm_sph_set_graph(mpm_sph* sph, int enable); /* default 1 */
+/* Up to max_particles particles, density and forces run one warp per
+ * particle (the lanes share the neighbour terms; the sums keep the
+ * one-thread order, so the results do not change); above it, one thread per
+ * particle.  Default 32768; 0: always a thread per particle; -1: the
+ * default. */
+int mpm_sph_set_warp_per_particle(mpm_sph* sph, int max_particles);
+int mpm_sph_get_warp_per_particle(const mpm_sph* sph);
 /* changeBoxSize(realBoxSize), sph.ts:383-388 (half sizes) */
 int mpm_sph_set_real_box(mpm_sph* sph, const float real_half_box[3]);
 int mpm_sph_num_particles(const mpm_sph* sph);

@@ -11,8 +11,9 @@ from helpers import assert_bits_equal
 pytestmark = pytest.mark.gpu
 
 
-def run_pair(pkg, oracle_mod, half, n, frames, seed=7, box_changes=None):
+def run_pair(pkg, oracle_mod, half, n, frames, seed=7, box_changes=None, warp_max=-1):
     sim = pkg.SPHSimulator(None, None, 0.08, maxParticles=200000, seed=seed)
+    sim.warpPerParticle = warp_max
     sim.reset(n, half)
     rec = sim.downloadParticles()
     assert len(rec) == n
@@ -30,11 +31,27 @@ def run_pair(pkg, oracle_mod, half, n, frames, seed=7, box_changes=None):
     return got
 
 
-def test_default_scene(cuda, pkg, oracle_mod):
-    """main.ts's SPH defaults: 20,000 particles, half box (1.0, 2.0, 1.0)."""
-    got = run_pair(pkg, oracle_mod, [1.0, 2.0, 1.0], 20000, 30)
+@pytest.mark.parametrize("warp_max", [-1, 0])
+def test_default_scene(cuda, pkg, oracle_mod, warp_max):
+    """main.ts's SPH defaults: 20,000 particles, half box (1.0, 2.0, 1.0);
+    density and forces one warp per particle (the default at this size) and
+    one thread per particle."""
+    got = run_pair(pkg, oracle_mod, [1.0, 2.0, 1.0], 20000, 30, warp_max=warp_max)
     assert np.isfinite(got).all()
     assert (got[:, 11] > 0).all()  # every particle has neighbours in the grid
+
+
+def test_warp_per_particle_dense_neighbourhoods(cuda, pkg, oracle_mod):
+    """A compressed block (more neighbours than one staging round of 64)
+    one warp per particle, and the knob's range."""
+    run_pair(pkg, oracle_mod, [0.35, 1.0, 0.35], 20000, 8)
+    sim = pkg.SPHSimulator(None, None, 0.08, maxParticles=1000)
+    assert sim.warpPerParticle == 32768
+    sim.warpPerParticle = 0
+    assert sim.warpPerParticle == 0
+    with pytest.raises(Exception):
+        sim.warpPerParticle = -2
+    sim.close()
 
 
 @pytest.mark.parametrize("n,half", [(10000, [0.7, 2.0, 0.7]), (1, [1.0, 2.0, 1.0]),

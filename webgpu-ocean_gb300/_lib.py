@@ -209,6 +209,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         "mpm_sph_upload": (i32, [vp, fp, i32, fp]),
         "mpm_sph_step": (i32, [vp, i32, vp]),
         "mpm_sph_set_graph": (i32, [vp, i32]),
+        "mpm_sph_set_warp_per_particle": (i32, [vp, i32]),
+        "mpm_sph_get_warp_per_particle": (i32, [vp]),
         "mpm_sph_set_real_box": (i32, [vp, fp]),
         "mpm_sph_num_particles": (i32, [vp]),
         "mpm_sph_grid_count": (i64, [vp]),

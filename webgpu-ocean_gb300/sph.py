@@ -58,6 +58,17 @@ class SPHSimulator:
         """Replay frames as CUDA graphs (default) or launch every kernel."""
         _check(self._lib.mpm_sph_set_graph(self._handle, int(bool(enable))), "setGraph")
 
+    @property
+    def warpPerParticle(self) -> int:
+        """Particle counts up to this run density and forces one warp per
+        particle (default 32768; 0: never; -1 to set: the default)."""
+        return _check(self._lib.mpm_sph_get_warp_per_particle(self._handle), "warpPerParticle")
+
+    @warpPerParticle.setter
+    def warpPerParticle(self, max_particles: int) -> None:
+        _check(self._lib.mpm_sph_set_warp_per_particle(self._handle, int(max_particles)),
+               "warpPerParticle")
+
     def changeBoxSize(self, realBoxSize) -> None:
         """sph.ts:383-388 (half sizes)."""
         b = (ctypes.c_float * 3)(*[float(x) for x in realBoxSize])
