@@ -484,8 +484,10 @@ __device__ __forceinline__ void build_lane_table(const Particles& P, const Geo& 
 template <bool BATCH, int TH>
 __global__ void __launch_bounds__(TH, 1024 / TH)
     k_p2g2(Particles P, Scene one, Dev d, int cur, unsigned long long* oob) {
-    __shared__ float s_mass[2][kNA];
-    __shared__ int s_q[2][3][kNA];
+    constexpr bool DB = TH != 128;  // double-buffered arenas (128 threads: one, 8 blocks/SM)
+    constexpr int NB = DB ? 2 : 1;
+    __shared__ float s_mass[NB][kNA];
+    __shared__ int s_q[NB][3][kNA];
     __shared__ int s_task[2];
     __shared__ LaneTable s_lt;
     constexpr int kPer = (kNA + TH - 1) / TH;  // arena slots per thread
@@ -496,7 +498,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     unsigned bad = 0;
     const int ntasks = (int)__ldcg(d.ntasks);
     const int nbig = (int)__ldcg(d.ntasks + 1);
-    for (int i = threadIdx.x; i < 2 * 3 * kNA; i += TH) (&s_q[0][0][0])[i] = 0;
+    for (int i = threadIdx.x; i < NB * 3 * kNA; i += TH) (&s_q[0][0][0])[i] = 0;
     if (threadIdx.x == 0) {
         s_task[0] = claim_task(d, kCtrP2G2);
         s_task[1] = claim_task(d, kCtrP2G2);
@@ -565,7 +567,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     };
 
     int t = s_task[0];
-    {
+    if (DB) {
         int m[kPer];
         float fm;
         load_mass(t, m, fm);
@@ -578,14 +580,24 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     bool have_prev = false;
     int it = 0;
     while (t < ntasks) {
-        const int buf = it & 1;
-        __syncthreads();  // arena `buf` ready; task it-1 computed
-        const int t_next = s_task[buf ^ 1];
-        if (threadIdx.x == 0) s_task[buf] = claim_task(d, kCtrP2G2);
+        const int cb = it & 1;           // claim slot
+        const int buf = DB ? cb : 0;     // arena buffer
+        __syncthreads();  // DB: arena `buf` ready; task it-1 computed
+        const int t_next = s_task[cb ^ 1];
+        if (threadIdx.x == 0) s_task[cb] = claim_task(d, kCtrP2G2);
         int m_next[kPer];
-        float fm_next;
-        load_mass(t_next, m_next, fm_next);
-        if (have_prev) flush(buf ^ 1, prev);
+        float fm_next = 0.0f;
+        if (DB) {
+            load_mass(t_next, m_next, fm_next);
+            if (have_prev) flush(buf ^ 1, prev);
+        } else {  // one arena: flush task it-1's, load this task's, then wait
+            if (have_prev) flush(0, prev);
+            int m[kPer];
+            float fm;
+            load_mass(t, m, fm);
+            store_mass(0, m, fm);
+            __syncthreads();
+        }
 
         const Task task = d.tasks[task_slot(d, nbig, t)];
         const Scene& sc = scene_ref<BATCH>(d, one, task.scene);
@@ -641,14 +653,14 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
                     });
             }
         }
-        store_mass(buf ^ 1, m_next, fm_next);
+        if (DB) store_mass(buf ^ 1, m_next, fm_next);
         prev = task;
         have_prev = true;
         t = t_next;
         ++it;
     }
     __syncthreads();
-    if (have_prev) flush((it - 1) & 1, prev);
+    if (have_prev) flush(DB ? (it - 1) & 1 : 0, prev);
     if (bad) atomicAdd(oob, (unsigned long long)bad);
 }
 
@@ -706,9 +718,11 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     k_g2p_p2g1(Particles Pin, Particles Pout, const uint32_t* __restrict__ id_in,
                uint32_t* __restrict__ id_out, float4* __restrict__ posvel, Scene one, Dev d,
                int src, int dst, unsigned long long* oob) {
-    __shared__ __align__(16) float4 s_v[DO_G2P ? 2 : 1][DO_G2P ? kNA : 1];
-    __shared__ int s_a[2][4][kNB];
-    __shared__ int s_touch[2][kTouch];
+    constexpr bool DB = TH != 128;  // double-buffered arenas (128 threads: one, 8 blocks/SM)
+    constexpr int NB = DB ? 2 : 1;
+    __shared__ __align__(16) float4 s_v[DO_G2P ? NB : 1][DO_G2P ? kNA : 1];
+    __shared__ int s_a[NB][4][kNB];
+    __shared__ int s_touch[NB][kTouch];
     __shared__ int s_task[2];
     constexpr int kPerA = DO_G2P ? (kNA + TH - 1) / TH : 1;  // g2p arena slots per thread
     constexpr int kPerB = (kNB + TH - 1) / TH;                // p2g_1 arena slots per thread
@@ -719,8 +733,8 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     unsigned bad = 0;
     const int ntasks = (int)__ldcg(d.ntasks);
     const int nbig = (int)__ldcg(d.ntasks + 1);
-    for (int i = threadIdx.x; i < 2 * 4 * kNB; i += TH) (&s_a[0][0][0])[i] = 0;
-    if (threadIdx.x < 2 * kTouch) (&s_touch[0][0])[threadIdx.x] = 0;
+    for (int i = threadIdx.x; i < NB * 4 * kNB; i += TH) (&s_a[0][0][0])[i] = 0;
+    if (threadIdx.x < NB * kTouch) (&s_touch[0][0])[threadIdx.x] = 0;
     if (threadIdx.x == 0) {
         s_task[0] = claim_task(d, ctr);
         s_task[1] = claim_task(d, ctr);
@@ -794,21 +808,32 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     };
 
     int t = s_task[0];
-    prefetch(t, 0);
+    if (DB) prefetch(t, 0);
     bool have_prev = false;
     Task prev;
     prev.bin = -1;
     prev.scene = 0;
     int it = 0;
     while (t < ntasks) {
-        const int buf = it & 1;
-        if (DO_G2P) cp_async_wait_all();
-        __syncthreads();  // s_v[buf] arrived; task it-1 computed everywhere
-        const int t_next = s_task[buf ^ 1];
-        if (threadIdx.x == 0) s_task[buf] = claim_task(d, ctr);
-        if (have_prev && prev.bin >= 0) mark(buf ^ 1, prev);
-        prefetch(t_next, buf ^ 1);
-        if (have_prev && prev.bin >= 0) flush(buf ^ 1, prev);
+        const int cb = it & 1;           // claim slot
+        const int buf = DB ? cb : 0;     // arena buffer
+        if (DB && DO_G2P) cp_async_wait_all();
+        __syncthreads();  // DB: s_v[buf] arrived; task it-1 computed everywhere
+        const int t_next = s_task[cb ^ 1];
+        if (threadIdx.x == 0) s_task[cb] = claim_task(d, ctr);
+        if (DB) {
+            if (have_prev && prev.bin >= 0) mark(buf ^ 1, prev);
+            prefetch(t_next, buf ^ 1);
+            if (have_prev && prev.bin >= 0) flush(buf ^ 1, prev);
+        } else {  // one arena: flush task it-1's, copy in this task's, then wait
+            if (have_prev && prev.bin >= 0) {
+                mark(0, prev);
+                flush(0, prev);
+            }
+            prefetch(t, 0);
+            if (DO_G2P) cp_async_wait_all();
+            __syncthreads();
+        }
 
         const Task task = d.tasks[task_slot(d, nbig, t)];
         const Scene& sc = scene_ref<BATCH>(d, one, task.scene);
@@ -932,8 +957,8 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     }
     __syncthreads();
     if (have_prev && prev.bin >= 0) {
-        mark((it - 1) & 1, prev);
-        flush((it - 1) & 1, prev);
+        mark(DB ? (it - 1) & 1 : 0, prev);
+        flush(DB ? (it - 1) & 1 : 0, prev);
     }
     if (bad) atomicAdd(oob, (unsigned long long)bad);
 }
