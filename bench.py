@@ -758,6 +758,8 @@ def measure_expanding(pkg, torch, substeps: int = 40) -> dict:
     whole substep at substeps 2 and `substeps`."""
     descs, recs, _ = pkg.inverse.inverse_scenes(64, seed=BATCH_SEED)
     b = pkg.MLSMPMBatch(descs, recs, graph=False)
+    b.autotune(4)  # on the initial state, which it restores
+    tuned = b.tuning()
     per = []
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -774,7 +776,7 @@ def measure_expanding(pkg, torch, substeps: int = 40) -> dict:
            "p2g2_ms_substep_2": per[1][0], f"p2g2_ms_substep_{substeps}": per[-1][0],
            "p2g2_ratio": per[-1][0] / per[1][0],
            "substep_ms_substep_2": per[1][1], f"substep_ms_substep_{substeps}": per[-1][1],
-           "substep_ratio": per[-1][1] / per[1][1],
+           "substep_ratio": per[-1][1] / per[1][1], "autotune": tuned,
            "timing": "CUDA events around each kernel of the substep (no CUDA graph)"}
     b.close()
     return out
