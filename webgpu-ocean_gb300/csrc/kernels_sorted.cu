@@ -67,9 +67,9 @@ namespace {
 // the autotuner.  Bricks at the free surface hold few particles, so smaller
 // chunks leave fewer lanes idle; larger CTAs share one arena among more
 // particles in flight.  Every variant asks for 1024 resident threads per SM
-// (64 registers per thread).
+// (64 registers per thread); the 128-thread kernels keep one arena buffer
+// instead of two so that their 8 blocks fit the SM's shared memory.
 constexpr int kTask = 256;
-constexpr int kThreadVariants[3] = {128, 256, 512};
 // Arena strides: with x-stride = 16 and y-stride = 12 (mod 32) the 64 cells
 // of a brick fall into 32 bank classes of exactly two cells each
 // (class = (16*x + 12*y + z) mod 32 for brick-relative x, y, z).  When the
@@ -1268,7 +1268,7 @@ struct SortedEngine {
     bool primed = false;
     bool has_grid = false;
     int blocks_update = 0;
-    int blocks_p2g2_v[3] = {0, 0, 0}, blocks_g2p_v[3] = {0, 0, 0};  // per kThreadVariants
+    int blocks_p2g2_v[3] = {0, 0, 0}, blocks_g2p_v[3] = {0, 0, 0};  // 128, 256, 512 threads
     int threads = kTask;         // CTA size of the task kernels
     int variant() const { return threads == 128 ? 0 : (threads == 512 ? 2 : 1); }
     int blocks_p2g2() const { return blocks_p2g2_v[variant()]; }
