@@ -397,7 +397,6 @@ struct LaneTable {
     uint32_t key[kMaxSort];     // class | rank << 6, per particle in bin order
     uint32_t tmp[kMaxSort];     // particle slots in bin order
     int cnt[33];                // particles per bank class (32: not in the arena)
-    int valid[32], core[32], empty_pre[33], over_pre[33];
 };
 
 // Orders a bin's n particles into a table of ceil(n/32) rows of 32 lanes
@@ -411,8 +410,7 @@ template <int TH>
 __device__ __forceinline__ void build_lane_table(const Particles& P, const Geo& g, const Dev& d,
                                                  const Task& task, LaneTable& lt) {
     const int n = task.count;
-    if (threadIdx.x < 33) lt.cnt[threadIdx.x] = 0;
-    __syncthreads();
+    // lt.cnt is zero here: zeroed at the kernel's start and after every table
     for (int j = threadIdx.x; j < n; j += TH) {
         const uint32_t slot = d.order[task.first + j];
         const float4 a = P.p0[slot];
@@ -428,49 +426,50 @@ __device__ __forceinline__ void build_lane_table(const Particles& P, const Geo& 
         lt.key[j] = (uint32_t)cls | ((uint32_t)r << 6);
     }
     __syncthreads();
-    if (threadIdx.x < 32) {
-        const int k = threadIdx.x;
-        const int rows = (n + 31) >> 5;
-        const int last = n - 32 * (rows - 1);            // lanes used in the last row
-        const int v = rows - 1 + (k < last ? 1 : 0);     // rows lane k holds
-        const int c = lt.cnt[k];
-        const int core = min(c, v);
-        int e = v - core, o = c - core;                  // empty lanes, overflow particles
-        int ei = e, oi = o;
+    // every warp scans the class counts itself (lane k: class k), so that no
+    // warp waits for another's scan
+    const unsigned full = 0xffffffffu;
+    const int k = (int)(threadIdx.x & 31u);
+    const int rows = (n + 31) >> 5;
+    const int last = n - 32 * (rows - 1);            // lanes used in the last row
+    const int v = rows - 1 + (k < last ? 1 : 0);     // rows lane k holds
+    const int c = lt.cnt[k];
+    const int core = min(c, v);
+    const int e = v - core, o = c - core;            // empty lanes, overflow particles
+    int ei = e, oi = o;
 #pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            const int ye = __shfl_up_sync(0xffffffffu, ei, off);
-            const int yo = __shfl_up_sync(0xffffffffu, oi, off);
-            if (k >= off) { ei += ye; oi += yo; }
-        }
-        lt.valid[k] = v;
-        lt.core[k] = core;
-        lt.empty_pre[k] = ei - e;
-        lt.over_pre[k] = oi - o;
-        if (k == 31) {
-            lt.empty_pre[32] = ei;
-            lt.over_pre[32] = oi;  // particles outside the arena overflow after these
-        }
+    for (int off = 1; off < 32; off <<= 1) {
+        const int ye = __shfl_up_sync(full, ei, off);
+        const int yo = __shfl_up_sync(full, oi, off);
+        if (k >= off) { ei += ye; oi += yo; }
     }
-    __syncthreads();
-    for (int j = threadIdx.x; j < n; j += TH) {
-        const uint32_t key = lt.key[j];
+    const int empty_pre = ei - e, over_pre = oi - o;
+    const int over_all = __shfl_sync(full, oi, 31);  // particles outside the arena overflow after these
+    for (int base = 0; base < n; base += TH) {         // the same trip count in every warp
+        const int j = base + (int)threadIdx.x;
+        const bool active = j < n;
+        const uint32_t key = active ? lt.key[j] : 0u;
         const int cls = (int)(key & 63u), r = (int)(key >> 6);
-        int pos;
-        if (cls < 32 && r < lt.valid[cls]) {
-            pos = r * 32 + cls;
-        } else {
-            const int i = cls < 32 ? lt.over_pre[cls] + (r - lt.valid[cls]) : lt.over_pre[32] + r;
-            int lo = 0;                                  // last lane with empty_pre <= i
+        const int v_c = __shfl_sync(full, v, cls & 31);
+        const int op_c = __shfl_sync(full, over_pre, cls & 31);
+        const bool direct = cls < 32 && r < v_c;
+        const int i = cls < 32 ? op_c + (r - v_c) : over_all + r;
+        int lo = 0;                                    // last lane with empty_pre <= i
 #pragma unroll
-            for (int step = 16; step > 0; step >>= 1)
-                if (lo + step < 32 && lt.empty_pre[lo + step] <= i) lo += step;
-            pos = (lt.core[lo] + (i - lt.empty_pre[lo])) * 32 + lo;
+        for (int step = 16; step > 0; step >>= 1) {
+            const int ep = __shfl_sync(full, empty_pre, lo + step);
+            if (ep <= i) lo += step;
         }
-        lt.slot[pos] = lt.tmp[j];
-        d.order[task.first + pos] = lt.tmp[j];
+        const int core_lo = __shfl_sync(full, core, lo);
+        const int ep_lo = __shfl_sync(full, empty_pre, lo);
+        const int pos = direct ? r * 32 + cls : (core_lo + (i - ep_lo)) * 32 + lo;
+        if (active) {
+            lt.slot[pos] = lt.tmp[j];
+            d.order[task.first + pos] = lt.tmp[j];
+        }
     }
     __syncthreads();
+    if (threadIdx.x < 33) lt.cnt[threadIdx.x] = 0;  // every warp has read them
 }
 
 // ---------------------------------------------------------------------------
@@ -499,6 +498,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     const int ntasks = (int)__ldcg(d.ntasks);
     const int nbig = (int)__ldcg(d.ntasks + 1);
     for (int i = threadIdx.x; i < NB * 3 * kNA; i += TH) (&s_q[0][0][0])[i] = 0;
+    if (threadIdx.x < 33) s_lt.cnt[threadIdx.x] = 0;
     if (threadIdx.x == 0) {
         s_task[0] = claim_task(d, kCtrP2G2);
         s_task[1] = claim_task(d, kCtrP2G2);
