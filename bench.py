@@ -384,16 +384,20 @@ def measure_batched(pkg, torch, stream, repeats: int = 3, autotune: bool = True)
     batch_ms = min(a.elapsed_time(b) for a, b in evs)
     batch_launches = (batch.launchCount() - l0) // repeats
     # the same rollout from the scenes' initial state (the blocks start above
-    # rest density and spread, so the first substeps cost the most)
-    first_ms = None
+    # rest density and spread, so the first substeps cost the most), and the
+    # K substeps after it
+    first_ms = next_ms = None
     for _ in range(2):
         batch.upload(recs)
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a, b, c = (torch.cuda.Event(enable_timing=True) for _ in range(3))
         a.record(stream)
         batch.step(K, stream)
         b.record(stream)
+        batch.step(K, stream)
+        c.record(stream)
         torch.cuda.synchronize()
         first_ms = a.elapsed_time(b) if first_ms is None else min(first_ms, a.elapsed_time(b))
+        next_ms = b.elapsed_time(c) if next_ms is None else min(next_ms, b.elapsed_time(c))
 
     offs = np.concatenate([[0], np.cumsum([d.num_particles for d in descs])])
     sims = []
@@ -490,6 +494,8 @@ def measure_batched(pkg, torch, stream, repeats: int = 3, autotune: bool = True)
                                "scene_substeps_per_s": S * K / (first_ms / 1e3),
                                "particle_substeps_per_s": total * K / (first_ms / 1e3),
                                "fraction_of_warmed_rate": batch_ms / first_ms,
+                               "next_ms_per_rollout": next_ms,
+                               "fraction_of_next_rollout_rate": next_ms / first_ms,
                                "loop_plain_ms": plain_first_ms,
                                "loop_graph_ms": graph_first_ms,
                                "speedup_vs_loop_plain": plain_first_ms / first_ms,
@@ -498,7 +504,8 @@ def measure_batched(pkg, torch, stream, repeats: int = 3, autotune: bool = True)
                   f"{K}-substep warm-up (batch and loop over the same substeps); "
                   "loop = MLSMPMSimulator.execute(substeps=100) per scene, back to back "
                   "(default task size and lane table; the batch's are autotuned on its initial "
-                  "state); from_initial_state: the first 100 substeps after an upload, best of 2",
+                  "state); from_initial_state: the first 100 substeps after an upload, best of 2 "
+                  "(next_ms_per_rollout: substeps 100-200 after the upload)",
     }
 
 
@@ -782,6 +789,40 @@ def measure_expanding(pkg, torch, substeps: int = 40) -> dict:
     return out
 
 
+def measure_batch_windows(pkg, torch) -> dict:
+    """Per-kernel device ms per substep of the 256-scene batch in four
+    windows of its rollout from the initial state (no CUDA graph, CUDA events
+    around each launch): substeps 0-10 (dense blocks), 55-65 (spread, most
+    bricks), 150-160 and 290-300 (settling).  The tuning is fixed at the
+    choice the autotuner makes for this batch on its initial state (every z
+    pair merged, 128-thread blocks, tasks of up to 1024 particles, lane table
+    from 32), so that the kernel launches are the same in every run."""
+    descs, recs = pkg.batch_scenes(BATCH_SCENES, seed=BATCH_SEED)
+    b = pkg.MLSMPMBatch(descs, recs, graph=False)
+    b.binPairing = 1 << 30
+    b.taskThreads = 128
+    b.setTaskSize(1024)
+    b.laneTableMin = 32
+    out = {"scenes": len(descs), "particles": int(b.numParticles), "tuning": b.tuning(),
+           "timing": "CUDA events around each launch, ms per substep (no CUDA graph)"}
+    done = 0
+    for lo, hi in ((0, 10), (55, 65), (150, 160), (290, 300)):
+        if done < lo:
+            b.step(lo - done)
+        torch.cuda.synchronize()
+        b.setProfiling(True)  # resets the counters
+        b.step(hi - lo)
+        torch.cuda.synchronize()
+        st = b.kernelStats()
+        b.setProfiling(False)
+        done = hi
+        row = {k: v[2] / (hi - lo) for k, v in st.items() if v[1]}
+        row["total"] = sum(v[2] for v in st.values()) / (hi - lo)
+        out[f"substeps_{lo}_{hi}"] = row
+    b.close()
+    return out
+
+
 def measure_adjoint_batch(pkg, torch, substeps: int = 40, every: int = 10) -> dict:
     """One checkpointed forward and backward of the inverse problem's 64
     scenes (1.52M particles) on the fixed-point tape (for kernel profiles)."""
@@ -821,6 +862,8 @@ def run_only(which: str, autotune: bool = True) -> None:
         out = measure_expanding(pkg, torch)
     elif which == "adjoint_batch":
         out = measure_adjoint_batch(pkg, torch)
+    elif which == "batch_windows":
+        out = measure_batch_windows(pkg, torch)
     else:
         out = measure_inverse(pkg)
     print(json.dumps({"only": which, which: out}), flush=True)
@@ -1131,7 +1174,7 @@ def main():
     ap.add_argument("--skip-adjoint", action="store_true",
                     help="leave out the adjoint and inverse-problem measurements")
     ap.add_argument("--only", choices=["batched", "adjoint", "inverse", "render", "sph",
-                                       "expanding", "adjoint_batch"],
+                                       "expanding", "adjoint_batch", "batch_windows"],
                     help="run one side measurement alone and print its JSON (profiling)")
     ap.add_argument("--quick", action="store_true",
                     help="time the device-resident steps only (for profiler captures)")
