@@ -160,6 +160,11 @@ struct Scene {
     int binbase;
     int pbase;
     int lbase;   // first cell in the reference-layout concatenation of all grids
+    // Batch: the index of the scene's (PY, PZ) among the batch's distinct
+    // pairs.  Arena slot offsets depend on these two only, so a task kernel
+    // keeps its offsets while consecutive tasks share the class; the bins
+    // are laid out class by class for that reason.
+    int gclass;
     SimConsts k;
 };
 
@@ -507,12 +512,15 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     // offsets of this thread's arena slots for the geometry of scene
     // off_scene (recomputed when a batch's task belongs to another scene)
     int off[kPer];
-    int off_scene = 0;
+    int off_class = one.gclass;
     slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPer>(one.g, off);
     auto offsets_for = [&](int scene) {
-        if (BATCH && scene != off_scene) {
-            slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPer>(scene_ref<BATCH>(d, one, scene).g, off);
-            off_scene = scene;
+        if (BATCH) {
+            const Scene& ts = scene_ref<BATCH>(d, one, scene);
+            if (ts.gclass != off_class) {
+                slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPer>(ts.g, off);
+                off_class = ts.gclass;
+            }
         }
     };
     __syncthreads();
@@ -744,12 +752,15 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     // off_scene (recomputed when a batch's task belongs to another); the
     // flush computes those of its touched p2g_1 slots
     int offA[kPerA];
-    int off_scene = 0;
+    int off_class = one.gclass;
     if (DO_G2P) slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPerA>(one.g, offA);
     auto offsets_for = [&](int scene) {
-        if (BATCH && DO_G2P && scene != off_scene) {
-            slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPerA>(scene_ref<BATCH>(d, one, scene).g, offA);
-            off_scene = scene;
+        if (BATCH && DO_G2P) {
+            const Scene& ts = scene_ref<BATCH>(d, one, scene);
+            if (ts.gclass != off_class) {
+                slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPerA>(ts.g, offA);
+                off_class = ts.gclass;
+            }
         }
     };
     __syncthreads();
@@ -1507,18 +1518,22 @@ int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes) {
     }
     std::vector<Scene> hs((size_t)nscenes);
     long long bricks = 0, bins = 0, parts = 0, lcells = 0;
+    std::vector<std::pair<int, int>> classes;  // distinct (PY, PZ)
     for (int s = 0; s < nscenes; ++s) {
         if (!make_geo(ks[s], hs[s].g)) {
             g_err = "scene " + std::to_string(s) + " has a degenerate box";
             return -1;
         }
+        const std::pair<int, int> pyz(hs[s].g.PY, hs[s].g.PZ);
+        size_t c = 0;
+        while (c < classes.size() && classes[c] != pyz) ++c;
+        if (c == classes.size()) classes.push_back(pyz);
+        hs[s].gclass = (int)c;
         hs[s].bbase = (int)bricks;
-        hs[s].binbase = (int)bins;
         hs[s].pbase = (int)parts;
         hs[s].lbase = (int)lcells;
         hs[s].k = ks[s];
         bricks += hs[s].g.nbricks;
-        bins += scene_bins(hs[s].g);
         parts += ks[s].n;
         lcells += ks[s].grid_count;
         if (bricks * 64 > INT_MAX || parts > e->max_particles || lcells > INT_MAX) {
@@ -1526,6 +1541,17 @@ int sorted_configure_batch(SortedEngine* e, const SimConsts* ks, int nscenes) {
             return -1;
         }
     }
+    // bins class by class (scene order within a class)
+    for (size_t c = 0; c < classes.size(); ++c)
+        for (int s = 0; s < nscenes; ++s)
+            if (hs[s].gclass == (int)c) {
+                hs[s].binbase = (int)bins;
+                bins += scene_bins(hs[s].g);
+                if (bins > INT_MAX / 2) {
+                    g_err = "batch exceeds the engine's capacity";
+                    return -1;
+                }
+            }
     drop_graphs(e);
     if (bins > INT_MAX / 2) {
         g_err = "batch exceeds the engine's capacity";
