@@ -495,6 +495,10 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     __shared__ int s_task[2];
     __shared__ LaneTable s_lt;
     constexpr int kPer = (kNA + TH - 1) / TH;  // arena slots per thread
+    // 128 threads: this thread's slot offsets in shared memory (entry
+    // [q][thread], written and read by that thread only), as in k_g2p_p2g1
+    constexpr bool kTab = TH == 128;
+    __shared__ int s_off[kTab ? kPer : 1][kTab ? TH : 1];
 
     clear_dirty(d, cur ^ 1);
 
@@ -509,16 +513,29 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         s_task[1] = claim_task(d, kCtrP2G2);
     }
 
-    // offsets of this thread's arena slots for the geometry of scene
-    // off_scene (recomputed when a batch's task belongs to another scene)
-    int off[kPer];
+    // offsets of this thread's arena slots for geometry class off_class
+    // (recomputed when a batch's task belongs to another class)
+    int off_r[kTab ? 1 : kPer];
+    auto set_offsets = [&](const Geo& g) {
+        if constexpr (kTab) {
+#pragma unroll
+            for (int q = 0; q < kPer; ++q)
+                s_off[q][threadIdx.x] = slot_offset<kA, kSXA, kSYA, 1, kNA>(g, (int)threadIdx.x + q * TH);
+        } else {
+            slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPer>(g, off_r);
+        }
+    };
+    auto off = [&](int q) -> int {
+        if constexpr (kTab) return s_off[q][threadIdx.x];
+        else return off_r[q];
+    };
     int off_class = one.gclass;
-    slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPer>(one.g, off);
+    set_offsets(one.g);
     auto offsets_for = [&](int scene) {
         if (BATCH) {
             const Scene& ts = scene_ref<BATCH>(d, one, scene);
             if (ts.gclass != off_class) {
-                slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPer>(ts.g, off);
+                set_offsets(ts.g);
                 off_class = ts.gclass;
             }
         }
@@ -541,7 +558,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         const bool pair = (tk.bin & kPairBit) != 0;
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
-            const int o = task_offset(off[q], pair);
+            const int o = task_offset(off(q), pair);
             if (o >= 0) m[q] = __ldcg(grid + 4 * o + 3);
         }
     };
@@ -566,8 +583,9 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
             s_q[buf][0][li] = 0;
             s_q[buf][1][li] = 0;
             s_q[buf][2][li] = 0;
-            if (off[q] < 0) continue;  // unreachable: stencils stay inside the arena
-            int* c = grid + 4 * (off[q] & ~kPairSlot);
+            const int oq = off(q);
+            if (oq < 0) continue;  // unreachable: stencils stay inside the arena
+            int* c = grid + 4 * (oq & ~kPairSlot);
             if (q0) atomicAdd(c + 0, q0);
             if (q1) atomicAdd(c + 1, q1);
             if (q2) atomicAdd(c + 2, q2);
@@ -734,6 +752,14 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     __shared__ int s_task[2];
     constexpr int kPerA = DO_G2P ? (kNA + TH - 1) / TH : 1;  // g2p arena slots per thread
     constexpr int kPerB = (kNB + TH - 1) / TH;                // p2g_1 arena slots per thread
+    // 128 threads (one arena): the offsets of each thread's arena slots live
+    // in shared memory (entry [q][thread], written and read by that thread
+    // only) for the geometry class of the last task, which frees registers;
+    // the larger blocks keep the g2p offsets in registers and compute the
+    // p2g_1 ones at the flush (their spills grew with the tables).
+    constexpr bool kTab = TH == 128;
+    __shared__ int s_offB[kTab ? kPerB : 1][kTab ? TH : 1];
+    __shared__ int s_offA[kTab ? kPerA : 1][kTab ? TH : 1];
 
     const float4* __restrict__ gv_all = d.gv[src];
     int4* __restrict__ gdst_all = d.grid[dst];
@@ -748,17 +774,38 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         s_task[1] = claim_task(d, ctr);
     }
 
-    // offsets of this thread's g2p arena slots for the geometry of scene
-    // off_scene (recomputed when a batch's task belongs to another); the
-    // flush computes those of its touched p2g_1 slots
-    int offA[kPerA];
+    // offsets of this thread's arena slots for geometry class off_class /
+    // offB_class (recomputed when a batch's task belongs to another class)
+    int offA[kTab ? 1 : kPerA];
     int off_class = one.gclass;
-    if (DO_G2P) slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPerA>(one.g, offA);
+    auto offsetsA = [&](const Geo& g) {
+        if constexpr (kTab) {
+#pragma unroll
+            for (int q = 0; q < kPerA; ++q)
+                s_offA[q][threadIdx.x] = slot_offset<kA, kSXA, kSYA, 1, kNA>(g, (int)threadIdx.x + q * TH);
+        } else {
+            slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPerA>(g, offA);
+        }
+    };
+    auto offA_at = [&](int q) -> int {
+        if constexpr (kTab) return s_offA[q][threadIdx.x];
+        else return offA[q];
+    };
+    if (DO_G2P) offsetsA(one.g);
+    int offB_class = one.gclass;
+    auto offsetsB = [&](const Geo& g) {
+        if constexpr (kTab) {
+#pragma unroll
+            for (int q = 0; q < kPerB; ++q)
+                s_offB[q][threadIdx.x] = slot_offset<kB, kSXB, kSYB, 2, kNB>(g, (int)threadIdx.x + q * TH);
+        }
+    };
+    offsetsB(one.g);
     auto offsets_for = [&](int scene) {
         if (BATCH && DO_G2P) {
             const Scene& ts = scene_ref<BATCH>(d, one, scene);
             if (ts.gclass != off_class) {
-                slot_offsets<kA, kSXA, kSYA, 1, kNA, TH, kPerA>(ts.g, offA);
+                offsetsA(ts.g);
                 off_class = ts.gclass;
             }
         }
@@ -776,7 +823,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         const bool pair = (tk.bin & kPairBit) != 0;
 #pragma unroll
         for (int q = 0; q < kPerA; ++q) {
-            const int o = task_offset(offA[q], pair);
+            const int o = task_offset(offA_at(q), pair);
             if (o >= 0) cp_async16(&s_v[buf][(int)threadIdx.x + q * TH], gvsrc + o);
         }
         cp_async_commit();
@@ -784,6 +831,10 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     // flush the p2g_1 arena of task tk
     auto flush = [&](int buf, const Task& tk) {
         const Scene& ts = scene_ref<BATCH>(d, one, tk.scene);
+        if (kTab && BATCH && ts.gclass != offB_class) {
+            offsetsB(ts.g);
+            offB_class = ts.gclass;
+        }
         int* gdst = reinterpret_cast<int*>(gdst_all + (size_t)brick_base<BATCH>(ts) * 64 + tk.abase);
 #pragma unroll
         for (int q = 0; q < kPerB; ++q) {
@@ -796,7 +847,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
             s_a[buf][1][li] = 0;
             s_a[buf][2][li] = 0;
             s_a[buf][3][li] = 0;
-            const int o = slot_offset<kB, kSXB, kSYB, 2, kNB>(ts.g, li);
+            const int o = kTab ? s_offB[q][threadIdx.x] : slot_offset<kB, kSXB, kSYB, 2, kNB>(ts.g, li);
             if (o < 0) continue;  // unreachable: stencils stay inside the arena
             int* c = gdst + 4 * (o & ~kPairSlot);
             if (q0) atomicAdd(c + 0, q0);
