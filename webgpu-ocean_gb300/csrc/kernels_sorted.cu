@@ -499,6 +499,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     // [q][thread], written and read by that thread only), as in k_g2p_p2g1
     constexpr bool kTab = TH == 128;
     __shared__ int s_off[kTab ? kPer : 1][kTab ? TH : 1];
+    __shared__ Task s_cur;  // 128 threads: the task being computed
 
     clear_dirty(d, cur ^ 1);
 
@@ -613,19 +614,23 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         if (threadIdx.x == 0) s_task[cb] = claim_task(d, kCtrP2G2);
         int m_next[kPer];
         float fm_next = 0.0f;
-        if (DB) {
+        if (DB) {  // the next task's masses: loads issued before the flush, stored after it
             load_mass(t_next, m_next, fm_next);
             if (have_prev) flush(buf ^ 1, prev);
+            store_mass(buf ^ 1, m_next, fm_next);
         } else {  // one arena: flush task it-1's, load this task's, then wait
             if (have_prev) flush(0, prev);
             int m[kPer];
             float fm;
             load_mass(t, m, fm);
             store_mass(0, m, fm);
+            if (kTab && threadIdx.x == 0) s_cur = d.tasks[task_slot(d, nbig, t)];
             __syncthreads();
         }
 
-        const Task task = d.tasks[task_slot(d, nbig, t)];
+        Task task_r;
+        if (!kTab) task_r = d.tasks[task_slot(d, nbig, t)];
+        const Task& task = kTab ? s_cur : task_r;
         const Scene& sc = scene_ref<BATCH>(d, one, task.scene);
         const Geo& g = sc.g;
         const SimConsts& k = sc.k;
@@ -679,7 +684,6 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
                     });
             }
         }
-        if (DB) store_mass(buf ^ 1, m_next, fm_next);
         prev = task;
         have_prev = true;
         t = t_next;
@@ -760,6 +764,10 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     constexpr bool kTab = TH == 128;
     __shared__ int s_offB[kTab ? kPerB : 1][kTab ? TH : 1];
     __shared__ int s_offA[kTab ? kPerA : 1][kTab ? TH : 1];
+    // 128 threads, batch: the task being computed (fewer spills; a single
+    // scene's kernel spilled more with it)
+    constexpr bool kCur = kTab && BATCH;
+    __shared__ Task s_cur;
 
     const float4* __restrict__ gv_all = d.gv[src];
     int4* __restrict__ gdst_all = d.grid[dst];
@@ -893,11 +901,14 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
                 flush(0, prev);
             }
             prefetch(t, 0);
+            if (kCur && threadIdx.x == 0) s_cur = d.tasks[task_slot(d, nbig, t)];
             if (DO_G2P) cp_async_wait_all();
             __syncthreads();
         }
 
-        const Task task = d.tasks[task_slot(d, nbig, t)];
+        Task task_r;
+        if (!kCur) task_r = d.tasks[task_slot(d, nbig, t)];
+        const Task& task = kCur ? s_cur : task_r;
         const Scene& sc = scene_ref<BATCH>(d, one, task.scene);
         const Geo& g = sc.g;
         const SimConsts& k = sc.k;
