@@ -499,7 +499,9 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     // [q][thread], written and read by that thread only), as in k_g2p_p2g1
     constexpr bool kTab = TH == 128;
     __shared__ int s_off[kTab ? kPer : 1][kTab ? TH : 1];
-    __shared__ Task s_cur;  // 128 threads: the task being computed
+    // the task being computed (slot it & 1 of a double-buffered kernel: the
+    // next task's record is written while this one computes)
+    __shared__ Task s_cur[NB];
 
     clear_dirty(d, cur ^ 1);
 
@@ -599,6 +601,7 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
         float fm;
         load_mass(t, m, fm);
         store_mass(0, m, fm);
+        if (threadIdx.x == 0 && t < ntasks) s_cur[0] = d.tasks[task_slot(d, nbig, t)];
     }
     Task prev;
     prev.bin = -1;
@@ -618,19 +621,18 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
             load_mass(t_next, m_next, fm_next);
             if (have_prev) flush(buf ^ 1, prev);
             store_mass(buf ^ 1, m_next, fm_next);
+            if (threadIdx.x == 0 && t_next < ntasks) s_cur[buf ^ 1] = d.tasks[task_slot(d, nbig, t_next)];
         } else {  // one arena: flush task it-1's, load this task's, then wait
             if (have_prev) flush(0, prev);
             int m[kPer];
             float fm;
             load_mass(t, m, fm);
             store_mass(0, m, fm);
-            if (kTab && threadIdx.x == 0) s_cur = d.tasks[task_slot(d, nbig, t)];
+            if (threadIdx.x == 0) s_cur[0] = d.tasks[task_slot(d, nbig, t)];
             __syncthreads();
         }
 
-        Task task_r;
-        if (!kTab) task_r = d.tasks[task_slot(d, nbig, t)];
-        const Task& task = kTab ? s_cur : task_r;
+        const Task& task = s_cur[buf];
         const Scene& sc = scene_ref<BATCH>(d, one, task.scene);
         const Geo& g = sc.g;
         const SimConsts& k = sc.k;
@@ -764,10 +766,12 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     constexpr bool kTab = TH == 128;
     __shared__ int s_offB[kTab ? kPerB : 1][kTab ? TH : 1];
     __shared__ int s_offA[kTab ? kPerA : 1][kTab ? TH : 1];
-    // 128 threads, batch: the task being computed (fewer spills; a single
-    // scene's kernel spilled more with it)
-    constexpr bool kCur = kTab && BATCH;
-    __shared__ Task s_cur;
+    // the task being computed, read from shared memory (slot it & 1 of a
+    // double-buffered kernel: the next task's record is written while this
+    // one computes); a single scene's 128-thread kernel keeps it in
+    // registers (it spilled more with it)
+    constexpr bool kCur = BATCH || DB;
+    __shared__ Task s_cur[kCur ? NB : 1];
 
     const float4* __restrict__ gv_all = d.gv[src];
     int4* __restrict__ gdst_all = d.grid[dst];
@@ -878,7 +882,10 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
     };
 
     int t = s_task[0];
-    if (DB) prefetch(t, 0);
+    if (DB) {
+        prefetch(t, 0);
+        if (threadIdx.x == 0 && t < ntasks) s_cur[0] = d.tasks[task_slot(d, nbig, t)];
+    }
     bool have_prev = false;
     Task prev;
     prev.bin = -1;
@@ -895,20 +902,21 @@ __global__ void __launch_bounds__(TH, 1024 / TH)
             if (have_prev && prev.bin >= 0) mark(buf ^ 1, prev);
             prefetch(t_next, buf ^ 1);
             if (have_prev && prev.bin >= 0) flush(buf ^ 1, prev);
+            if (threadIdx.x == 0 && t_next < ntasks) s_cur[buf ^ 1] = d.tasks[task_slot(d, nbig, t_next)];
         } else {  // one arena: flush task it-1's, copy in this task's, then wait
             if (have_prev && prev.bin >= 0) {
                 mark(0, prev);
                 flush(0, prev);
             }
             prefetch(t, 0);
-            if (kCur && threadIdx.x == 0) s_cur = d.tasks[task_slot(d, nbig, t)];
+            if (kCur && threadIdx.x == 0) s_cur[0] = d.tasks[task_slot(d, nbig, t)];
             if (DO_G2P) cp_async_wait_all();
             __syncthreads();
         }
 
         Task task_r;
         if (!kCur) task_r = d.tasks[task_slot(d, nbig, t)];
-        const Task& task = kCur ? s_cur : task_r;
+        const Task& task = kCur ? s_cur[buf] : task_r;
         const Scene& sc = scene_ref<BATCH>(d, one, task.scene);
         const Geo& g = sc.g;
         const SimConsts& k = sc.k;
