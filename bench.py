@@ -312,10 +312,10 @@ def run_reference(args) -> None:
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
 # capture of `bench.py --quick` on this workload: its posvel-writing variant
 # (profiles/k_g2p_p2g1_1M_128.md).
-MEASURED_TRAFFIC_PER_LAUNCH = {"sorted_g2p_p2g_1": 96.26e6}
+MEASURED_TRAFFIC_PER_LAUNCH = {"sorted_g2p_p2g_1": 93.59e6}
 # ncu smsp__inst_executed.sum of one launch at the early dam-break state
 # (profiles/k_g2p_p2g1_1M_128.md): the instruction-issue roofline.
-MEASURED_WARP_INSTRUCTIONS_PER_LAUNCH = {"sorted_g2p_p2g_1": 69.55e6}
+MEASURED_WARP_INSTRUCTIONS_PER_LAUNCH = {"sorted_g2p_p2g_1": 70.22e6}
 
 
 def algorithmic_bytes(kernel: str, n: int, cells: int) -> float | None:
