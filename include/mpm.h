@@ -215,8 +215,10 @@ int mpm_set_graph(mpm_sim* sim, int enable);
 
 /* Sorted engine: most particles per task.  A bin (4x4x4-cell brick) with
  * more particles is split into several tasks, so that small scenes still
- * spread over every SM.  0 (the default) picks it from the particle count;
- * otherwise 64 ... 2^30.  Results do not depend on it. */
+ * spread over every SM.  0 (the default) picks it from the particle count:
+ * particles per resident task-kernel block, rounded to the nearest power of
+ * two within 64 ... 1024; otherwise 64 ... 2^30.  Results do not depend on
+ * it. */
 int mpm_set_task_size(mpm_sim* sim, int task_size);
 int mpm_get_task_size(const mpm_sim* sim);
 /* Sorted engine: tasks of at least `min_particles` particles spread them over
